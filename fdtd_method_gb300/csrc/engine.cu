@@ -1,0 +1,673 @@
+// C-ABI layer of the engine: handle lifetime, storage, step scheduling,
+// host transfers, sources and diagnostics.  See include/fdtd_gb300.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fdtd_gb300.h"
+#include "engine_internal.h"
+
+using namespace fdtd;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? FDTD_ERR_OUT_OF_MEMORY : FDTD_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define FDTD_CUDA(call, what)                   \
+  do {                                          \
+    cudaError_t e_ = (call);                    \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+// Speed of light and pi as the reference defines them (include/Constants.h:6,11).
+constexpr double kC = 3e10;
+constexpr double kPi = 3.14159265358;
+
+constexpr int64_t kStagingElems = int64_t(1) << 24;  // 16 Mi doubles = 128 MiB
+constexpr int kMaxDiagBlocks = 152 * 8;
+
+struct HostSource {
+  fdtd_source s;  // table pointers are not kept
+  std::vector<double> gx, gy, gz, amp;
+};
+
+Coef split_coef(double c) {
+  const float h = (float)c;
+  return Coef{h, (float)(c - (double)h)};
+}
+
+}  // namespace
+
+struct fdtd_handle {
+  fdtd_params p{};
+  double dt = 0;
+  int precision = 0;
+  Form form = Form::F64;
+  Grid g{};
+  int device = 0;
+  // {cEx, cEy, cEz, cBx, cBy, cBz, cJ}, src/FDTD_kokkos/FDTD_kokkos.cpp:45-55
+  double coef[7] = {0, 0, 0, 0, 0, 0, 0};
+  CoefSet cs{};
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+
+  // Storage.  FP64: field[0..8] are double arrays (E, B, J).  Other forms:
+  // field[0..5] hold the E/B words of the form, lo[0..5] the compensation
+  // words (FP32_COMP), jf[0..2] FP32 current arrays (allocated on first use).
+  void* field[9] = {nullptr};
+  int8_t* lo[6] = {nullptr};
+  float* jf[3] = {nullptr};
+  bool dense_j = false;  // the E update reads the dense J arrays
+  int fp16_exp[6] = {0, 0, 0, 0, 0, 0};
+
+  // Sources.
+  std::vector<HostSource> sources;
+  DevSource* d_src = nullptr;
+  double* d_tables = nullptr;
+  float* d_tables_f = nullptr;
+  int64_t* d_step = nullptr;
+  int64_t host_step = 0;
+
+  // Scratch.
+  double* d_staging = nullptr;
+  double* d_partials = nullptr;
+  double* d_diag_out = nullptr;
+
+  std::vector<void*> allocations;
+
+  // Kernel timing: event pairs recorded around launches while enabled.
+  struct TimedLaunch {
+    cudaEvent_t start, stop;
+    int kind;
+  };
+  bool timing = false;
+  std::vector<TimedLaunch> timed;
+  std::vector<cudaEvent_t> event_pool;
+
+  StateView view() const {
+    StateView v{};
+    v.form = form;
+    v.g = g;
+    for (int c = 0; c < 6; ++c) v.f64[c] = (form == Form::F64) ? (double*)field[c] : nullptr;
+    for (int c = 0; c < 6; ++c) {
+      v.s32.v[c] = (float*)field[c];
+      v.s32c.hi[c] = (float*)field[c];
+      v.s32c.lo[c] = lo[c];
+      v.s16.v[c] = (__half*)field[c];
+      v.s16.scale[c] = std::ldexp(1.0f, fp16_exp[c]);
+      v.s16.inv_scale[c] = std::ldexp(1.0f, -fp16_exp[c]);
+    }
+    return v;
+  }
+  SourceSet source_set() const {
+    SourceSet ss{};
+    ss.count = (int)sources.size();
+    ss.src = d_src;
+    ss.tables = d_tables;
+    ss.step = d_step;
+    return ss;
+  }
+};
+
+namespace {
+
+cudaError_t dev_alloc(fdtd_handle* h, void** ptr, size_t bytes) {
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e == cudaSuccess) h->allocations.push_back(*ptr);
+  return e;
+}
+
+void release(fdtd_handle* h) {
+  if (!h) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (void* p : h->allocations) cudaFree(p);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  cudaSetDevice(prev);
+  delete h;
+}
+
+size_t elem_bytes(Form f) {
+  switch (f) {
+    case Form::F64: return 8;
+    case Form::F32: return 4;
+    case Form::F32C: return 4;
+    case Form::F16: return 2;
+  }
+  return 8;
+}
+
+int ensure_staging(fdtd_handle* h) {
+  if (!h->d_staging)
+    FDTD_CUDA(dev_alloc(h, (void**)&h->d_staging, sizeof(double) * kStagingElems), "staging buffer");
+  return FDTD_OK;
+}
+
+int ensure_jf(fdtd_handle* h) {
+  if (h->form == Form::F64 || h->jf[0]) return FDTD_OK;
+  for (int c = 0; c < 3; ++c) {
+    FDTD_CUDA(dev_alloc(h, (void**)&h->jf[c], sizeof(float) * h->g.cells), "current arrays");
+    FDTD_CUDA(cudaMemsetAsync(h->jf[c], 0, sizeof(float) * h->g.cells, h->stream), "zero current");
+  }
+  return FDTD_OK;
+}
+
+// Uploads the source tables after any change to the source list.
+int upload_sources(fdtd_handle* h) {
+  std::vector<double> tables;
+  std::vector<DevSource> ds;
+  for (const HostSource& hs : h->sources) {
+    DevSource d{};
+    d.comp_mask = hs.s.comp_mask;
+    d.i0 = hs.s.i0; d.j0 = hs.s.j0; d.k0 = hs.s.k0;
+    d.ni = hs.s.ni; d.nj = hs.s.nj; d.nk = hs.s.nk;
+    d.gx_off = (int64_t)tables.size(); tables.insert(tables.end(), hs.gx.begin(), hs.gx.end());
+    d.gy_off = (int64_t)tables.size(); tables.insert(tables.end(), hs.gy.begin(), hs.gy.end());
+    d.gz_off = (int64_t)tables.size(); tables.insert(tables.end(), hs.gz.begin(), hs.gz.end());
+    d.amp_off = (int64_t)tables.size(); tables.insert(tables.end(), hs.amp.begin(), hs.amp.end());
+    d.n_amp = (int64_t)hs.amp.size();
+    ds.push_back(d);
+  }
+  // The previous tables may still be read by queued kernels.
+  FDTD_CUDA(cudaStreamSynchronize(h->stream), "synchronize before source upload");
+  if (h->d_src) { cudaFree(h->d_src); h->d_src = nullptr; }
+  if (h->d_tables) { cudaFree(h->d_tables); h->d_tables = nullptr; }
+  if (h->d_tables_f) { cudaFree(h->d_tables_f); h->d_tables_f = nullptr; }
+  if (ds.empty()) return FDTD_OK;
+  FDTD_CUDA(cudaMalloc(&h->d_src, sizeof(DevSource) * ds.size()), "source descriptors");
+  FDTD_CUDA(cudaMalloc(&h->d_tables, sizeof(double) * tables.size()), "source tables");
+  FDTD_CUDA(cudaMalloc(&h->d_tables_f, sizeof(float) * tables.size()), "source tables (fp32)");
+  FDTD_CUDA(cudaMemcpy(h->d_src, ds.data(), sizeof(DevSource) * ds.size(), cudaMemcpyHostToDevice),
+            "upload source descriptors");
+  FDTD_CUDA(cudaMemcpy(h->d_tables, tables.data(), sizeof(double) * tables.size(),
+                       cudaMemcpyHostToDevice),
+            "upload source tables");
+  FDTD_CUDA(launch_to_f32(h->d_tables, h->d_tables_f, (int64_t)tables.size(), h->stream),
+            "convert source tables");
+  FDTD_CUDA(cudaStreamSynchronize(h->stream), "source upload");
+  return FDTD_OK;
+}
+
+struct DeviceGuard {
+  int prev = 0;
+  bool ok = false;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess) ok = true;
+  }
+  ~DeviceGuard() {
+    if (ok) cudaSetDevice(prev);
+  }
+};
+
+cudaEvent_t take_event(fdtd_handle* h) {
+  if (!h->event_pool.empty()) {
+    cudaEvent_t e = h->event_pool.back();
+    h->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+// Brackets one launch with events when kernel timing is on.
+struct LaunchTimer {
+  fdtd_handle* h;
+  cudaEvent_t start = nullptr;
+  int kind;
+  LaunchTimer(fdtd_handle* hh, int k) : h(hh), kind(k) {
+    if (h->timing && (start = take_event(h))) cudaEventRecord(start, h->stream);
+  }
+  void done() {
+    if (!start) return;
+    cudaEvent_t stop = take_event(h);
+    if (!stop) {
+      h->event_pool.push_back(start);
+      return;
+    }
+    cudaEventRecord(stop, h->stream);
+    h->timed.push_back({start, stop, kind});
+  }
+};
+
+// B update with `apps` applications of the curl term; `inc` bumps the
+// device step counter (the sweep that completes a step).
+int run_b(fdtd_handle* h, int apps, bool inc) {
+  LaunchTimer lt(h, apps == 2 ? FDTD_KERNEL_B_DOUBLE : FDTD_KERNEL_B_HALF);
+  int64_t* step_inc = inc ? h->d_step : nullptr;
+  cudaError_t e = cudaSuccess;
+  if (h->form == Form::F64) {
+    Fp64Fields F;
+    for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c];
+    e = launch_b_fp64(h->g, F, &h->coef[3], apps, step_inc, h->stream);
+  } else {
+    StateView v = h->view();
+    switch (h->form) {
+      case Form::F32: e = launch_b_f32(h->g, v.s32, h->cs, apps, step_inc, h->stream); break;
+      case Form::F32C: e = launch_b_f32(h->g, v.s32c, h->cs, apps, step_inc, h->stream); break;
+      case Form::F16: e = launch_b_f32(h->g, v.s16, h->cs, apps, step_inc, h->stream); break;
+      default: break;
+    }
+  }
+  lt.done();
+  if (e != cudaSuccess) return cuda_fail(e, "B update launch");
+  return FDTD_OK;
+}
+
+int run_e(fdtd_handle* h) {
+  LaunchTimer lt(h, FDTD_KERNEL_E);
+  SourceSet ss = h->source_set();
+  cudaError_t e = cudaSuccess;
+  if (h->form == Form::F64) {
+    Fp64Fields F;
+    for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c];
+    e = launch_e_fp64(h->g, F, &h->coef[0], h->coef[6], h->dense_j, ss, h->stream);
+  } else {
+    StateView v = h->view();
+    const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
+    const bool dj = h->dense_j && h->jf[0];
+    switch (h->form) {
+      case Form::F32: e = launch_e_f32(h->g, v.s32, J, dj, h->cs, ss, h->d_tables_f, h->stream); break;
+      case Form::F32C: e = launch_e_f32(h->g, v.s32c, J, dj, h->cs, ss, h->d_tables_f, h->stream); break;
+      case Form::F16: e = launch_e_f32(h->g, v.s16, J, dj, h->cs, ss, h->d_tables_f, h->stream); break;
+      default: break;
+    }
+  }
+  lt.done();
+  if (e != cudaSuccess) return cuda_fail(e, "E update launch");
+  return FDTD_OK;
+}
+
+int check_handle(fdtd_handle* h) {
+  if (!h) return fail(FDTD_ERR_INVALID_ARGUMENT, "null handle");
+  return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fdtd_last_error(void) { return g_last_error.c_str(); }
+int fdtd_abi_version(void) { return FDTD_ABI_VERSION; }
+
+int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle** out) {
+  if (!params || !out) return fail(FDTD_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  // src/FDTD_kokkos/FDTD_kokkos.cpp:7-12
+  if (params->Ni <= 0 || params->Nj <= 0 || params->Nk <= 0 || !(dt > 0))
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "ERROR: invalid parameters");
+  if (precision < FDTD_PRECISION_FP64 || precision > FDTD_PRECISION_FP16_SCALED)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid precision");
+
+  fdtd_handle* h = new fdtd_handle();
+  h->p = *params;
+  h->dt = dt;
+  h->precision = precision;
+  h->form = (Form)precision;
+  h->g.Ni = params->Ni;
+  h->g.Nj = params->Nj;
+  h->g.Nk = params->Nk;
+  h->g.plane = (int64_t)params->Ni * params->Nj;
+  h->g.cells = h->g.plane * params->Nk;
+  cudaGetDevice(&h->device);
+
+  // src/FDTD_kokkos/FDTD_kokkos.cpp:45-55
+  const double cdt = kC * dt;
+  h->coef[0] = cdt / params->dx;
+  h->coef[1] = cdt / params->dy;
+  h->coef[2] = cdt / params->dz;
+  h->coef[3] = cdt / (2.0 * params->dx);
+  h->coef[4] = cdt / (2.0 * params->dy);
+  h->coef[5] = cdt / (2.0 * params->dz);
+  h->coef[6] = -4.0 * kPi * dt;
+  for (int a = 0; a < 3; ++a) {
+    h->cs.ce[a] = split_coef(h->coef[a]);
+    h->cs.cb[a] = split_coef(h->coef[3 + a]);
+  }
+  h->cs.cj = split_coef(h->coef[6]);
+  if (h->form != Form::F32C) {  // only the compensated form carries coefficient lo parts
+    for (int a = 0; a < 3; ++a) h->cs.ce[a].lo = h->cs.cb[a].lo = 0.f;
+    h->cs.cj.lo = 0.f;
+  }
+
+  cudaError_t e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    int rc = cuda_fail(e, "stream creation");
+    delete h;
+    return rc;
+  }
+  h->stream = h->own_stream;
+
+  const size_t eb = elem_bytes(h->form);
+  const int nfields = (h->form == Form::F64) ? 9 : 6;
+  for (int c = 0; c < nfields; ++c) {
+    e = dev_alloc(h, &h->field[c], eb * h->g.cells);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->field[c], 0, eb * h->g.cells, h->stream);
+    if (e != cudaSuccess) {
+      int rc = cuda_fail(e, "field allocation");
+      release(h);
+      return rc;
+    }
+  }
+  if (h->form == Form::F32C) {
+    for (int c = 0; c < 6; ++c) {
+      e = dev_alloc(h, (void**)&h->lo[c], h->g.cells);
+      if (e == cudaSuccess) e = cudaMemsetAsync(h->lo[c], 0, h->g.cells, h->stream);
+      if (e != cudaSuccess) {
+        int rc = cuda_fail(e, "compensation allocation");
+        release(h);
+        return rc;
+      }
+    }
+  }
+  e = dev_alloc(h, (void**)&h->d_step, sizeof(int64_t));
+  if (e == cudaSuccess) e = dev_alloc(h, (void**)&h->d_partials, sizeof(double) * kDiagValues * kMaxDiagBlocks);
+  if (e == cudaSuccess) e = dev_alloc(h, (void**)&h->d_diag_out, sizeof(double) * kDiagValues);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->d_step, 0, sizeof(int64_t), h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    int rc = cuda_fail(e, "handle set-up");
+    release(h);
+    return rc;
+  }
+  *out = h;
+  return FDTD_OK;
+}
+
+int fdtd_destroy(fdtd_handle* h) {
+  if (!h) return FDTD_OK;
+  // Source buffers are not in `allocations` (they are replaced on update).
+  DeviceGuard dg(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->d_src) cudaFree(h->d_src);
+  if (h->d_tables) cudaFree(h->d_tables);
+  if (h->d_tables_f) cudaFree(h->d_tables_f);
+  h->d_src = nullptr;
+  h->d_tables = nullptr;
+  h->d_tables_f = nullptr;
+  for (auto& t : h->timed) {
+    cudaEventDestroy(t.start);
+    cudaEventDestroy(t.stop);
+  }
+  for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
+  release(h);
+  return FDTD_OK;
+}
+
+int fdtd_set_kernel_timing(fdtd_handle* h, int enabled) {
+  if (int rc = check_handle(h)) return rc;
+  h->timing = enabled != 0;
+  return FDTD_OK;
+}
+
+int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t launches[FDTD_KERNEL_KINDS]) {
+  if (int rc = check_handle(h)) return rc;
+  if (!ms || !launches) return fail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  DeviceGuard dg(h->device);
+  FDTD_CUDA(cudaStreamSynchronize(h->stream), "synchronize for kernel times");
+  for (int k = 0; k < FDTD_KERNEL_KINDS; ++k) {
+    ms[k] = 0.0;
+    launches[k] = 0;
+  }
+  for (auto& t : h->timed) {
+    float m = 0.f;
+    if (cudaEventElapsedTime(&m, t.start, t.stop) == cudaSuccess) {
+      ms[t.kind] += m;
+      launches[t.kind] += 1;
+    }
+    h->event_pool.push_back(t.start);
+    h->event_pool.push_back(t.stop);
+  }
+  h->timed.clear();
+  return FDTD_OK;
+}
+
+int fdtd_step(fdtd_handle* h, int64_t n) {
+  if (int rc = check_handle(h)) return rc;
+  if (n < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "negative step count");
+  if (n == 0) return FDTD_OK;
+  DeviceGuard dg(h->device);
+  // src/FDTD_kokkos/FDTD_kokkos.cpp:91-104 repeated n times; the trailing B
+  // half step of one step and the leading one of the next share one sweep.
+  if (int rc = run_b(h, 1, false)) return rc;
+  for (int64_t s = 0; s < n; ++s) {
+    if (int rc = run_e(h)) return rc;
+    if (int rc = run_b(h, s + 1 < n ? 2 : 1, true)) return rc;
+  }
+  h->host_step += n;
+  return FDTD_OK;
+}
+
+int fdtd_update_fields(fdtd_handle* h) { return fdtd_step(h, 1); }
+
+int fdtd_zeroed_currents(fdtd_handle* h) {
+  if (int rc = check_handle(h)) return rc;
+  DeviceGuard dg(h->device);
+  // src/FDTD_kokkos/FDTD_kokkos.cpp:69-73.  The E update keeps reading J if a
+  // J address was handed out (the holder may write it again).
+  if (h->form == Form::F64) {
+    for (int c = 6; c < 9; ++c)
+      FDTD_CUDA(cudaMemsetAsync(h->field[c], 0, sizeof(double) * h->g.cells, h->stream), "zero J");
+  } else if (h->jf[0]) {
+    for (int c = 0; c < 3; ++c)
+      FDTD_CUDA(cudaMemsetAsync(h->jf[c], 0, sizeof(float) * h->g.cells, h->stream), "zero J");
+    h->dense_j = false;
+  }
+  return FDTD_OK;
+}
+
+int fdtd_get_field(fdtd_handle* h, int comp, double** device_ptr) {
+  if (int rc = check_handle(h)) return rc;
+  if (!device_ptr) return fail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  if (comp < FDTD_EX || comp > FDTD_JZ)
+    return fail(FDTD_ERR_LOGIC, "ERROR: Invalid field component");  // FDTD_kokkos.cpp:87
+  if (h->form != Form::F64)
+    return fail(FDTD_ERR_UNSUPPORTED, "device field addresses are FP64-only; use fdtd_copy_field_*");
+  if (comp >= FDTD_JX) h->dense_j = true;
+  *device_ptr = (double*)h->field[comp];
+  return FDTD_OK;
+}
+
+int fdtd_copy_field_to_host(fdtd_handle* h, int comp, double* host, size_t n) {
+  if (int rc = check_handle(h)) return rc;
+  if (comp < FDTD_EX || comp > FDTD_JZ) return fail(FDTD_ERR_LOGIC, "ERROR: Invalid field component");
+  if (!host || (int64_t)n != h->g.cells) return fail(FDTD_ERR_INVALID_ARGUMENT, "host buffer size mismatch");
+  DeviceGuard dg(h->device);
+  if (h->form == Form::F64) {
+    FDTD_CUDA(cudaMemcpyAsync(host, h->field[comp], sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream),
+              "copy field to host");
+    FDTD_CUDA(cudaStreamSynchronize(h->stream), "copy field to host");
+    return FDTD_OK;
+  }
+  if (comp >= FDTD_JX && !h->jf[0]) {  // never written: zero
+    std::memset(host, 0, sizeof(double) * n);
+    return FDTD_OK;
+  }
+  if (int rc = ensure_staging(h)) return rc;
+  StateView v = h->view();
+  for (int64_t off = 0; off < (int64_t)n; off += kStagingElems) {
+    const int64_t m = std::min<int64_t>(kStagingElems, (int64_t)n - off);
+    cudaError_t e;
+    if (comp >= FDTD_JX) {
+      // J is stored as FP32: widen on the host side of the copy.
+      std::vector<float> tmp(m);
+      e = cudaMemcpyAsync(tmp.data(), h->jf[comp - FDTD_JX] + off, sizeof(float) * m,
+                          cudaMemcpyDeviceToHost, h->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "copy current to host");
+      for (int64_t t = 0; t < m; ++t) host[off + t] = tmp[t];
+      continue;
+    }
+    e = launch_export(v, comp, h->d_staging, off, m, h->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(host + off, h->d_staging, sizeof(double) * m, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "copy field to host");
+  }
+  return FDTD_OK;
+}
+
+int fdtd_copy_field_from_host(fdtd_handle* h, int comp, const double* host, size_t n) {
+  if (int rc = check_handle(h)) return rc;
+  if (comp < FDTD_EX || comp > FDTD_JZ) return fail(FDTD_ERR_LOGIC, "ERROR: Invalid field component");
+  if (!host || (int64_t)n != h->g.cells) return fail(FDTD_ERR_INVALID_ARGUMENT, "host buffer size mismatch");
+  DeviceGuard dg(h->device);
+  if (h->form == Form::F64) {
+    FDTD_CUDA(cudaMemcpyAsync(h->field[comp], host, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream),
+              "copy field from host");
+    FDTD_CUDA(cudaStreamSynchronize(h->stream), "copy field from host");
+    if (comp >= FDTD_JX) h->dense_j = true;
+    return FDTD_OK;
+  }
+  if (int rc = ensure_staging(h)) return rc;
+  if (comp >= FDTD_JX) {
+    if (int rc = ensure_jf(h)) return rc;
+    h->dense_j = true;
+  }
+  StateView v = h->view();
+  for (int64_t off = 0; off < (int64_t)n; off += kStagingElems) {
+    const int64_t m = std::min<int64_t>(kStagingElems, (int64_t)n - off);
+    cudaError_t e = cudaMemcpyAsync(h->d_staging, host + off, sizeof(double) * m,
+                                    cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+      if (comp >= FDTD_JX) e = launch_to_f32(h->d_staging, h->jf[comp - FDTD_JX] + off, m, h->stream);
+      else e = launch_import(v, comp, h->d_staging, off, m, h->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "copy field from host");
+  }
+  return FDTD_OK;
+}
+
+int fdtd_add_source(fdtd_handle* h, const fdtd_source* src, int* index) {
+  if (int rc = check_handle(h)) return rc;
+  if (!src) return fail(FDTD_ERR_INVALID_ARGUMENT, "null source");
+  if (src->comp_mask <= 0 || src->comp_mask > 7) return fail(FDTD_ERR_INVALID_ARGUMENT, "source comp_mask must be 1..7");
+  if (src->ni <= 0 || src->nj <= 0 || src->nk <= 0 || src->ni > h->g.Ni || src->nj > h->g.Nj ||
+      src->nk > h->g.Nk)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "source box extents must be in 1..N per axis");
+  if (src->i0 < 0 || src->i0 >= h->g.Ni || src->j0 < 0 || src->j0 >= h->g.Nj || src->k0 < 0 ||
+      src->k0 >= h->g.Nk)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "source box origin outside the grid");
+  if (!src->gx || !src->gy || !src->gz || src->n_amp < 0 || (src->n_amp > 0 && !src->amp))
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "source tables missing");
+  if ((int)h->sources.size() >= kMaxSources) return fail(FDTD_ERR_INVALID_ARGUMENT, "too many sources");
+  DeviceGuard dg(h->device);
+  HostSource hs;
+  hs.s = *src;
+  hs.s.gx = hs.s.gy = hs.s.gz = hs.s.amp = nullptr;
+  hs.gx.assign(src->gx, src->gx + src->ni);
+  hs.gy.assign(src->gy, src->gy + src->nj);
+  hs.gz.assign(src->gz, src->gz + src->nk);
+  if (src->n_amp > 0) hs.amp.assign(src->amp, src->amp + src->n_amp);
+  h->sources.push_back(std::move(hs));
+  if (int rc = upload_sources(h)) {
+    h->sources.pop_back();
+    return rc;
+  }
+  if (index) *index = (int)h->sources.size() - 1;
+  return FDTD_OK;
+}
+
+int fdtd_clear_sources(fdtd_handle* h) {
+  if (int rc = check_handle(h)) return rc;
+  DeviceGuard dg(h->device);
+  h->sources.clear();
+  return upload_sources(h);
+}
+
+int fdtd_get_step(fdtd_handle* h, int64_t* step) {
+  if (int rc = check_handle(h)) return rc;
+  if (!step) return fail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  *step = h->host_step;
+  return FDTD_OK;
+}
+
+int fdtd_set_step(fdtd_handle* h, int64_t step) {
+  if (int rc = check_handle(h)) return rc;
+  if (step < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "negative step");
+  DeviceGuard dg(h->device);
+  FDTD_CUDA(launch_set_i64(h->d_step, step, h->stream), "set step");
+  h->host_step = step;
+  return FDTD_OK;
+}
+
+int fdtd_field_sums(fdtd_handle* h, double out[FDTD_DIAG_COUNT]) {
+  if (int rc = check_handle(h)) return rc;
+  if (!out) return fail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  DeviceGuard dg(h->device);
+  const int nb = diag_blocks_for(h->g.cells, kMaxDiagBlocks);
+  FDTD_CUDA(launch_field_sums(h->view(), h->d_partials, nb, h->d_diag_out, h->stream), "field sums");
+  FDTD_CUDA(cudaMemcpyAsync(out, h->d_diag_out, sizeof(double) * kDiagValues, cudaMemcpyDeviceToHost,
+                            h->stream),
+            "field sums readback");
+  FDTD_CUDA(cudaStreamSynchronize(h->stream), "field sums");
+  return FDTD_OK;
+}
+
+int fdtd_get_params(fdtd_handle* h, fdtd_params* params, double* dt, int* precision) {
+  if (int rc = check_handle(h)) return rc;
+  if (params) *params = h->p;
+  if (dt) *dt = h->dt;
+  if (precision) *precision = h->precision;
+  return FDTD_OK;
+}
+
+int fdtd_set_stream(fdtd_handle* h, void* stream) {
+  if (int rc = check_handle(h)) return rc;
+  DeviceGuard dg(h->device);
+  FDTD_CUDA(cudaStreamSynchronize(h->stream), "synchronize previous stream");
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return FDTD_OK;
+}
+
+int fdtd_synchronize(fdtd_handle* h) {
+  if (int rc = check_handle(h)) return rc;
+  DeviceGuard dg(h->device);
+  FDTD_CUDA(cudaStreamSynchronize(h->stream), "synchronize");
+  return FDTD_OK;
+}
+
+int fdtd_set_fp16_exponents(fdtd_handle* h, const int exponents[6]) {
+  if (int rc = check_handle(h)) return rc;
+  if (!exponents) return fail(FDTD_ERR_INVALID_ARGUMENT, "null exponents");
+  if (h->form != Form::F16) return fail(FDTD_ERR_UNSUPPORTED, "exponents apply to the FP16_SCALED form only");
+  for (int c = 0; c < 6; ++c)
+    if (exponents[c] < -100 || exponents[c] > 100) return fail(FDTD_ERR_INVALID_ARGUMENT, "exponent out of range");
+  // Rescale stored values so the fields they represent are unchanged.
+  DeviceGuard dg(h->device);
+  if (int rc = ensure_staging(h)) return rc;
+  for (int c = 0; c < 6; ++c) {
+    if (exponents[c] == h->fp16_exp[c]) continue;
+    for (int64_t off = 0; off < h->g.cells; off += kStagingElems) {
+      const int64_t m = std::min<int64_t>(kStagingElems, h->g.cells - off);
+      FDTD_CUDA(launch_export(h->view(), c, h->d_staging, off, m, h->stream), "rescale export");
+      const int old = h->fp16_exp[c];
+      h->fp16_exp[c] = exponents[c];
+      cudaError_t e = launch_import(h->view(), c, h->d_staging, off, m, h->stream);
+      h->fp16_exp[c] = old;
+      if (e != cudaSuccess) return cuda_fail(e, "rescale import");
+    }
+    h->fp16_exp[c] = exponents[c];
+  }
+  FDTD_CUDA(cudaStreamSynchronize(h->stream), "rescale");
+  return FDTD_OK;
+}
+
+}  // extern "C"

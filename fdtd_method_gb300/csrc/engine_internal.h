@@ -1,0 +1,71 @@
+// Declarations shared between the C-ABI layer (engine.cu) and the kernel
+// translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+#include "storage.cuh"
+
+namespace fdtd {
+
+struct Fp64Fields {
+  double* f[9];  // EX..JZ
+};
+
+struct CoefSet {
+  Coef cb[3];
+  Coef ce[3];
+  Coef cj;
+};
+
+// kernels_fp64.cu
+cudaError_t launch_b_fp64(const Grid& g, const Fp64Fields& F, const double cb[3], int applications,
+                          int64_t* step_inc, cudaStream_t st);
+cudaError_t launch_e_fp64(const Grid& g, const Fp64Fields& F, const double ce[3], double cJ,
+                          bool dense_j, const SourceSet& ss, cudaStream_t st);
+
+// kernels_f32.cu
+template <class S>
+cudaError_t launch_b_f32(const Grid& g, const S& st, const CoefSet& cs, int applications,
+                         int64_t* step_inc, cudaStream_t stream);
+template <class S>
+cudaError_t launch_e_f32(const Grid& g, const S& st, const float* const J[3], bool dense_j,
+                         const CoefSet& cs, const SourceSet& ss, const float* tables_f,
+                         cudaStream_t stream);
+
+// misc.cu — conversions, diagnostics, small helpers.
+enum class Form { F64 = 0, F32 = 1, F32C = 2, F16 = 3 };
+
+struct StateView {
+  Form form;
+  Grid g;
+  double* f64[6];
+  StoreF32 s32;
+  StoreF32C s32c;
+  StoreF16 s16;
+};
+
+// Writes component c (0..5) of the state from n FP64 values at `src` starting
+// at flat offset `off`.
+cudaError_t launch_import(const StateView& v, int c, const double* src, int64_t off, int64_t n,
+                          cudaStream_t st);
+// Reads component c (0..5) of the state as FP64 into `dst`.
+cudaError_t launch_export(const StateView& v, int c, double* dst, int64_t off, int64_t n,
+                          cudaStream_t st);
+// FP64 -> FP32 conversion of n values.
+cudaError_t launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
+
+// Field sums (fdtd_diag order, 10 values) in two passes through `partials`
+// (room for `max_blocks` * 10 doubles); the result lands in out_dev[10].
+constexpr int kDiagValues = 10;
+constexpr int kDiagThreads = 256;
+int diag_blocks_for(int64_t cells, int max_blocks);
+cudaError_t launch_field_sums(const StateView& v, double* partials, int nblocks, double* out_dev,
+                              cudaStream_t st);
+
+cudaError_t launch_set_i64(int64_t* dst, int64_t value, cudaStream_t st);
+
+}  // namespace fdtd

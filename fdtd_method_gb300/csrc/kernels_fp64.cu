@@ -1,0 +1,183 @@
+// FP64 Yee kernels — the drop-in form.
+//
+// Each update is evaluated in the reference's operation order with explicit
+// round-to-nearest intrinsics (__dadd_rn / __dsub_rn / __dmul_rn), which the
+// compiler never fuses into FMA.  Results are therefore bit-identical to the
+// reference's (kokkos_functors.h:64-90 and :128-151 built without FMA
+// contraction, which is what its stock x86-64 build does).
+//
+// On GB300 the FP64 pipe issues ~5e11 instructions/s in total, 1/64 of the
+// FP32 rate, so these kernels are bound by FP64 issue, not by HBM: a B half
+// step costs 18 FP64 instructions per cell, a merged double half step 21 and
+// the E step 18 (24 with current).  The kernels keep every other cost off the
+// FP64 pipe: one thread per (i, j) column marching along z with the z
+// neighbour carried in registers, all index arithmetic in 32-bit integers
+// plus one 64-bit plane offset per z step.
+#include "engine_internal.h"
+
+namespace fdtd {
+
+#define DADD __dadd_rn
+#define DSUB __dsub_rn
+#define DMUL __dmul_rn
+
+// B += t (once: a half step; twice: the second half step of one update_fields
+// followed by the first half step of the next, which see the same E and
+// therefore the same t — the two additions stay separate, so the result is
+// the reference's bit for bit).  kernels: kokkos_functors.h:128-151.
+template <int kApplications>
+__global__ void __launch_bounds__(256) b_update_fp64(Grid g, const double* __restrict__ Ex,
+                                                     const double* __restrict__ Ey,
+                                                     const double* __restrict__ Ez,
+                                                     double* __restrict__ Bx, double* __restrict__ By,
+                                                     double* __restrict__ Bz, double cx, double cy,
+                                                     double cz, int kchunk, int64_t* step_inc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k0 = blockIdx.z * kchunk;
+  if (step_inc && i == 0 && j == 0 && k0 == 0) *step_inc += 1;
+  if (i >= g.Ni || j >= g.Nj || k0 >= g.Nk) return;
+  const int k1 = min(k0 + kchunk, g.Nk);
+  const int64_t col = i + (int64_t)j * g.Ni;
+  const int64_t col_in = wrap_next(i, g.Ni) + (int64_t)j * g.Ni;
+  const int64_t col_jn = i + (int64_t)wrap_next(j, g.Nj) * g.Ni;
+
+  int64_t base = (int64_t)k0 * g.plane;
+  double ex = Ex[col + base];
+  double ey = Ey[col + base];
+  for (int k = k0; k < k1; ++k) {
+    const int64_t nbase = (int64_t)wrap_next(k, g.Nk) * g.plane;
+    const double ex_kn = Ex[col + nbase];
+    const double ey_kn = Ey[col + nbase];
+    const double ez = Ez[col + base];
+    const double ez_jn = Ez[col_jn + base];
+    const double ez_in = Ez[col_in + base];
+    const double ey_in = Ey[col_in + base];
+    const double ex_jn = Ex[col_jn + base];
+
+    const double tx = DSUB(DMUL(cz, DSUB(ey_kn, ey)), DMUL(cy, DSUB(ez_jn, ez)));
+    const double ty = DSUB(DMUL(cx, DSUB(ez_in, ez)), DMUL(cz, DSUB(ex_kn, ex)));
+    const double tz = DSUB(DMUL(cy, DSUB(ex_jn, ex)), DMUL(cx, DSUB(ey_in, ey)));
+
+    double bx = DADD(Bx[col + base], tx);
+    double by = DADD(By[col + base], ty);
+    double bz = DADD(Bz[col + base], tz);
+    if (kApplications == 2) {
+      bx = DADD(bx, tx);
+      by = DADD(by, ty);
+      bz = DADD(bz, tz);
+    }
+    Bx[col + base] = bx;
+    By[col + base] = by;
+    Bz[col + base] = bz;
+
+    ex = ex_kn;
+    ey = ey_kn;
+    base = nbase;
+  }
+}
+
+// E += cJ*J + c*curl(B), kokkos_functors.h:64-90.  Cells with no current skip
+// the cJ*J term: cJ < 0, so cJ*0 = -0 and x + (-0) = x for every x, which
+// leaves the result bit-identical.
+template <bool kDenseJ, bool kSources>
+__global__ void __launch_bounds__(256) e_update_fp64(Grid g, const double* __restrict__ Bx,
+                                                     const double* __restrict__ By,
+                                                     const double* __restrict__ Bz,
+                                                     const double* __restrict__ Jx,
+                                                     const double* __restrict__ Jy,
+                                                     const double* __restrict__ Jz,
+                                                     double* __restrict__ Ex, double* __restrict__ Ey,
+                                                     double* __restrict__ Ez, double cJ, double cx,
+                                                     double cy, double cz, int kchunk, SourceSet ss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k0 = blockIdx.z * kchunk;
+  if (i >= g.Ni || j >= g.Nj || k0 >= g.Nk) return;
+  const int k1 = min(k0 + kchunk, g.Nk);
+  const int64_t col = i + (int64_t)j * g.Ni;
+  const int64_t col_ip = wrap_prev(i, g.Ni) + (int64_t)j * g.Ni;
+  const int64_t col_jp = i + (int64_t)wrap_prev(j, g.Nj) * g.Ni;
+  int64_t s = 0;
+  if (kSources) s = *ss.step;
+
+  int64_t base = (int64_t)k0 * g.plane;
+  const int64_t pbase0 = (int64_t)wrap_prev(k0, g.Nk) * g.plane;
+  double bx_kp = Bx[col + pbase0];
+  double by_kp = By[col + pbase0];
+  for (int k = k0; k < k1; ++k) {
+    const double bx = Bx[col + base];
+    const double by = By[col + base];
+    const double bz = Bz[col + base];
+    const double bz_jp = Bz[col_jp + base];
+    const double bz_ip = Bz[col_ip + base];
+    const double by_ip = By[col_ip + base];
+    const double bx_jp = Bx[col_jp + base];
+
+    double tx = DSUB(DMUL(cy, DSUB(bz, bz_jp)), DMUL(cz, DSUB(by, by_kp)));
+    double ty = DSUB(DMUL(cz, DSUB(bx, bx_kp)), DMUL(cx, DSUB(bz, bz_ip)));
+    double tz = DSUB(DMUL(cx, DSUB(by, by_ip)), DMUL(cy, DSUB(bx, bx_jp)));
+
+    bool has_j = false;
+    double jx = 0.0, jy = 0.0, jz = 0.0;
+    if (kDenseJ) {
+      jx = Jx[col + base];
+      jy = Jy[col + base];
+      jz = Jz[col + base];
+      has_j = true;
+    }
+    if (kSources) has_j |= source_current(ss, s, i, j, k, g, jx, jy, jz);
+    if (has_j) {
+      // (cJ*J + c1*d1) - c2*d2, the reference's association.
+      tx = DSUB(DADD(DMUL(cJ, jx), DMUL(cy, DSUB(bz, bz_jp))), DMUL(cz, DSUB(by, by_kp)));
+      ty = DSUB(DADD(DMUL(cJ, jy), DMUL(cz, DSUB(bx, bx_kp))), DMUL(cx, DSUB(bz, bz_ip)));
+      tz = DSUB(DADD(DMUL(cJ, jz), DMUL(cx, DSUB(by, by_ip))), DMUL(cy, DSUB(bx, bx_jp)));
+    }
+    Ex[col + base] = DADD(Ex[col + base], tx);
+    Ey[col + base] = DADD(Ey[col + base], ty);
+    Ez[col + base] = DADD(Ez[col + base], tz);
+
+    bx_kp = bx;
+    by_kp = by;
+    base += g.plane;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launchers (called from engine.cu).
+
+static dim3 fp64_grid(const Grid& g, int kchunk) {
+  return dim3((g.Ni + 31) / 32, (g.Nj + 7) / 8, (g.Nk + kchunk - 1) / kchunk);
+}
+
+cudaError_t launch_b_fp64(const Grid& g, const Fp64Fields& F, const double cb[3], int applications,
+                          int64_t* step_inc, cudaStream_t st) {
+  const int kchunk = 16;
+  dim3 block(32, 8), grid = fp64_grid(g, kchunk);
+  if (applications == 2)
+    b_update_fp64<2><<<grid, block, 0, st>>>(g, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5],
+                                             cb[0], cb[1], cb[2], kchunk, step_inc);
+  else
+    b_update_fp64<1><<<grid, block, 0, st>>>(g, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5],
+                                             cb[0], cb[1], cb[2], kchunk, step_inc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_e_fp64(const Grid& g, const Fp64Fields& F, const double ce[3], double cJ,
+                          bool dense_j, const SourceSet& ss, cudaStream_t st) {
+  const int kchunk = 16;
+  dim3 block(32, 8), grid = fp64_grid(g, kchunk);
+  const bool src = ss.count > 0;
+#define FDTD_E64(DJ, SRC)                                                                     \
+  e_update_fp64<DJ, SRC><<<grid, block, 0, st>>>(g, F.f[3], F.f[4], F.f[5], F.f[6], F.f[7],   \
+                                                 F.f[8], F.f[0], F.f[1], F.f[2], cJ, ce[0],   \
+                                                 ce[1], ce[2], kchunk, ss)
+  if (dense_j && src) FDTD_E64(true, true);
+  else if (dense_j) FDTD_E64(true, false);
+  else if (src) FDTD_E64(false, true);
+  else FDTD_E64(false, false);
+#undef FDTD_E64
+  return cudaGetLastError();
+}
+
+}  // namespace fdtd

@@ -1,0 +1,192 @@
+// Conversions between FP64 host data and the storage forms, FP64 field
+// diagnostics, and small helpers.
+#include "engine_internal.h"
+
+namespace fdtd {
+
+namespace {
+
+constexpr int kConvThreads = 256;
+
+inline int conv_blocks(int64_t n) {
+  int64_t b = (n + kConvThreads - 1) / kConvThreads;
+  if (b > 152 * 64) b = 152 * 64;  // grid-stride beyond this
+  return (int)(b < 1 ? 1 : b);
+}
+
+// Splits an FP64 value into hi + lo of the compensated form.
+__device__ __forceinline__ Pair split_f64(double x) {
+  const float h = __double2float_rn(x);
+  const float l = __double2float_rn(x - (double)h);
+  return Pair{h, l};
+}
+
+template <class S>
+__global__ void import_kernel(S st, int c, const double* __restrict__ src, int64_t off, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    if (S::kComp) st.store(c, off + t, split_f64(src[t]));
+    else st.store(c, off + t, Pair{__double2float_rn(src[t]), 0.f});
+  }
+}
+
+template <class S>
+__global__ void export_kernel(S st, int c, double* __restrict__ dst, int64_t off, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    dst[t] = st.load_f64(c, off + t);
+}
+
+__global__ void to_f32_kernel(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    dst[t] = __double2float_rn(src[t]);
+}
+
+// One FP64 value of each field at flat index idx.
+struct F64Loader {
+  const double* f[6];
+  __device__ __forceinline__ void get(int64_t idx, double v[6]) const {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) v[c] = f[c][idx];
+  }
+};
+template <class S>
+struct StoreLoader {
+  S st;
+  __device__ __forceinline__ void get(int64_t idx, double v[6]) const {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) v[c] = st.load_f64(c, idx);
+  }
+};
+
+// Pass 1: every block accumulates its grid-stride share of the ten sums in
+// FP64 and writes them to partials[block * 10 + q].
+template <class L>
+__global__ void __launch_bounds__(kDiagThreads) sums_pass1(L ld, int64_t cells, double* partials) {
+  double acc[kDiagValues];
+#pragma unroll
+  for (int q = 0; q < kDiagValues; ++q) acc[q] = 0.0;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < cells;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    double v[6];
+    ld.get(idx, v);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      acc[c] = fma(v[c], v[c], acc[c]);
+      acc[9] += isfinite(v[c]) ? 0.0 : 1.0;
+    }
+    acc[6] += v[1] * v[5] - v[2] * v[4];
+    acc[7] += v[2] * v[3] - v[0] * v[5];
+    acc[8] += v[0] * v[4] - v[1] * v[3];
+  }
+  __shared__ double red[kDiagThreads / 32][kDiagValues];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < kDiagValues; ++q) {
+    double x = acc[q];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp][q] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < kDiagValues) {
+    double x = 0.0;
+    for (int w = 0; w < kDiagThreads / 32; ++w) x += red[w][threadIdx.x];
+    partials[(int64_t)blockIdx.x * kDiagValues + threadIdx.x] = x;
+  }
+}
+
+// Pass 2: one block folds the per-block partials into out[10].
+__global__ void __launch_bounds__(kDiagThreads) sums_pass2(const double* partials, int nblocks,
+                                                          double* out) {
+  __shared__ double red[kDiagThreads / 32][kDiagValues];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int q = 0; q < kDiagValues; ++q) {
+    double x = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) x += partials[(int64_t)b * kDiagValues + q];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp][q] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < kDiagValues) {
+    double x = 0.0;
+    for (int w = 0; w < kDiagThreads / 32; ++w) x += red[w][threadIdx.x];
+    out[threadIdx.x] = x;
+  }
+}
+
+__global__ void set_i64_kernel(int64_t* dst, int64_t value) { *dst = value; }
+
+}  // namespace
+
+cudaError_t launch_import(const StateView& v, int c, const double* src, int64_t off, int64_t n,
+                          cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int nb = conv_blocks(n);
+  switch (v.form) {
+    case Form::F64:
+      return cudaMemcpyAsync(v.f64[c] + off, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
+    case Form::F32: import_kernel<<<nb, kConvThreads, 0, st>>>(v.s32, c, src, off, n); break;
+    case Form::F32C: import_kernel<<<nb, kConvThreads, 0, st>>>(v.s32c, c, src, off, n); break;
+    case Form::F16: import_kernel<<<nb, kConvThreads, 0, st>>>(v.s16, c, src, off, n); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_export(const StateView& v, int c, double* dst, int64_t off, int64_t n,
+                          cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int nb = conv_blocks(n);
+  switch (v.form) {
+    case Form::F64:
+      return cudaMemcpyAsync(dst, v.f64[c] + off, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
+    case Form::F32: export_kernel<<<nb, kConvThreads, 0, st>>>(v.s32, c, dst, off, n); break;
+    case Form::F32C: export_kernel<<<nb, kConvThreads, 0, st>>>(v.s32c, c, dst, off, n); break;
+    case Form::F16: export_kernel<<<nb, kConvThreads, 0, st>>>(v.s16, c, dst, off, n); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  to_f32_kernel<<<conv_blocks(n), kConvThreads, 0, st>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
+int diag_blocks_for(int64_t cells, int max_blocks) {
+  int64_t b = (cells + kDiagThreads * 8 - 1) / (kDiagThreads * 8);
+  if (b > max_blocks) b = max_blocks;
+  return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_field_sums(const StateView& v, double* partials, int nblocks, double* out_dev,
+                              cudaStream_t st) {
+  const int64_t cells = v.g.cells;
+  switch (v.form) {
+    case Form::F64: {
+      F64Loader ld{{v.f64[0], v.f64[1], v.f64[2], v.f64[3], v.f64[4], v.f64[5]}};
+      sums_pass1<<<nblocks, kDiagThreads, 0, st>>>(ld, cells, partials);
+      break;
+    }
+    case Form::F32:
+      sums_pass1<<<nblocks, kDiagThreads, 0, st>>>(StoreLoader<StoreF32>{v.s32}, cells, partials);
+      break;
+    case Form::F32C:
+      sums_pass1<<<nblocks, kDiagThreads, 0, st>>>(StoreLoader<StoreF32C>{v.s32c}, cells, partials);
+      break;
+    case Form::F16:
+      sums_pass1<<<nblocks, kDiagThreads, 0, st>>>(StoreLoader<StoreF16>{v.s16}, cells, partials);
+      break;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  sums_pass2<<<1, kDiagThreads, 0, st>>>(partials, nblocks, out_dev);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_i64(int64_t* dst, int64_t value, cudaStream_t st) {
+  set_i64_kernel<<<1, 1, 0, st>>>(dst, value);
+  return cudaGetLastError();
+}
+
+}  // namespace fdtd

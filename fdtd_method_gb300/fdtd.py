@@ -1,0 +1,323 @@
+"""Host-side mirror of the reference's FDTD solver class over the CUDA engine.
+
+Reference surface (Amazingkivas/FDTD_Method):
+  struct Parameters          include/Structures.h:23-38
+  struct CurrentParameters   include/Structures.h:13-21
+  struct SelectedFields      include/Structures.h:8-11
+  enum class Component/Axis  include/Enums.h:5-6
+  FDTD_const::C, PI, ...     include/Constants.h:4-12
+  class FDTD                 include/FDTD_kokkos/FDTD_kokkos.h:7-36
+    FDTD(Parameters, FP dt)  src/FDTD_kokkos/FDTD_kokkos.cpp:5-67
+    zeroed_currents()        src/FDTD_kokkos/FDTD_kokkos.cpp:69-73
+    get_field(Component)     src/FDTD_kokkos/FDTD_kokkos.cpp:75-89
+    update_fields()          src/FDTD_kokkos/FDTD_kokkos.cpp:91-104
+
+Same names, argument meaning and error behaviour: invalid parameters raise
+``InvalidArgument`` (a ValueError; the reference throws
+std::invalid_argument("ERROR: invalid parameters")), an invalid component
+raises ``LogicError`` (std::logic_error("ERROR: Invalid field component")).
+All work runs through the C ABI of ``libfdtd_gb300.so``; nothing here
+computes fields.
+"""
+import ctypes
+import enum
+from dataclasses import dataclass, field as dc_field
+
+import numpy as np
+
+from . import _lib
+from ._lib import FDTDError, InvalidArgument, LogicError, OutOfMemory  # noqa: F401
+
+
+class Const:
+    """FDTD_const (include/Constants.h:4-12)."""
+    C = 3e10
+    R = 1e-12
+    EPS0 = 1.0
+    MU0 = 1.0
+    N = 4.0
+    PI = 3.14159265358
+
+
+class Component(enum.IntEnum):
+    EX = 0
+    EY = 1
+    EZ = 2
+    BX = 3
+    BY = 4
+    BZ = 5
+    JX = 6
+    JY = 7
+    JZ = 8
+
+
+class Axis(enum.IntEnum):
+    X = 0
+    Y = 1
+    Z = 2
+
+
+class Precision(enum.IntEnum):
+    FP64 = 0          # the drop-in: bit-identical to the reference
+    FP32 = 1
+    FP32_COMP = 2     # FP32 hi + int8 lo compensated storage
+    FP16_SCALED = 3   # FP16 storage, power-of-two scale per component
+
+
+@dataclass
+class Parameters:
+    Ni: int
+    Nj: int
+    Nk: int
+    ax: float
+    bx: float
+    ay: float
+    by: float
+    az: float
+    bz: float
+    dx: float
+    dy: float
+    dz: float
+
+    def to_c(self):
+        return _lib.Params(int(self.Ni), int(self.Nj), int(self.Nk),
+                           float(self.ax), float(self.bx), float(self.ay), float(self.by),
+                           float(self.az), float(self.bz),
+                           float(self.dx), float(self.dy), float(self.dz))
+
+    @property
+    def cells(self):
+        return int(self.Ni) * int(self.Nj) * int(self.Nk)
+
+
+@dataclass
+class SelectedFields:
+    selected_E: Component
+    selected_B: Component
+
+
+@dataclass
+class CurrentParameters:
+    """include/Structures.h:13-21; period_* default to m * C as there."""
+    period: int
+    m: int
+    dt: float
+    iterations: int = 0
+    period_x: float = None
+    period_y: float = None
+    period_z: float = None
+
+    def __post_init__(self):
+        for a in ("period_x", "period_y", "period_z"):
+            if getattr(self, a) is None:
+                setattr(self, a, float(self.m) * Const.C)
+
+
+@dataclass
+class SeparableSource:
+    """A current source J_c(i,j,k,s) += amp[s] * gx[di] * gy[dj] * gz[dk] in a
+    periodic box at (i0, j0, k0) of extent len(gx) x len(gy) x len(gz), for the
+    components in comp_mask (bit 0 Jx, 1 Jy, 2 Jz).  See fdtd_source in
+    include/fdtd_gb300.h."""
+    comp_mask: int
+    i0: int
+    j0: int
+    k0: int
+    gx: np.ndarray
+    gy: np.ndarray
+    gz: np.ndarray
+    amp: np.ndarray
+    meta: dict = dc_field(default_factory=dict)
+
+    def to_c(self):
+        keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (self.gx, self.gy, self.gz, self.amp)]
+        ptr = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        s = _lib.Source(int(self.comp_mask), int(self.i0), int(self.j0), int(self.k0),
+                        len(keep[0]), len(keep[1]), len(keep[2]),
+                        ptr(keep[0]), ptr(keep[1]), ptr(keep[2]), ptr(keep[3]), len(keep[3]))
+        return s, keep
+
+
+class Field:
+    """Handle to one component of a solver's state (the reference's
+    Kokkos::View member).  It aliases the solver's storage: ``numpy()`` is the
+    host mirror + deep_copy, ``assign()`` the copy back.  For the FP64 form
+    ``device_ptr`` is the device address (and ``__cuda_array_interface__``
+    lets array libraries wrap it without a copy)."""
+
+    def __init__(self, solver, comp):
+        self._solver = solver
+        self.comp = Component(comp)
+
+    def size(self):
+        return self._solver.parameters.cells
+
+    def __len__(self):
+        return self.size()
+
+    @property
+    def device_ptr(self):
+        return self._solver._device_ptr(self.comp)
+
+    @property
+    def __cuda_array_interface__(self):
+        return {"shape": (self.size(),), "typestr": "<f8", "data": (self.device_ptr, False),
+                "version": 3, "strides": None, "stream": None}
+
+    def numpy(self, out=None):
+        return self._solver.copy_to_host(self.comp, out)
+
+    def assign(self, values):
+        self._solver.copy_from_host(self.comp, values)
+
+
+class FDTD:
+    """Drop-in for FDTD_kokkos::FDTD on one GPU."""
+
+    def __init__(self, parameters, dt, precision=Precision.FP64):
+        self._h = None
+        lib = _lib.load()
+        self.parameters = parameters
+        self.dt = float(dt)
+        self.precision = Precision(precision)
+        p = parameters.to_c()
+        h = ctypes.c_void_p()
+        _lib.check(lib.fdtd_create(ctypes.byref(p), self.dt, int(self.precision), ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+        self._sources = []
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self):
+        if self._h is not None:
+            self._lib.fdtd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _handle(self):
+        if self._h is None:
+            raise FDTDError(_lib.FDTD_ERR_INVALID_ARGUMENT, "solver is closed")
+        return self._h
+
+    # -- the reference's API ----------------------------------------------
+    def get_field(self, comp):
+        c = int(comp)
+        if c < 0 or c > 8:
+            raise LogicError(_lib.FDTD_ERR_LOGIC, "ERROR: Invalid field component")
+        return Field(self, c)
+
+    def update_fields(self):
+        _lib.check(self._lib.fdtd_update_fields(self._handle()))
+
+    def zeroed_currents(self):
+        _lib.check(self._lib.fdtd_zeroed_currents(self._handle()))
+
+    # -- extensions ---------------------------------------------------------
+    def step(self, n):
+        """n consecutive update_fields() calls."""
+        _lib.check(self._lib.fdtd_step(self._handle(), int(n)))
+
+    def synchronize(self):
+        """Kokkos::fence() equivalent."""
+        _lib.check(self._lib.fdtd_synchronize(self._handle()))
+
+    def _device_ptr(self, comp):
+        ptr = ctypes.POINTER(ctypes.c_double)()
+        _lib.check(self._lib.fdtd_get_field(self._handle(), int(comp), ctypes.byref(ptr)))
+        return ctypes.cast(ptr, ctypes.c_void_p).value
+
+    def copy_to_host(self, comp, out=None):
+        n = self.parameters.cells
+        if out is None:
+            out = np.empty(n, dtype=np.float64)
+        if out.dtype != np.float64 or out.size != n or not out.flags.c_contiguous:
+            raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "output must be a contiguous float64 array of Ni*Nj*Nk")
+        _lib.check(self._lib.fdtd_copy_field_to_host(self._handle(), int(comp), out.ctypes.data, n))
+        return out
+
+    def copy_from_host(self, comp, values):
+        n = self.parameters.cells
+        a = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        if a.size != n:
+            raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "expected %d values, got %d" % (n, a.size))
+        _lib.check(self._lib.fdtd_copy_field_from_host(self._handle(), int(comp), a.ctypes.data, n))
+
+    def add_source(self, src):
+        c, keep = src.to_c()
+        idx = ctypes.c_int()
+        _lib.check(self._lib.fdtd_add_source(self._handle(), ctypes.byref(c), ctypes.byref(idx)))
+        self._sources.append(src)
+        return idx.value
+
+    def clear_sources(self):
+        _lib.check(self._lib.fdtd_clear_sources(self._handle()))
+        self._sources = []
+
+    @property
+    def step_index(self):
+        v = ctypes.c_int64()
+        _lib.check(self._lib.fdtd_get_step(self._handle(), ctypes.byref(v)))
+        return v.value
+
+    @step_index.setter
+    def step_index(self, value):
+        _lib.check(self._lib.fdtd_set_step(self._handle(), int(value)))
+
+    def field_sums(self):
+        """FP64 sums over all cells: [Ex^2, Ey^2, Ez^2, Bx^2, By^2, Bz^2,
+        (ExB)_x, (ExB)_y, (ExB)_z, non-finite count]."""
+        out = (ctypes.c_double * _lib.DIAG_COUNT)()
+        _lib.check(self._lib.fdtd_field_sums(self._handle(), out))
+        return np.array(out[:], dtype=np.float64)
+
+    def energy(self):
+        """Total field energy (E^2 + B^2) dV / (8 pi), Gaussian units."""
+        s = self.field_sums()
+        p = self.parameters
+        return float(s[:6].sum() * p.dx * p.dy * p.dz / (8.0 * Const.PI))
+
+    def poynting(self):
+        """Volume integral of the Poynting vector c/(4 pi) E x B (E and B taken
+        at their own staggered points)."""
+        s = self.field_sums()
+        p = self.parameters
+        return s[6:9] * Const.C * p.dx * p.dy * p.dz / (4.0 * Const.PI)
+
+    def set_fp16_exponents(self, exps):
+        arr = (ctypes.c_int * 6)(*[int(e) for e in exps])
+        _lib.check(self._lib.fdtd_set_fp16_exponents(self._handle(), arr))
+
+    KERNEL_KINDS = ("e_update", "b_half", "b_double", "fused_step")
+
+    def set_kernel_timing(self, enabled):
+        """Bracket every step-pipeline kernel launch with CUDA events."""
+        _lib.check(self._lib.fdtd_set_kernel_timing(self._handle(), 1 if enabled else 0))
+
+    def kernel_times(self):
+        """{kind: (total ms, launches)} since the previous call."""
+        ms = (ctypes.c_double * 4)()
+        n = (ctypes.c_int64 * 4)()
+        _lib.check(self._lib.fdtd_kernel_times(self._handle(), ms, n))
+        return {k: (ms[q], n[q]) for q, k in enumerate(self.KERNEL_KINDS)}
+
+    def set_stream(self, stream_handle):
+        _lib.check(self._lib.fdtd_set_stream(self._handle(), ctypes.c_void_p(int(stream_handle or 0))))
+
+    def coefficients(self):
+        """The reference's coefficients (src/FDTD_kokkos/FDTD_kokkos.cpp:45-55)."""
+        p, dt = self.parameters, self.dt
+        cdt = Const.C * dt
+        return {"coef_E": (cdt / p.dx, cdt / p.dy, cdt / p.dz),
+                "coef_B": (cdt / (2.0 * p.dx), cdt / (2.0 * p.dy), cdt / (2.0 * p.dz)),
+                "current_coef": -4.0 * Const.PI * dt}

@@ -1,0 +1,189 @@
+/*
+ * fdtd_gb300.h — C ABI of the GB300 (sm_103a) Yee FDTD engine.
+ *
+ * One handle = one periodic 3-D grid on one GPU, driven on one CUDA stream.
+ * The entry points replace the public surface of the reference's Kokkos
+ * solver class FDTD_kokkos::FDTD (Amazingkivas/FDTD_Method,
+ * include/FDTD_kokkos/FDTD_kokkos.h:7-36); each declaration names the
+ * reference interface it stands in for.  Plain pointers and sizes only.
+ *
+ * Every function returns FDTD_OK (0) or a negative FDTD_ERR_* code; the text
+ * of the last error on the calling thread is fdtd_last_error().  A handle is
+ * not thread-safe; distinct handles are independent.
+ *
+ * Field storage: component c lives in device memory as Ni*Nj*Nk values, flat
+ * index i + j*Ni + k*Ni*Nj (x fastest), the layout of the reference's
+ * Kokkos::View<double*, LayoutLeft> fields (include/FDTD_kokkos/kokkos_shared.h:16).
+ */
+#ifndef FDTD_GB300_H
+#define FDTD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDTD_ABI_VERSION 1
+
+/* Status codes. */
+#define FDTD_OK 0
+#define FDTD_ERR_INVALID_ARGUMENT (-1) /* reference: std::invalid_argument */
+#define FDTD_ERR_LOGIC (-2)            /* reference: std::logic_error     */
+#define FDTD_ERR_CUDA (-3)             /* a CUDA call failed              */
+#define FDTD_ERR_OUT_OF_MEMORY (-4)    /* device allocation failed        */
+#define FDTD_ERR_UNSUPPORTED (-5)      /* not available for this storage  */
+#define FDTD_ERR_TIMEOUT (-6)          /* a bounded device wait gave up   */
+
+/* Field components, numbered as the reference's enum class Component
+ * (include/Enums.h:5). */
+enum fdtd_component {
+    FDTD_EX = 0, FDTD_EY, FDTD_EZ,
+    FDTD_BX, FDTD_BY, FDTD_BZ,
+    FDTD_JX, FDTD_JY, FDTD_JZ
+};
+
+/* Storage / arithmetic forms of the field state.
+ *   FP64        — the drop-in: FP64 storage and arithmetic, evaluated in the
+ *                 reference's operation order with no fused multiply-add, so
+ *                 results are bit-identical to the reference's.
+ *   FP32        — FP32 storage and arithmetic.
+ *   FP32_COMP   — FP32 arithmetic; each E/B value stored as an FP32 "hi" word
+ *                 plus a 16-bit "lo" correction word (compensated storage).
+ *   FP16_SCALED — FP16 storage with a power-of-two scale per component and
+ *                 FP32 arithmetic. */
+enum fdtd_precision {
+    FDTD_PRECISION_FP64 = 0,
+    FDTD_PRECISION_FP32 = 1,
+    FDTD_PRECISION_FP32_COMP = 2,
+    FDTD_PRECISION_FP16_SCALED = 3
+};
+
+/* Grid description; same members, order and meaning as the reference's
+ * struct Parameters (include/Structures.h:23-38). */
+typedef struct fdtd_params {
+    int Ni, Nj, Nk;
+    double ax, bx, ay, by, az, bz;
+    double dx, dy, dz;
+} fdtd_params;
+
+/* A separable current source.  During time step s (s = number of completed
+ * update_fields calls) it adds, for every component c with bit c of
+ * comp_mask set (bit 0 = Jx, 1 = Jy, 2 = Jz),
+ *     amp[s] * gx[di] * gy[dj] * gz[dk]        (product formed left to right)
+ * to J at cell ((i0+di) mod Ni, (j0+dj) mod Nj, (k0+dk) mod Nk) for
+ * 0 <= di < ni, 0 <= dj < nj, 0 <= dk < nk.  Steps s >= n_amp add nothing.
+ * This is the form of the reference sample's box current
+ * sin(2 pi t/T) cos^2(2 pi x/Tx) cos^2(2 pi y/Ty) cos^2(2 pi z/Tz)
+ * (perf-tests/kokkos_sample/kokkos_sample.cpp:91-108) and of a Gaussian pulse
+ * with a Gaussian spatial envelope.  The tables are copied at registration. */
+typedef struct fdtd_source {
+    int comp_mask;
+    int i0, j0, k0;
+    int ni, nj, nk;
+    const double* gx;
+    const double* gy;
+    const double* gz;
+    const double* amp;
+    int64_t n_amp;
+} fdtd_source;
+
+/* Diagnostics vector filled by fdtd_field_sums (FP64 sums over all cells). */
+enum fdtd_diag {
+    FDTD_DIAG_EX2 = 0, FDTD_DIAG_EY2, FDTD_DIAG_EZ2,  /* sum of E_c^2            */
+    FDTD_DIAG_BX2, FDTD_DIAG_BY2, FDTD_DIAG_BZ2,      /* sum of B_c^2            */
+    FDTD_DIAG_SX, FDTD_DIAG_SY, FDTD_DIAG_SZ,         /* sum of (E x B)_c        */
+    FDTD_DIAG_NONFINITE,                              /* count of NaN/Inf values */
+    FDTD_DIAG_COUNT
+};
+
+typedef struct fdtd_handle fdtd_handle;
+
+/* Text of the last error on this thread ("" if none). */
+const char* fdtd_last_error(void);
+int fdtd_abi_version(void);
+
+/* Replaces FDTD::FDTD(Parameters, FP dt) (src/FDTD_kokkos/FDTD_kokkos.cpp:5-67):
+ * validates (any N <= 0 or dt <= 0 -> FDTD_ERR_INVALID_ARGUMENT with the
+ * reference's message "ERROR: invalid parameters"), allocates the nine
+ * zero-filled fields on the current CUDA device and derives the reference's
+ * coefficients.  `precision` is an fdtd_precision. */
+int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle** out);
+
+/* Releases the fields (the reference's Views are freed with the object). */
+int fdtd_destroy(fdtd_handle* h);
+
+/* Replaces FDTD::update_fields() (src/FDTD_kokkos/FDTD_kokkos.cpp:91-104):
+ * one full step B/2, E, B/2.  Asynchronous on the handle's stream. */
+int fdtd_update_fields(fdtd_handle* h);
+
+/* n consecutive update_fields() calls, scheduled as one sequence (the two B
+ * half steps that meet between steps share one sweep). */
+int fdtd_step(fdtd_handle* h, int64_t n);
+
+/* Replaces FDTD::zeroed_currents() (src/FDTD_kokkos/FDTD_kokkos.cpp:69-73). */
+int fdtd_zeroed_currents(fdtd_handle* h);
+
+/* Replaces FDTD::get_field(Component) (src/FDTD_kokkos/FDTD_kokkos.cpp:75-89)
+ * for the FP64 form: the device address of the component's Ni*Nj*Nk doubles,
+ * which aliases the engine's storage as the reference's View handle does.
+ * Writing J through it switches the E update to read J.  An out-of-range
+ * component gives FDTD_ERR_LOGIC ("ERROR: Invalid field component"); other
+ * storage forms give FDTD_ERR_UNSUPPORTED (use fdtd_copy_field). */
+int fdtd_get_field(fdtd_handle* h, int comp, double** device_ptr);
+
+/* Host mirror + deep_copy of one component (the reference's
+ * create_mirror_view / deep_copy, perf-tests/kokkos_sample/kokkos_sample.cpp:135-139),
+ * converting to/from FP64 for every storage form.  n must be Ni*Nj*Nk.
+ * Synchronous with respect to the host buffer. */
+int fdtd_copy_field_to_host(fdtd_handle* h, int comp, double* host, size_t n);
+int fdtd_copy_field_from_host(fdtd_handle* h, int comp, const double* host, size_t n);
+
+/* Registers a separable current source (see fdtd_source); returns its index
+ * through *index if non-null.  Sources replace the reference sample driver's
+ * per-step SetCurrent kernel (perf-tests/kokkos_sample/kokkos_sample.cpp:88-129). */
+int fdtd_add_source(fdtd_handle* h, const fdtd_source* src, int* index);
+int fdtd_clear_sources(fdtd_handle* h);
+
+/* Number of completed update_fields steps (indexes source amplitude tables). */
+int fdtd_get_step(fdtd_handle* h, int64_t* step);
+int fdtd_set_step(fdtd_handle* h, int64_t step);
+
+/* FP64 field sums (fdtd_diag order) over the whole grid; synchronous.  New:
+ * the reference has no energy or Poynting diagnostics.  Energy
+ * = (sum E^2 + sum B^2) dV / (8 pi); Poynting integral = c dV/(4 pi) sum E x B. */
+int fdtd_field_sums(fdtd_handle* h, double out[FDTD_DIAG_COUNT]);
+
+/* Grid and storage information. */
+int fdtd_get_params(fdtd_handle* h, fdtd_params* params, double* dt, int* precision);
+
+/* Stream control: the handle's work runs on `stream` (a cudaStream_t; 0 = the
+ * handle's own stream).  fdtd_synchronize waits for it (Kokkos::fence()). */
+int fdtd_set_stream(fdtd_handle* h, void* stream);
+int fdtd_synchronize(fdtd_handle* h);
+
+/* Per-component power-of-two scales of the FP16_SCALED form: stored value =
+ * field * 2^exponent.  `exponents` has 6 entries (Ex..Bz). */
+int fdtd_set_fp16_exponents(fdtd_handle* h, const int exponents[6]);
+
+/* Kernel timing (new; for roofline accounting).  While enabled, every kernel
+ * launch of the step pipeline is bracketed by CUDA events on the handle's
+ * stream.  fdtd_kernel_times synchronizes, then returns per kernel kind the
+ * summed duration in milliseconds and the launch count since the last call,
+ * and clears them.  Kinds: FDTD_KERNEL_E, _B_HALF, _B_DOUBLE, _FUSED. */
+enum fdtd_kernel_kind {
+    FDTD_KERNEL_E = 0,        /* E update sweep                            */
+    FDTD_KERNEL_B_HALF = 1,   /* one B half step                           */
+    FDTD_KERNEL_B_DOUBLE = 2, /* two B half steps sharing one sweep        */
+    FDTD_KERNEL_FUSED = 3,    /* a whole step (B/2, E, B/2) in one sweep   */
+    FDTD_KERNEL_KINDS = 4
+};
+int fdtd_set_kernel_timing(fdtd_handle* h, int enabled);
+int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t launches[FDTD_KERNEL_KINDS]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDTD_GB300_H */

@@ -1,0 +1,271 @@
+/*
+ * ORACLE — CPU restatement of the reference's Yee FDTD step.
+ *
+ * Test infrastructure only.  The parity tests, the engine's smoke check and
+ * the CPU-baseline leg of the benchmark call this code as the checker; the
+ * engine never links it and never falls back to it.
+ *
+ * Parity is pinned: the tests compare every function below against the
+ * reference's own Kokkos-path sources compiled unmodified against the host
+ * Kokkos stand-in (oracle/_ref, built by oracle/Makefile) and against the
+ * golden numbers recorded from that build under tests/golden/.
+ *
+ * What it restates (file:line in Amazingkivas/FDTD_Method):
+ *   periodic wrap             include/FDTD_kokkos/kokkos_functors.h:13-20
+ *   E update (UpdateEField)   include/FDTD_kokkos/kokkos_functors.h:64-90
+ *   B update (UpdateBField)   include/FDTD_kokkos/kokkos_functors.h:128-151
+ *   coefficients              src/FDTD_kokkos/FDTD_kokkos.cpp:45-55
+ *   parameter validation      src/FDTD_kokkos/FDTD_kokkos.cpp:7-12
+ *   update_fields = B/2,E,B/2 src/FDTD_kokkos/FDTD_kokkos.cpp:91-104
+ *   current box source        perf-tests/kokkos_sample/kokkos_sample.cpp:88-129
+ *
+ * Arithmetic is written in the reference's evaluation order and must be built
+ * with -ffp-contract=off so that no multiply-add is fused (the reference's
+ * stock x86-64 build has no FMA either); the results are then bit-identical
+ * to the reference's on every host.  The loops are the reference's three
+ * full-grid sweeps per step, parallelised over k with OpenMP, so the same code
+ * also serves as the timed CPU port of the reference.
+ *
+ * Field order everywhere: EX, EY, EZ, BX, BY, BZ, JX, JY, JZ
+ * (include/Enums.h:5); flat index i + j*Ni + k*Ni*Nj, x fastest.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Speed of light and pi exactly as the reference defines them
+ * (include/Constants.h:6,11); the truncated pi is deliberate. */
+#define ORACLE_C 3e10
+#define ORACLE_PI 3.14159265358
+
+typedef struct {
+    int Ni, Nj, Nk;
+    double ax, bx, ay, by, az, bz;
+    double dx, dy, dz;
+} oracle_params; /* include/Structures.h:23-38 */
+
+/* One separable current source:
+ *   J_c(i,j,k, step) += amp[step] * gx[(i-i0) mod Ni] * gy[...] * gz[...]
+ * for every component c in comp_mask (bit 0 = Jx, 1 = Jy, 2 = Jz) and every
+ * cell of the (periodically wrapped) box of extent ni x nj x nk at (i0,j0,k0).
+ * The product is formed left to right, as the reference's sample driver forms
+ * sin(t) * cos^2(x) * cos^2(y) * cos^2(z) (kokkos_sample.cpp:100-103).  Steps
+ * at or past n_amp contribute nothing. */
+typedef struct {
+    int comp_mask;
+    int i0, j0, k0;
+    int ni, nj, nk;
+    const double* gx;
+    const double* gy;
+    const double* gz;
+    const double* amp;
+    long n_amp;
+} oracle_source;
+
+int oracle_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* src/FDTD_kokkos/FDTD_kokkos.cpp:7-12 and :45-55.  coef = {cEx, cEy, cEz,
+ * cBx, cBy, cBz, cJ}.  Returns -1 (the reference throws invalid_argument) for
+ * a non-positive size or time step. */
+int oracle_coefficients(const oracle_params* p, double dt, double coef[7]) {
+    if (p->Ni <= 0 || p->Nj <= 0 || p->Nk <= 0 || dt <= 0) return -1;
+    const double cdt = ORACLE_C * dt;
+    coef[0] = cdt / p->dx;
+    coef[1] = cdt / p->dy;
+    coef[2] = cdt / p->dz;
+    coef[3] = cdt / (2.0 * p->dx);
+    coef[4] = cdt / (2.0 * p->dy);
+    coef[5] = cdt / (2.0 * p->dz);
+    coef[6] = -4.0 * ORACLE_PI * dt;
+    return 0;
+}
+
+/* include/FDTD_kokkos/kokkos_functors.h:13-20: -1 -> N-1, N -> 0, others unchanged. */
+static inline long wrap(long i, long N) {
+    const long minus_one = (i < 0);
+    const long at_n = (i == N);
+    return (N - 1) * minus_one + i * !(minus_one || at_n);
+}
+
+/* include/FDTD_kokkos/kokkos_functors.h:128-151 over the whole grid. */
+void oracle_update_B(long Ni, long Nj, long Nk,
+                     const double* Ex, const double* Ey, const double* Ez,
+                     double* Bx, double* By, double* Bz,
+                     double cx, double cy, double cz) {
+    const long plane = Ni * Nj;
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < Nk; ++k) {
+        const long kn = wrap(k + 1, Nk);
+        for (long j = 0; j < Nj; ++j) {
+            const long jn = wrap(j + 1, Nj);
+            for (long i = 0; i < Ni; ++i) {
+                const long in = wrap(i + 1, Ni);
+                const long idx = i + j * Ni + k * plane;
+                const long i_n = in + j * Ni + k * plane;
+                const long j_n = i + jn * Ni + k * plane;
+                const long k_n = i + j * Ni + kn * plane;
+                Bx[idx] += cz * (Ey[k_n] - Ey[idx]) - cy * (Ez[j_n] - Ez[idx]);
+                By[idx] += cx * (Ez[i_n] - Ez[idx]) - cz * (Ex[k_n] - Ex[idx]);
+                Bz[idx] += cy * (Ex[j_n] - Ex[idx]) - cx * (Ey[i_n] - Ey[idx]);
+            }
+        }
+    }
+}
+
+/* include/FDTD_kokkos/kokkos_functors.h:64-90 over the whole grid.  A null
+ * J pointer set means J == 0 (the term cJ*0 = -0 leaves every sum unchanged). */
+void oracle_update_E(long Ni, long Nj, long Nk,
+                     const double* Bx, const double* By, const double* Bz,
+                     const double* Jx, const double* Jy, const double* Jz,
+                     double* Ex, double* Ey, double* Ez,
+                     double cJ, double cx, double cy, double cz) {
+    const long plane = Ni * Nj;
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < Nk; ++k) {
+        const long kp = wrap(k - 1, Nk);
+        for (long j = 0; j < Nj; ++j) {
+            const long jp = wrap(j - 1, Nj);
+            for (long i = 0; i < Ni; ++i) {
+                const long ip = wrap(i - 1, Ni);
+                const long idx = i + j * Ni + k * plane;
+                const long i_p = ip + j * Ni + k * plane;
+                const long j_p = i + jp * Ni + k * plane;
+                const long k_p = i + j * Ni + kp * plane;
+                const double jx = Jx ? Jx[idx] : 0.0;
+                const double jy = Jy ? Jy[idx] : 0.0;
+                const double jz = Jz ? Jz[idx] : 0.0;
+                Ex[idx] += cJ * jx + cy * (Bz[idx] - Bz[j_p]) - cz * (By[idx] - By[k_p]);
+                Ey[idx] += cJ * jy + cz * (Bx[idx] - Bx[k_p]) - cx * (Bz[idx] - Bz[i_p]);
+                Ez[idx] += cJ * jz + cx * (By[idx] - By[i_p]) - cy * (Bx[idx] - Bx[j_p]);
+            }
+        }
+    }
+}
+
+/* Adds every active source's contribution for time step `step` into the three
+ * J arrays (perf-tests/kokkos_sample/kokkos_sample.cpp:91-108 writes the same
+ * product into a box of Jx, Jy, Jz before each update_fields). */
+void oracle_add_sources(long Ni, long Nj, long Nk, double* J[3],
+                        const oracle_source* src, int nsrc, long step) {
+    for (int s = 0; s < nsrc; ++s) {
+        const oracle_source* q = &src[s];
+        if (step < 0 || step >= q->n_amp) continue;
+        const double a = q->amp[step];
+#pragma omp parallel for schedule(static)
+        for (long dk = 0; dk < q->nk; ++dk) {
+            const long k = (q->k0 + dk) % Nk;
+            for (long dj = 0; dj < q->nj; ++dj) {
+                const long j = (q->j0 + dj) % Nj;
+                for (long di = 0; di < q->ni; ++di) {
+                    const long i = (q->i0 + di) % Ni;
+                    const long idx = i + j * Ni + k * Ni * Nj;
+                    const double v = a * q->gx[di] * q->gy[dj] * q->gz[dk];
+                    for (int c = 0; c < 3; ++c)
+                        if (q->comp_mask & (1 << c)) J[c][idx] = J[c][idx] + v;
+                }
+            }
+        }
+    }
+}
+
+/* src/FDTD_kokkos/FDTD_kokkos.cpp:91-104 repeated `steps` times.
+ * f = the nine arrays in component order; f[6..8] may be null (J == 0).
+ * With sources, step s (counted from step0) uses J_eff = J + sum of sources,
+ * formed in jwork[3] (three scratch arrays of Ni*Nj*Nk doubles). */
+void oracle_run(long Ni, long Nj, long Nk, double* f[9], const double coef[7],
+                const oracle_source* src, int nsrc, long step0, int steps,
+                double* jwork[3]) {
+    const long n = Ni * Nj * Nk;
+    for (int s = 0; s < steps; ++s) {
+        const double* J[3] = {f[6], f[7], f[8]};
+        if (nsrc > 0) {
+            for (int c = 0; c < 3; ++c) {
+                if (f[6 + c]) memcpy(jwork[c], f[6 + c], sizeof(double) * n);
+                else memset(jwork[c], 0, sizeof(double) * n);
+            }
+            oracle_add_sources(Ni, Nj, Nk, jwork, src, nsrc, step0 + s);
+            J[0] = jwork[0];
+            J[1] = jwork[1];
+            J[2] = jwork[2];
+        }
+        oracle_update_B(Ni, Nj, Nk, f[0], f[1], f[2], f[3], f[4], f[5], coef[3], coef[4], coef[5]);
+        oracle_update_E(Ni, Nj, Nk, f[3], f[4], f[5], J[0], J[1], J[2], f[0], f[1], f[2],
+                        coef[6], coef[0], coef[1], coef[2]);
+        oracle_update_B(Ni, Nj, Nk, f[0], f[1], f[2], f[3], f[4], f[5], coef[3], coef[4], coef[5]);
+    }
+}
+
+/* The reference sample driver's loop (perf-tests/kokkos_sample/kokkos_sample.cpp:88-113):
+ * before each update_fields, write the sources' values into their boxes of
+ * the dense J arrays f[6..8] (which must exist and be zero outside the
+ * boxes), then run the three sweeps.  Same results as oracle_run with zero
+ * dense J, at the reference driver's cost; used as the timed CPU baseline. */
+void oracle_run_driver(long Ni, long Nj, long Nk, double* f[9], const double coef[7],
+                       const oracle_source* src, int nsrc, long step0, int steps) {
+    double* J[3] = {f[6], f[7], f[8]};
+    for (int s = 0; s < steps; ++s) {
+        const long step = step0 + s;
+        for (int q = 0; q < nsrc; ++q) {
+            const oracle_source* b = &src[q];
+#pragma omp parallel for schedule(static)
+            for (long dk = 0; dk < b->nk; ++dk) {
+                const long k = (b->k0 + dk) % Nk;
+                for (long dj = 0; dj < b->nj; ++dj) {
+                    const long j = (b->j0 + dj) % Nj;
+                    for (long di = 0; di < b->ni; ++di) {
+                        const long idx = (b->i0 + di) % Ni + j * Ni + k * Ni * Nj;
+                        for (int c = 0; c < 3; ++c)
+                            if (b->comp_mask & (1 << c)) J[c][idx] = 0.0;
+                    }
+                }
+            }
+        }
+        oracle_add_sources(Ni, Nj, Nk, J, src, nsrc, step);
+        oracle_update_B(Ni, Nj, Nk, f[0], f[1], f[2], f[3], f[4], f[5], coef[3], coef[4], coef[5]);
+        oracle_update_E(Ni, Nj, Nk, f[3], f[4], f[5], J[0], J[1], J[2], f[0], f[1], f[2],
+                        coef[6], coef[0], coef[1], coef[2]);
+        oracle_update_B(Ni, Nj, Nk, f[0], f[1], f[2], f[3], f[4], f[5], coef[3], coef[4], coef[5]);
+    }
+}
+
+/* Field diagnostics (new; the reference has none).  Neumaier-compensated FP64
+ * sums over all cells:
+ *   out[0..5] = sum Ex^2, Ey^2, Ez^2, Bx^2, By^2, Bz^2
+ *   out[6..8] = sum (Ey Bz - Ez By), (Ez Bx - Ex Bz), (Ex By - Ey Bx)
+ *   out[9]    = number of non-finite values among the six fields
+ * Energy and Poynting integrals follow by the factors dV/(8 pi) and
+ * c dV/(4 pi). */
+void oracle_field_sums(long n, const double* f[6], double out[10]) {
+    double s[9], c[9];
+    long bad = 0;
+    for (int q = 0; q < 9; ++q) s[q] = c[q] = 0.0;
+    for (long i = 0; i < n; ++i) {
+        double v[9];
+        const double ex = f[0][i], ey = f[1][i], ez = f[2][i];
+        const double bx = f[3][i], by = f[4][i], bz = f[5][i];
+        v[0] = ex * ex; v[1] = ey * ey; v[2] = ez * ez;
+        v[3] = bx * bx; v[4] = by * by; v[5] = bz * bz;
+        v[6] = ey * bz - ez * by;
+        v[7] = ez * bx - ex * bz;
+        v[8] = ex * by - ey * bx;
+        for (int q = 0; q < 6; ++q) bad += !isfinite(f[q][i]);
+        for (int q = 0; q < 9; ++q) {
+            const double t = s[q] + v[q];
+            if (fabs(s[q]) >= fabs(v[q])) c[q] += (s[q] - t) + v[q];
+            else c[q] += (v[q] - t) + s[q];
+            s[q] = t;
+        }
+    }
+    for (int q = 0; q < 9; ++q) out[q] = s[q] + c[q];
+    out[9] = (double)bad;
+}

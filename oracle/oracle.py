@@ -1,0 +1,252 @@
+"""ctypes access to the oracle (test infrastructure only).
+
+``Oracle`` runs the C restatement in fdtd_oracle.c (each function there cites
+the reference file:line it restates).  ``RefKokkos`` drives the reference's own
+FDTD_kokkos::FDTD compiled from its sources in oracle/_ref (present only where
+the reference checkout was available to build it).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_LIB = os.path.join(REF_DIR, "libfdtd_ref.so")
+
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+class OracleParams(ctypes.Structure):
+    _fields_ = [("Ni", ctypes.c_int), ("Nj", ctypes.c_int), ("Nk", ctypes.c_int),
+                ("ax", ctypes.c_double), ("bx", ctypes.c_double),
+                ("ay", ctypes.c_double), ("by", ctypes.c_double),
+                ("az", ctypes.c_double), ("bz", ctypes.c_double),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double)]
+
+
+class OracleSource(ctypes.Structure):
+    _fields_ = [("comp_mask", ctypes.c_int),
+                ("i0", ctypes.c_int), ("j0", ctypes.c_int), ("k0", ctypes.c_int),
+                ("ni", ctypes.c_int), ("nj", ctypes.c_int), ("nk", ctypes.c_int),
+                ("gx", _D), ("gy", _D), ("gz", _D), ("amp", _D), ("n_amp", ctypes.c_long)]
+
+
+def build_oracle(force=False):
+    """Compiles liboracle.so (and nothing else) with the oracle's Makefile."""
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "fdtd_oracle.c")):
+        subprocess.run(["make", "-C", HERE, "liboracle.so"], check=True, capture_output=True)
+    return LIB
+
+
+_olib = None
+_rlib = None
+
+
+def oracle_lib():
+    global _olib
+    if _olib is None:
+        build_oracle()
+        lib = ctypes.CDLL(LIB)
+        lib.oracle_coefficients.argtypes = [ctypes.POINTER(OracleParams), ctypes.c_double, _D]
+        lib.oracle_coefficients.restype = ctypes.c_int
+        lib.oracle_run.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.POINTER(_D), _D,
+                                   ctypes.POINTER(OracleSource), ctypes.c_int, ctypes.c_long, ctypes.c_int,
+                                   ctypes.POINTER(_D)]
+        lib.oracle_run.restype = None
+        lib.oracle_run_driver.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.POINTER(_D), _D,
+                                          ctypes.POINTER(OracleSource), ctypes.c_int, ctypes.c_long, ctypes.c_int]
+        lib.oracle_run_driver.restype = None
+        lib.oracle_field_sums.argtypes = [ctypes.c_long, ctypes.POINTER(_D), _D]
+        lib.oracle_field_sums.restype = None
+        lib.oracle_threads.restype = ctypes.c_int
+        _olib = lib
+    return _olib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_D)
+
+
+def coefficients(params, dt):
+    """[cEx, cEy, cEz, cBx, cBy, cBz, cJ] or raises ValueError like the
+    reference's constructor."""
+    p = OracleParams(params.Ni, params.Nj, params.Nk, params.ax, params.bx, params.ay, params.by,
+                     params.az, params.bz, params.dx, params.dy, params.dz)
+    out = np.zeros(7)
+    if oracle_lib().oracle_coefficients(ctypes.byref(p), float(dt), _ptr(out)) != 0:
+        raise ValueError("ERROR: invalid parameters")
+    return out
+
+
+def field_sums(fields):
+    """Compensated FP64 sums: see oracle_field_sums in fdtd_oracle.c."""
+    arrs = [np.ascontiguousarray(f, dtype=np.float64) for f in fields[:6]]
+    ptrs = (_D * 6)(*[_ptr(a) for a in arrs])
+    out = np.zeros(10)
+    oracle_lib().oracle_field_sums(arrs[0].size, ptrs, _ptr(out))
+    return out
+
+
+class Oracle:
+    """The reference's FDTD state and update, restated in C (fdtd_oracle.c).
+    fields: dict component-index -> flat float64 array of Ni*Nj*Nk."""
+
+    def __init__(self, params, dt, with_current=True):
+        self.params = params
+        self.dt = float(dt)
+        self.coef = coefficients(params, dt)
+        n = params.Ni * params.Nj * params.Nk
+        self.f = [np.zeros(n) for _ in range(6)] + ([np.zeros(n) for _ in range(3)] if with_current else [None] * 3)
+        self.sources = []
+        self.step_index = 0
+        self._jwork = None
+
+    def set(self, comp, values):
+        a = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        if self.f[int(comp)] is None:
+            self.f[int(comp)] = np.zeros_like(self.f[0])
+        self.f[int(comp)][...] = a
+
+    def get(self, comp):
+        f = self.f[int(comp)]
+        return np.zeros_like(self.f[0]) if f is None else f.copy()
+
+    def add_source(self, src):
+        self.sources.append(src)
+
+    def _csources(self):
+        keep = []
+        csrc = (OracleSource * max(1, len(self.sources)))()
+        for q, s in enumerate(self.sources):
+            arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (s.gx, s.gy, s.gz, s.amp)]
+            keep.append(arrs)
+            csrc[q] = OracleSource(s.comp_mask, s.i0, s.j0, s.k0, len(arrs[0]), len(arrs[1]), len(arrs[2]),
+                                   _ptr(arrs[0]), _ptr(arrs[1]), _ptr(arrs[2]), _ptr(arrs[3]), len(arrs[3]))
+        return csrc, keep
+
+    def step_driver(self, n=1):
+        """The reference sample driver's loop: sources written into their
+        boxes of the dense J arrays, then update_fields (oracle_run_driver)."""
+        p = self.params
+        for c in range(6, 9):
+            if self.f[c] is None:
+                self.f[c] = np.zeros_like(self.f[0])
+        ptrs = (_D * 9)(*[_ptr(a) for a in self.f])
+        csrc, keep = self._csources()
+        oracle_lib().oracle_run_driver(p.Ni, p.Nj, p.Nk, ptrs, _ptr(self.coef), csrc, len(self.sources),
+                                       self.step_index, int(n))
+        self.step_index += int(n)
+
+    def step(self, n=1):
+        p = self.params
+        ptrs = (_D * 9)(*[(_ptr(a) if a is not None else _D()) for a in self.f])
+        csrc, keep = self._csources()
+        if self.sources and self._jwork is None:
+            self._jwork = [np.zeros_like(self.f[0]) for _ in range(3)]
+        jw = (_D * 3)(*([_ptr(a) for a in self._jwork] if self._jwork else [_D(), _D(), _D()]))
+        oracle_lib().oracle_run(p.Ni, p.Nj, p.Nk, ptrs, _ptr(self.coef), csrc, len(self.sources),
+                                self.step_index, int(n), jw)
+        self.step_index += int(n)
+
+    def field_sums(self):
+        return field_sums(self.f[:6])
+
+
+# ---------------------------------------------------------------------------
+# The reference itself (oracle/_ref), where it was built.
+
+def ref_available():
+    return os.path.exists(REF_LIB)
+
+
+def ref_lib():
+    global _rlib
+    if _rlib is None:
+        if not ref_available():
+            raise FileNotFoundError("reference build %s not present" % REF_LIB)
+        lib = ctypes.CDLL(REF_LIB)
+        lib.ref_kokkos_create.argtypes = [ctypes.POINTER(ctypes.c_int), _D, ctypes.c_double]
+        lib.ref_kokkos_create.restype = ctypes.c_void_p
+        lib.ref_kokkos_destroy.argtypes = [ctypes.c_void_p]
+        lib.ref_kokkos_update_fields.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.ref_kokkos_zeroed_currents.argtypes = [ctypes.c_void_p]
+        lib.ref_kokkos_field.argtypes = [ctypes.c_void_p, ctypes.c_int, _D, ctypes.c_long, ctypes.c_int]
+        lib.ref_kokkos_field.restype = ctypes.c_int
+        lib.ref_run_test_kokkos.argtypes = [ctypes.c_int] * 6
+        lib.ref_run_test_kokkos.restype = ctypes.c_double
+        lib.ref_last_error.restype = ctypes.c_char_p
+        lib.ref_omp_create.argtypes = [ctypes.POINTER(ctypes.c_int), _D, ctypes.c_double]
+        lib.ref_omp_create.restype = ctypes.c_void_p
+        lib.ref_omp_destroy.argtypes = [ctypes.c_void_p]
+        lib.ref_omp_update_fields.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.ref_omp_field.argtypes = [ctypes.c_void_p, ctypes.c_int, _D, ctypes.c_long, ctypes.c_int]
+        lib.ref_omp_field.restype = ctypes.c_int
+        _rlib = lib
+    return _rlib
+
+
+class RefKokkos:
+    """FDTD_kokkos::FDTD from the reference's own sources (oracle/_ref).
+    kind="kokkos" (the north-star path) or "openmp" (its OpenMP twin)."""
+
+    def __init__(self, params, dt, kind="kokkos"):
+        lib = ref_lib()
+        self.kind = kind
+        n = (ctypes.c_int * 3)(params.Ni, params.Nj, params.Nk)
+        b = (ctypes.c_double * 9)(params.ax, params.bx, params.ay, params.by, params.az, params.bz,
+                                  params.dx, params.dy, params.dz)
+        create = lib.ref_kokkos_create if kind == "kokkos" else lib.ref_omp_create
+        self.h = create(n, b, float(dt))
+        if not self.h:
+            raise ValueError(lib.ref_last_error().decode())
+        self.n = params.Ni * params.Nj * params.Nk
+
+    def close(self):
+        if self.h:
+            (ref_lib().ref_kokkos_destroy if self.kind == "kokkos" else ref_lib().ref_omp_destroy)(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _field(self, comp, buf, direction):
+        fn = ref_lib().ref_kokkos_field if self.kind == "kokkos" else ref_lib().ref_omp_field
+        rc = fn(self.h, int(comp), _ptr(buf), self.n, direction)
+        if rc == -2:
+            raise RuntimeError(ref_lib().ref_last_error().decode())
+        if rc != 0:
+            raise ValueError(ref_lib().ref_last_error().decode())
+
+    def set(self, comp, values):
+        a = np.ascontiguousarray(values, dtype=np.float64).reshape(-1).copy()
+        self._field(comp, a, 1)
+
+    def get(self, comp):
+        a = np.empty(self.n)
+        self._field(comp, a, 0)
+        return a
+
+    def update_fields(self, steps=1):
+        (ref_lib().ref_kokkos_update_fields if self.kind == "kokkos" else ref_lib().ref_omp_update_fields)(self.h, int(steps))
+
+    def zeroed_currents(self):
+        ref_lib().ref_kokkos_zeroed_currents(self.h)
+
+
+def run_reference_unit_tests():
+    """Runs the reference's own unit tests (oracle/_ref/ref_unit_tests) and
+    returns {test name: (value, expected, tol, passed)}."""
+    exe = os.path.join(REF_DIR, "ref_unit_tests")
+    r = subprocess.run([exe], capture_output=True, text=True, check=True)
+    out = {}
+    for line in r.stdout.splitlines():
+        parts = line.split()
+        if parts and parts[0] == "NEAR":
+            out[parts[1]] = (float(parts[2]), float(parts[3]), float(parts[4]), parts[5] == "PASS")
+    return out

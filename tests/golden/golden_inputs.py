@@ -1,0 +1,32 @@
+"""Seeded inputs of the golden reference cases (shared by the generator and
+the tests).  Values are k / 2^20 for integers k drawn by numpy's PCG64, so
+every host regenerates them bit for bit."""
+import numpy as np
+
+# name -> grid, domain, steps, seed, which components get random data
+CASES = {
+    "random_12x10x7": {"n": (12, 10, 7), "steps": 5, "seed": 11, "comps": range(9)},
+    "random_noJ_9x6x5": {"n": (9, 6, 5), "steps": 7, "seed": 12, "comps": range(6)},
+    "tiny_1x1x1": {"n": (1, 1, 1), "steps": 4, "seed": 13, "comps": range(9)},
+    "line_5x1x3": {"n": (5, 1, 3), "steps": 4, "seed": 14, "comps": range(9)},
+    "line_1x7x1": {"n": (1, 7, 1), "steps": 3, "seed": 15, "comps": range(9)},
+    "odd_7x3x5": {"n": (7, 3, 5), "steps": 6, "seed": 16, "comps": range(9)},
+    "wide_33x2x2": {"n": (33, 2, 2), "steps": 5, "seed": 17, "comps": range(9)},
+}
+
+
+def case_params(spec):
+    from fdtd_method_gb300.fdtd import Parameters
+    Ni, Nj, Nk = spec["n"]
+    # the reference unit tests' domain [0,1]x[0,2]x[0,3] (unit-tests/test_FDTD_method_kokkos.cpp:21-31)
+    p = Parameters(Ni, Nj, Nk, 0.0, 1.0, 0.0, 2.0, 0.0, 3.0, 1.0 / Ni, 2.0 / Nj, 3.0 / Nk)
+    # Courant number 0.3 on the finest axis
+    dt = 0.3 * min(p.dx, p.dy, p.dz) / 3e10
+    return p, dt
+
+
+def case_inputs(spec):
+    rng = np.random.default_rng(spec["seed"])
+    n = spec["n"][0] * spec["n"][1] * spec["n"][2]
+    return {c: rng.integers(-(1 << 20), 1 << 20, size=n).astype(np.float64) / float(1 << 20)
+            for c in spec["comps"]}

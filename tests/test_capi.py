@@ -1,0 +1,69 @@
+"""The C-ABI library: it builds for sm_103a, loads, exports every symbol
+include/fdtd_gb300.h declares, and validates arguments on the host before any
+GPU work (so these run without a GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from fdtd_method_gb300 import FDTD, InvalidArgument, Parameters, Precision, _lib, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "fdtd_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(fdtd_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for required in ("fdtd_create", "fdtd_destroy", "fdtd_update_fields", "fdtd_step",
+                     "fdtd_zeroed_currents", "fdtd_get_field", "fdtd_copy_field_to_host",
+                     "fdtd_copy_field_from_host", "fdtd_add_source", "fdtd_field_sums",
+                     "fdtd_synchronize", "fdtd_last_error"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    assert set(declared_functions()) <= set(_lib.SIGNATURES)
+
+
+def test_abi_version(lib):
+    assert lib.fdtd_abi_version() == 1
+
+
+@pytest.mark.parametrize("dims,dt", [((0, 4, 4), 1e-12), ((4, 0, 4), 1e-12), ((4, 4, -2), 1e-12),
+                                     ((4, 4, 4), 0.0), ((4, 4, 4), -1.0)])
+def test_invalid_parameters_raise_like_the_reference(lib, dims, dt):
+    # src/FDTD_kokkos/FDTD_kokkos.cpp:7-12 throws std::invalid_argument("ERROR: invalid parameters")
+    p = Parameters(*dims, 0, 1, 0, 1, 0, 1, 0.25, 0.25, 0.25)
+    with pytest.raises(InvalidArgument, match="ERROR: invalid parameters"):
+        FDTD(p, dt)
+    with pytest.raises(ValueError):
+        FDTD(p, dt)
+
+
+def test_invalid_precision_rejected(lib):
+    p = Parameters(4, 4, 4, 0, 1, 0, 1, 0, 1, 0.25, 0.25, 0.25)
+    h = ctypes.c_void_p()
+    cp = p.to_c()
+    assert lib.fdtd_create(ctypes.byref(cp), 1e-12, 7, ctypes.byref(h)) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert b"precision" in lib.fdtd_last_error()
+
+
+def test_null_handle_calls_fail_cleanly(lib):
+    assert lib.fdtd_step(None, 1) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_update_fields(None) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_destroy(None) == 0
+    assert Precision.FP32_COMP == 2
