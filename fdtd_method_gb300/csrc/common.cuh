@@ -33,9 +33,9 @@ constexpr int kMaxSources = 64;
 
 struct SourceSet {
   int count;
-  const DevSource* src;   // device array [count]
-  const double* tables;   // device buffer holding every profile and amplitude table
-  const int64_t* step;    // device step counter (completed update_fields steps)
+  const DevSource* src;    // device array [count]
+  const double* tables;    // device buffer holding every profile and amplitude table
+  const float* tables_f;   // the same tables rounded to FP32
 };
 
 // Offset of index v inside the periodic window [o, o+n) of an axis of length N,

@@ -70,6 +70,10 @@ struct fdtd_handle {
   // words (FP32_COMP), jf[0..2] FP32 current arrays (allocated on first use).
   void* field[9] = {nullptr};
   int8_t* lo[6] = {nullptr};
+  // Second copy of E/B (and lo) that the fused sweep writes into; swapped
+  // with field/lo after every fused step.
+  void* alt_field[6] = {nullptr};
+  int8_t* alt_lo[6] = {nullptr};
   float* jf[3] = {nullptr};
   bool dense_j = false;  // the E update reads the dense J arrays
   int fp16_exp[6] = {0, 0, 0, 0, 0, 0};
@@ -79,8 +83,12 @@ struct fdtd_handle {
   DevSource* d_src = nullptr;
   double* d_tables = nullptr;
   float* d_tables_f = nullptr;
-  int64_t* d_step = nullptr;
-  int64_t host_step = 0;
+  int64_t host_step = 0;  // completed update_fields steps
+
+  // Step pipeline of the FP32-arithmetic forms (FP64 always uses the split
+  // sweeps, whose FP64 instruction count is the smallest).
+  int pipeline = FDTD_PIPELINE_AUTO;
+  FusedConfig fused_cfg;
 
   // Scratch.
   double* d_staging = nullptr;
@@ -98,27 +106,29 @@ struct fdtd_handle {
   std::vector<TimedLaunch> timed;
   std::vector<cudaEvent_t> event_pool;
 
-  StateView view() const {
+  StateView make_view(void* const* f, int8_t* const* l) const {
     StateView v{};
     v.form = form;
     v.g = g;
-    for (int c = 0; c < 6; ++c) v.f64[c] = (form == Form::F64) ? (double*)field[c] : nullptr;
+    for (int c = 0; c < 6; ++c) v.f64[c] = (form == Form::F64) ? (double*)f[c] : nullptr;
     for (int c = 0; c < 6; ++c) {
-      v.s32.v[c] = (float*)field[c];
-      v.s32c.hi[c] = (float*)field[c];
-      v.s32c.lo[c] = lo[c];
-      v.s16.v[c] = (__half*)field[c];
+      v.s32.v[c] = (float*)f[c];
+      v.s32c.hi[c] = (float*)f[c];
+      v.s32c.lo[c] = l[c];
+      v.s16.v[c] = (__half*)f[c];
       v.s16.scale[c] = std::ldexp(1.0f, fp16_exp[c]);
       v.s16.inv_scale[c] = std::ldexp(1.0f, -fp16_exp[c]);
     }
     return v;
   }
+  StateView view() const { return make_view(field, lo); }
+  StateView view_alt() const { return make_view(alt_field, alt_lo); }
   SourceSet source_set() const {
     SourceSet ss{};
     ss.count = (int)sources.size();
     ss.src = d_src;
     ss.tables = d_tables;
-    ss.step = d_step;
+    ss.tables_f = d_tables_f;
     return ss;
   }
 };
@@ -246,22 +256,21 @@ struct LaunchTimer {
   }
 };
 
-// B update with `apps` applications of the curl term; `inc` bumps the
-// device step counter (the sweep that completes a step).
-int run_b(fdtd_handle* h, int apps, bool inc) {
+// B update with `apps` applications of the curl term (2: the last half
+// step of one update_fields and the first of the next share one sweep).
+int run_b(fdtd_handle* h, int apps) {
   LaunchTimer lt(h, apps == 2 ? FDTD_KERNEL_B_DOUBLE : FDTD_KERNEL_B_HALF);
-  int64_t* step_inc = inc ? h->d_step : nullptr;
   cudaError_t e = cudaSuccess;
   if (h->form == Form::F64) {
     Fp64Fields F;
     for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c];
-    e = launch_b_fp64(h->g, F, &h->coef[3], apps, step_inc, h->stream);
+    e = launch_b_fp64(h->g, F, &h->coef[3], apps, h->stream);
   } else {
     StateView v = h->view();
     switch (h->form) {
-      case Form::F32: e = launch_b_f32(h->g, v.s32, h->cs, apps, step_inc, h->stream); break;
-      case Form::F32C: e = launch_b_f32(h->g, v.s32c, h->cs, apps, step_inc, h->stream); break;
-      case Form::F16: e = launch_b_f32(h->g, v.s16, h->cs, apps, step_inc, h->stream); break;
+      case Form::F32: e = launch_b_f32(h->g, v.s32, h->cs, apps, h->stream); break;
+      case Form::F32C: e = launch_b_f32(h->g, v.s32c, h->cs, apps, h->stream); break;
+      case Form::F16: e = launch_b_f32(h->g, v.s16, h->cs, apps, h->stream); break;
       default: break;
     }
   }
@@ -270,27 +279,67 @@ int run_b(fdtd_handle* h, int apps, bool inc) {
   return FDTD_OK;
 }
 
-int run_e(fdtd_handle* h) {
+// E update of time step `step` (indexes the source amplitude tables).
+int run_e(fdtd_handle* h, int64_t step) {
   LaunchTimer lt(h, FDTD_KERNEL_E);
   SourceSet ss = h->source_set();
   cudaError_t e = cudaSuccess;
   if (h->form == Form::F64) {
     Fp64Fields F;
     for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c];
-    e = launch_e_fp64(h->g, F, &h->coef[0], h->coef[6], h->dense_j, ss, h->stream);
+    e = launch_e_fp64(h->g, F, &h->coef[0], h->coef[6], h->dense_j, ss, step, h->stream);
   } else {
     StateView v = h->view();
     const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
     const bool dj = h->dense_j && h->jf[0];
     switch (h->form) {
-      case Form::F32: e = launch_e_f32(h->g, v.s32, J, dj, h->cs, ss, h->d_tables_f, h->stream); break;
-      case Form::F32C: e = launch_e_f32(h->g, v.s32c, J, dj, h->cs, ss, h->d_tables_f, h->stream); break;
-      case Form::F16: e = launch_e_f32(h->g, v.s16, J, dj, h->cs, ss, h->d_tables_f, h->stream); break;
+      case Form::F32: e = launch_e_f32(h->g, v.s32, J, dj, h->cs, ss, step, h->stream); break;
+      case Form::F32C: e = launch_e_f32(h->g, v.s32c, J, dj, h->cs, ss, step, h->stream); break;
+      case Form::F16: e = launch_e_f32(h->g, v.s16, J, dj, h->cs, ss, step, h->stream); break;
       default: break;
     }
   }
   lt.done();
   if (e != cudaSuccess) return cuda_fail(e, "E update launch");
+  return FDTD_OK;
+}
+
+// E step `step` followed by `apps` B half steps, in one sweep.
+// Second copy of the E/B storage for the fused sweep (allocated on first use).
+int ensure_alt(fdtd_handle* h) {
+  if (h->alt_field[0]) return FDTD_OK;
+  const size_t eb = elem_bytes(h->form);
+  for (int c = 0; c < 6; ++c) {
+    FDTD_CUDA(dev_alloc(h, &h->alt_field[c], eb * h->g.cells), "second field copy");
+    if (h->form == Form::F32C)
+      FDTD_CUDA(dev_alloc(h, (void**)&h->alt_lo[c], h->g.cells), "second compensation copy");
+  }
+  return FDTD_OK;
+}
+
+int run_fused(fdtd_handle* h, int64_t step, int apps) {
+  if (int rc = ensure_alt(h)) return rc;
+  LaunchTimer lt(h, FDTD_KERNEL_FUSED);
+  SourceSet ss = h->source_set();
+  StateView v = h->view();
+  StateView w = h->view_alt();
+  const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
+  const bool dj = h->dense_j && h->jf[0];
+  const FusedConfig& cf = h->fused_cfg;
+  cudaError_t e = cudaSuccess;
+  switch (h->form) {
+    case Form::F32: e = launch_fused_f32(h->g, v.s32, w.s32, J, dj, h->cs, ss, step, apps, cf, h->stream); break;
+    case Form::F32C: e = launch_fused_f32(h->g, v.s32c, w.s32c, J, dj, h->cs, ss, step, apps, cf, h->stream); break;
+    case Form::F16: e = launch_fused_f32(h->g, v.s16, w.s16, J, dj, h->cs, ss, step, apps, cf, h->stream); break;
+    default: e = cudaErrorInvalidValue; break;
+  }
+  lt.done();
+  if (e != cudaSuccess) return cuda_fail(e, "fused step launch");
+  // The stepped state is now in the second copy: make it current.
+  for (int c = 0; c < 6; ++c) {
+    std::swap(h->field[c], h->alt_field[c]);
+    std::swap(h->lo[c], h->alt_lo[c]);
+  }
   return FDTD_OK;
 }
 
@@ -341,6 +390,7 @@ int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle
     h->cs.cb[a] = split_coef(h->coef[3 + a]);
   }
   h->cs.cj = split_coef(h->coef[6]);
+  h->cs.cj64 = h->coef[6];
   if (h->form != Form::F32C) {  // only the compensated form carries coefficient lo parts
     for (int a = 0; a < 3; ++a) h->cs.ce[a].lo = h->cs.cb[a].lo = 0.f;
     h->cs.cj.lo = 0.f;
@@ -376,10 +426,8 @@ int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle
       }
     }
   }
-  e = dev_alloc(h, (void**)&h->d_step, sizeof(int64_t));
-  if (e == cudaSuccess) e = dev_alloc(h, (void**)&h->d_partials, sizeof(double) * kDiagValues * kMaxDiagBlocks);
+  e = dev_alloc(h, (void**)&h->d_partials, sizeof(double) * kDiagValues * kMaxDiagBlocks);
   if (e == cudaSuccess) e = dev_alloc(h, (void**)&h->d_diag_out, sizeof(double) * kDiagValues);
-  if (e == cudaSuccess) e = cudaMemsetAsync(h->d_step, 0, sizeof(int64_t), h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) {
     int rc = cuda_fail(e, "handle set-up");
@@ -445,10 +493,16 @@ int fdtd_step(fdtd_handle* h, int64_t n) {
   DeviceGuard dg(h->device);
   // src/FDTD_kokkos/FDTD_kokkos.cpp:91-104 repeated n times; the trailing B
   // half step of one step and the leading one of the next share one sweep.
-  if (int rc = run_b(h, 1, false)) return rc;
+  const bool fused = h->form != Form::F64 && h->pipeline != FDTD_PIPELINE_SPLIT;
+  if (int rc = run_b(h, 1)) return rc;
   for (int64_t s = 0; s < n; ++s) {
-    if (int rc = run_e(h)) return rc;
-    if (int rc = run_b(h, s + 1 < n ? 2 : 1, true)) return rc;
+    const int apps = s + 1 < n ? 2 : 1;
+    if (fused) {
+      if (int rc = run_fused(h, h->host_step + s, apps)) return rc;
+    } else {
+      if (int rc = run_e(h, h->host_step + s)) return rc;
+      if (int rc = run_b(h, apps)) return rc;
+    }
   }
   h->host_step += n;
   return FDTD_OK;
@@ -602,9 +656,20 @@ int fdtd_get_step(fdtd_handle* h, int64_t* step) {
 int fdtd_set_step(fdtd_handle* h, int64_t step) {
   if (int rc = check_handle(h)) return rc;
   if (step < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "negative step");
-  DeviceGuard dg(h->device);
-  FDTD_CUDA(launch_set_i64(h->d_step, step, h->stream), "set step");
   h->host_step = step;
+  return FDTD_OK;
+}
+
+int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk) {
+  if (int rc = check_handle(h)) return rc;
+  if (pipeline < FDTD_PIPELINE_AUTO || pipeline > FDTD_PIPELINE_FUSED)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid pipeline");
+  if (tile_y != 0 && tile_y != 8 && tile_y != 16)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "tile_y must be 0 (default), 8 or 16");
+  if (kchunk < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "kchunk must be >= 0");
+  h->pipeline = pipeline;
+  h->fused_cfg.tile_y = tile_y ? tile_y : 16;
+  h->fused_cfg.kchunk = kchunk ? kchunk : 64;
   return FDTD_OK;
 }
 

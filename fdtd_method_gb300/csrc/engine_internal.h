@@ -16,25 +16,36 @@ struct Fp64Fields {
 };
 
 struct CoefSet {
-  Coef cb[3];
-  Coef ce[3];
-  Coef cj;
+  Coef cb[3];   // C dt / (2 d) per axis, split hi + lo
+  Coef ce[3];   // C dt / d per axis
+  Coef cj;      // -4 pi dt
+  double cj64;  // -4 pi dt in FP64 (current term of the compensated form)
+};
+
+// Launch shape of the fused step kernel (tile rows, z chunk).
+struct FusedConfig {
+  int tile_y = 16;
+  int kchunk = 64;
 };
 
 // kernels_fp64.cu
 cudaError_t launch_b_fp64(const Grid& g, const Fp64Fields& F, const double cb[3], int applications,
-                          int64_t* step_inc, cudaStream_t st);
+                          cudaStream_t st);
 cudaError_t launch_e_fp64(const Grid& g, const Fp64Fields& F, const double ce[3], double cJ,
-                          bool dense_j, const SourceSet& ss, cudaStream_t st);
+                          bool dense_j, const SourceSet& ss, int64_t step, cudaStream_t st);
 
 // kernels_f32.cu
 template <class S>
 cudaError_t launch_b_f32(const Grid& g, const S& st, const CoefSet& cs, int applications,
-                         int64_t* step_inc, cudaStream_t stream);
+                         cudaStream_t stream);
 template <class S>
 cudaError_t launch_e_f32(const Grid& g, const S& st, const float* const J[3], bool dense_j,
-                         const CoefSet& cs, const SourceSet& ss, const float* tables_f,
-                         cudaStream_t stream);
+                         const CoefSet& cs, const SourceSet& ss, int64_t step, cudaStream_t stream);
+// Reads the state from `st`, writes the stepped state to `out`.
+template <class S>
+cudaError_t launch_fused_f32(const Grid& g, const S& st, const S& out, const float* const J[3],
+                             bool dense_j, const CoefSet& cs, const SourceSet& ss, int64_t step,
+                             int applications, const FusedConfig& cfg, cudaStream_t stream);
 
 // misc.cu — conversions, diagnostics, small helpers.
 enum class Form { F64 = 0, F32 = 1, F32C = 2, F16 = 3 };

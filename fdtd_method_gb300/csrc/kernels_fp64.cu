@@ -31,11 +31,10 @@ __global__ void __launch_bounds__(256) b_update_fp64(Grid g, const double* __res
                                                      const double* __restrict__ Ez,
                                                      double* __restrict__ Bx, double* __restrict__ By,
                                                      double* __restrict__ Bz, double cx, double cy,
-                                                     double cz, int kchunk, int64_t* step_inc) {
+                                                     double cz, int kchunk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k0 = blockIdx.z * kchunk;
-  if (step_inc && i == 0 && j == 0 && k0 == 0) *step_inc += 1;
   if (i >= g.Ni || j >= g.Nj || k0 >= g.Nk) return;
   const int k1 = min(k0 + kchunk, g.Nk);
   const int64_t col = i + (int64_t)j * g.Ni;
@@ -89,7 +88,8 @@ __global__ void __launch_bounds__(256) e_update_fp64(Grid g, const double* __res
                                                      const double* __restrict__ Jz,
                                                      double* __restrict__ Ex, double* __restrict__ Ey,
                                                      double* __restrict__ Ez, double cJ, double cx,
-                                                     double cy, double cz, int kchunk, SourceSet ss) {
+                                                     double cy, double cz, int kchunk, SourceSet ss,
+                                                     int64_t s) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k0 = blockIdx.z * kchunk;
@@ -98,8 +98,6 @@ __global__ void __launch_bounds__(256) e_update_fp64(Grid g, const double* __res
   const int64_t col = i + (int64_t)j * g.Ni;
   const int64_t col_ip = wrap_prev(i, g.Ni) + (int64_t)j * g.Ni;
   const int64_t col_jp = i + (int64_t)wrap_prev(j, g.Nj) * g.Ni;
-  int64_t s = 0;
-  if (kSources) s = *ss.step;
 
   int64_t base = (int64_t)k0 * g.plane;
   const int64_t pbase0 = (int64_t)wrap_prev(k0, g.Nk) * g.plane;
@@ -151,27 +149,27 @@ static dim3 fp64_grid(const Grid& g, int kchunk) {
 }
 
 cudaError_t launch_b_fp64(const Grid& g, const Fp64Fields& F, const double cb[3], int applications,
-                          int64_t* step_inc, cudaStream_t st) {
+                          cudaStream_t st) {
   const int kchunk = 16;
   dim3 block(32, 8), grid = fp64_grid(g, kchunk);
   if (applications == 2)
     b_update_fp64<2><<<grid, block, 0, st>>>(g, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5],
-                                             cb[0], cb[1], cb[2], kchunk, step_inc);
+                                             cb[0], cb[1], cb[2], kchunk);
   else
     b_update_fp64<1><<<grid, block, 0, st>>>(g, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5],
-                                             cb[0], cb[1], cb[2], kchunk, step_inc);
+                                             cb[0], cb[1], cb[2], kchunk);
   return cudaGetLastError();
 }
 
 cudaError_t launch_e_fp64(const Grid& g, const Fp64Fields& F, const double ce[3], double cJ,
-                          bool dense_j, const SourceSet& ss, cudaStream_t st) {
+                          bool dense_j, const SourceSet& ss, int64_t step, cudaStream_t st) {
   const int kchunk = 16;
   dim3 block(32, 8), grid = fp64_grid(g, kchunk);
   const bool src = ss.count > 0;
 #define FDTD_E64(DJ, SRC)                                                                     \
   e_update_fp64<DJ, SRC><<<grid, block, 0, st>>>(g, F.f[3], F.f[4], F.f[5], F.f[6], F.f[7],   \
                                                  F.f[8], F.f[0], F.f[1], F.f[2], cJ, ce[0],   \
-                                                 ce[1], ce[2], kchunk, ss)
+                                                 ce[1], ce[2], kchunk, ss, step)
   if (dense_j && src) FDTD_E64(true, true);
   else if (dense_j) FDTD_E64(true, false);
   else if (src) FDTD_E64(false, true);

@@ -33,6 +33,8 @@ struct StoreF32 {
   __device__ __forceinline__ float load_hi(int c, int64_t idx) const { return v[c][idx]; }
   __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const { v[c][idx] = p.hi; }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const { return (double)v[c][idx]; }
+  // The value a store followed by a load returns.
+  __device__ __forceinline__ Pair quantize(int, Pair p) const { return Pair{p.hi, 0.f}; }
 };
 
 // FP16 storage with a power-of-two scale per component: stored = field * 2^e.
@@ -52,6 +54,9 @@ struct StoreF16 {
   }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const {
     return (double)__half2float(v[c][idx]) * (double)inv_scale[c];
+  }
+  __device__ __forceinline__ Pair quantize(int c, Pair p) const {
+    return Pair{__half2float(__float2half_rn(p.hi * scale[c])) * inv_scale[c], 0.f};
   }
 };
 
@@ -79,11 +84,16 @@ struct StoreF32C {
     return Pair{h, (float)lo[c][idx] * lo_decode_scale(h)};
   }
   __device__ __forceinline__ float load_hi(int c, int64_t idx) const { return hi[c][idx]; }
+  __device__ __forceinline__ static int encode_lo(Pair p) {
+    const int q = __float2int_rn(p.lo * lo_encode_scale(p.hi));
+    return max(-127, min(127, q));
+  }
   __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const {
     hi[c][idx] = p.hi;
-    int q = __float2int_rn(p.lo * lo_encode_scale(p.hi));
-    q = max(-127, min(127, q));
-    lo[c][idx] = (int8_t)q;
+    lo[c][idx] = (int8_t)encode_lo(p);
+  }
+  __device__ __forceinline__ Pair quantize(int, Pair p) const {
+    return Pair{p.hi, (float)encode_lo(p) * lo_decode_scale(p.hi)};
   }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const {
     const float h = hi[c][idx];

@@ -299,6 +299,12 @@ class FDTD:
         _lib.check(self._lib.fdtd_set_fp16_exponents(self._handle(), arr))
 
     KERNEL_KINDS = ("e_update", "b_half", "b_double", "fused_step")
+    PIPELINES = {"auto": 0, "split": 1, "fused": 2}
+
+    def set_pipeline(self, pipeline="auto", tile_y=0, kchunk=0):
+        """Step pipeline of the FP32-arithmetic forms: 'fused' (one sweep per
+        step, the default) or 'split' (one sweep per half step); same results."""
+        _lib.check(self._lib.fdtd_set_pipeline(self._handle(), self.PIPELINES[pipeline], int(tile_y), int(kchunk)))
 
     def set_kernel_timing(self, enabled):
         """Bracket every step-pipeline kernel launch with CUDA events."""

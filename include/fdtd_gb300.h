@@ -49,8 +49,10 @@ enum fdtd_component {
  *                 reference's operation order with no fused multiply-add, so
  *                 results are bit-identical to the reference's.
  *   FP32        — FP32 storage and arithmetic.
- *   FP32_COMP   — FP32 arithmetic; each E/B value stored as an FP32 "hi" word
- *                 plus a 16-bit "lo" correction word (compensated storage).
+ *   FP32_COMP   — compensated: each E/B value stored as an FP32 "hi" word plus
+ *                 a signed 8-bit "lo" word in units of 2^-30 of hi's binary
+ *                 exponent (a 30-bit significand in 5 bytes), updated with
+ *                 error-free FP32 transformations (TwoSum, FMA products).
  *   FP16_SCALED — FP16 storage with a power-of-two scale per component and
  *                 FP32 arithmetic. */
 enum fdtd_precision {
@@ -180,6 +182,15 @@ enum fdtd_kernel_kind {
     FDTD_KERNEL_KINDS = 4
 };
 int fdtd_set_kernel_timing(fdtd_handle* h, int enabled);
+
+/* Step pipeline of the FP32-arithmetic forms (new; tuning and testing).
+ * AUTO and FUSED: one sweep per step (E step + double B half step); SPLIT:
+ * one sweep per half step.  Both give bit-identical results.  tile_y (rows
+ * of a fused tile: 0 = default 16, or 8) and kchunk (planes per fused tile:
+ * 0 = default 64) shape the fused launch.  The FP64 form always uses the
+ * split sweeps. */
+enum fdtd_pipeline { FDTD_PIPELINE_AUTO = 0, FDTD_PIPELINE_SPLIT = 1, FDTD_PIPELINE_FUSED = 2 };
+int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk);
 int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t launches[FDTD_KERNEL_KINDS]);
 
 #ifdef __cplusplus
