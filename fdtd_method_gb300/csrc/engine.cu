@@ -11,6 +11,7 @@
 
 #include "../../include/fdtd_gb300.h"
 #include "engine_internal.h"
+#include "tma.cuh"
 
 using namespace fdtd;
 
@@ -89,6 +90,13 @@ struct fdtd_handle {
   // sweeps, whose FP64 instruction count is the smallest).
   int pipeline = FDTD_PIPELINE_AUTO;
   FusedConfig fused_cfg;
+  PLayout L{};  // padded layout of the FP32-arithmetic forms
+  // TMA maps of the current and the second copy (rebuilt when the tile
+  // shape changes; swapped with the copies).
+  TmaMaps maps_cur;
+  TmaMaps maps_alt;
+  int maps_tile_y = 0;
+  int* d_err = nullptr;  // device status word (bounded waits that gave up)
 
   // Scratch.
   double* d_staging = nullptr;
@@ -110,6 +118,7 @@ struct fdtd_handle {
     StateView v{};
     v.form = form;
     v.g = g;
+    v.L = L;
     for (int c = 0; c < 6; ++c) v.f64[c] = (form == Form::F64) ? (double*)f[c] : nullptr;
     for (int c = 0; c < 6; ++c) {
       v.s32.v[c] = (float*)f[c];
@@ -268,9 +277,9 @@ int run_b(fdtd_handle* h, int apps) {
   } else {
     StateView v = h->view();
     switch (h->form) {
-      case Form::F32: e = launch_b_f32(h->g, v.s32, h->cs, apps, h->stream); break;
-      case Form::F32C: e = launch_b_f32(h->g, v.s32c, h->cs, apps, h->stream); break;
-      case Form::F16: e = launch_b_f32(h->g, v.s16, h->cs, apps, h->stream); break;
+      case Form::F32: e = launch_b_f32(h->L, v.s32, h->cs, apps, h->stream); break;
+      case Form::F32C: e = launch_b_f32(h->L, v.s32c, h->cs, apps, h->stream); break;
+      case Form::F16: e = launch_b_f32(h->L, v.s16, h->cs, apps, h->stream); break;
       default: break;
     }
   }
@@ -293,9 +302,9 @@ int run_e(fdtd_handle* h, int64_t step) {
     const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
     const bool dj = h->dense_j && h->jf[0];
     switch (h->form) {
-      case Form::F32: e = launch_e_f32(h->g, v.s32, J, dj, h->cs, ss, step, h->stream); break;
-      case Form::F32C: e = launch_e_f32(h->g, v.s32c, J, dj, h->cs, ss, step, h->stream); break;
-      case Form::F16: e = launch_e_f32(h->g, v.s16, J, dj, h->cs, ss, step, h->stream); break;
+      case Form::F32: e = launch_e_f32(h->L, v.s32, J, dj, h->cs, ss, step, h->stream); break;
+      case Form::F32C: e = launch_e_f32(h->L, v.s32c, J, dj, h->cs, ss, step, h->stream); break;
+      case Form::F16: e = launch_e_f32(h->L, v.s16, J, dj, h->cs, ss, step, h->stream); break;
       default: break;
     }
   }
@@ -304,19 +313,36 @@ int run_e(fdtd_handle* h, int64_t step) {
   return FDTD_OK;
 }
 
-// E step `step` followed by `apps` B half steps, in one sweep.
-// Second copy of the E/B storage for the fused sweep (allocated on first use).
+// Second copy of the E/B storage for the fused sweep (allocated on first
+// use) and the TMA maps of both copies for the current tile shape.
 int ensure_alt(fdtd_handle* h) {
-  if (h->alt_field[0]) return FDTD_OK;
-  const size_t eb = elem_bytes(h->form);
-  for (int c = 0; c < 6; ++c) {
-    FDTD_CUDA(dev_alloc(h, &h->alt_field[c], eb * h->g.cells), "second field copy");
-    if (h->form == Form::F32C)
-      FDTD_CUDA(dev_alloc(h, (void**)&h->alt_lo[c], h->g.cells), "second compensation copy");
+  if (!h->alt_field[0]) {
+    const size_t eb = elem_bytes(h->form);
+    for (int c = 0; c < 6; ++c) {
+      FDTD_CUDA(dev_alloc(h, &h->alt_field[c], eb * h->L.elems()), "second field copy");
+      FDTD_CUDA(cudaMemsetAsync(h->alt_field[c], 0, eb * h->L.elems(), h->stream), "zero second copy");
+      if (h->form == Form::F32C) {
+        FDTD_CUDA(dev_alloc(h, (void**)&h->alt_lo[c], h->L.elems()), "second compensation copy");
+        FDTD_CUDA(cudaMemsetAsync(h->alt_lo[c], 0, h->L.elems(), h->stream), "zero second copy");
+      }
+    }
+    h->maps_tile_y = 0;
+  }
+  if (h->maps_tile_y != h->fused_cfg.tile_y) {
+    const HiType ht = h->form == Form::F16 ? HiType::F16 : HiType::F32;
+    const int bw = h->form == Form::F16 ? fused_box_width<StoreF16>() : fused_box_width<StoreF32>();
+    int8_t* const* lo_cur = h->form == Form::F32C ? h->lo : nullptr;
+    int8_t* const* lo_alt = h->form == Form::F32C ? h->alt_lo : nullptr;
+    if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, h->fused_cfg.tile_y) != cudaSuccess ||
+        build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, h->fused_cfg.tile_y) != cudaSuccess)
+      return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
+    h->maps_tile_y = h->fused_cfg.tile_y;
   }
   return FDTD_OK;
 }
 
+// E step `step` followed by `apps` B half steps, in one sweep from the
+// current copy into the second one, which then becomes current.
 int run_fused(fdtd_handle* h, int64_t step, int apps) {
   if (int rc = ensure_alt(h)) return rc;
   LaunchTimer lt(h, FDTD_KERNEL_FUSED);
@@ -326,20 +352,21 @@ int run_fused(fdtd_handle* h, int64_t step, int apps) {
   const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
   const bool dj = h->dense_j && h->jf[0];
   const FusedConfig& cf = h->fused_cfg;
+  const void* m = &h->maps_cur;
   cudaError_t e = cudaSuccess;
   switch (h->form) {
-    case Form::F32: e = launch_fused_f32(h->g, v.s32, w.s32, J, dj, h->cs, ss, step, apps, cf, h->stream); break;
-    case Form::F32C: e = launch_fused_f32(h->g, v.s32c, w.s32c, J, dj, h->cs, ss, step, apps, cf, h->stream); break;
-    case Form::F16: e = launch_fused_f32(h->g, v.s16, w.s16, J, dj, h->cs, ss, step, apps, cf, h->stream); break;
+    case Form::F32: e = launch_fused_f32(h->L, v.s32, w.s32, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;
+    case Form::F32C: e = launch_fused_f32(h->L, v.s32c, w.s32c, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;
+    case Form::F16: e = launch_fused_f32(h->L, v.s16, w.s16, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;
     default: e = cudaErrorInvalidValue; break;
   }
   lt.done();
   if (e != cudaSuccess) return cuda_fail(e, "fused step launch");
-  // The stepped state is now in the second copy: make it current.
   for (int c = 0; c < 6; ++c) {
     std::swap(h->field[c], h->alt_field[c]);
     std::swap(h->lo[c], h->alt_lo[c]);
   }
+  std::swap(h->maps_cur, h->maps_alt);
   return FDTD_OK;
 }
 
@@ -404,11 +431,15 @@ int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle
   }
   h->stream = h->own_stream;
 
+  // FP64: the reference's nine dense arrays.  Other forms: six padded E/B
+  // arrays (ghosts included) and, for FP32_COMP, six padded lo arrays.
+  h->L = PLayout::make(params->Ni, params->Nj, params->Nk);
   const size_t eb = elem_bytes(h->form);
   const int nfields = (h->form == Form::F64) ? 9 : 6;
+  const int64_t per_field = (h->form == Form::F64) ? h->g.cells : h->L.elems();
   for (int c = 0; c < nfields; ++c) {
-    e = dev_alloc(h, &h->field[c], eb * h->g.cells);
-    if (e == cudaSuccess) e = cudaMemsetAsync(h->field[c], 0, eb * h->g.cells, h->stream);
+    e = dev_alloc(h, &h->field[c], eb * per_field);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->field[c], 0, eb * per_field, h->stream);
     if (e != cudaSuccess) {
       int rc = cuda_fail(e, "field allocation");
       release(h);
@@ -417,8 +448,8 @@ int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle
   }
   if (h->form == Form::F32C) {
     for (int c = 0; c < 6; ++c) {
-      e = dev_alloc(h, (void**)&h->lo[c], h->g.cells);
-      if (e == cudaSuccess) e = cudaMemsetAsync(h->lo[c], 0, h->g.cells, h->stream);
+      e = dev_alloc(h, (void**)&h->lo[c], per_field);
+      if (e == cudaSuccess) e = cudaMemsetAsync(h->lo[c], 0, per_field, h->stream);
       if (e != cudaSuccess) {
         int rc = cuda_fail(e, "compensation allocation");
         release(h);
@@ -428,6 +459,8 @@ int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle
   }
   e = dev_alloc(h, (void**)&h->d_partials, sizeof(double) * kDiagValues * kMaxDiagBlocks);
   if (e == cudaSuccess) e = dev_alloc(h, (void**)&h->d_diag_out, sizeof(double) * kDiagValues);
+  if (e == cudaSuccess) e = dev_alloc(h, (void**)&h->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) {
     int rc = cuda_fail(e, "handle set-up");
@@ -664,11 +697,11 @@ int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk) {
   if (int rc = check_handle(h)) return rc;
   if (pipeline < FDTD_PIPELINE_AUTO || pipeline > FDTD_PIPELINE_FUSED)
     return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid pipeline");
-  if (tile_y != 0 && tile_y != 8 && tile_y != 16)
-    return fail(FDTD_ERR_INVALID_ARGUMENT, "tile_y must be 0 (default), 8 or 16");
+  if (tile_y != 0 && tile_y != 6 && tile_y != 14)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "tile_y must be 0 (default), 6 or 14");
   if (kchunk < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "kchunk must be >= 0");
   h->pipeline = pipeline;
-  h->fused_cfg.tile_y = tile_y ? tile_y : 16;
+  h->fused_cfg.tile_y = tile_y ? tile_y : 14;
   h->fused_cfg.kchunk = kchunk ? kchunk : 64;
   return FDTD_OK;
 }
@@ -706,6 +739,12 @@ int fdtd_synchronize(fdtd_handle* h) {
   if (int rc = check_handle(h)) return rc;
   DeviceGuard dg(h->device);
   FDTD_CUDA(cudaStreamSynchronize(h->stream), "synchronize");
+  int status = 0;
+  FDTD_CUDA(cudaMemcpy(&status, h->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read device status");
+  if (status != 0) {
+    cudaMemset(h->d_err, 0, sizeof(int));
+    return fail(FDTD_ERR_TIMEOUT, "a bounded wait in a step kernel gave up; results of that step are invalid");
+  }
   return FDTD_OK;
 }
 

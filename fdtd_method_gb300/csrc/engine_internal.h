@@ -7,6 +7,7 @@
 #include <cstdint>
 
 #include "common.cuh"
+#include "layout.cuh"
 #include "storage.cuh"
 
 namespace fdtd {
@@ -22,9 +23,10 @@ struct CoefSet {
   double cj64;  // -4 pi dt in FP64 (current term of the compensated form)
 };
 
-// Launch shape of the fused step kernel (tile rows, z chunk).
+// Launch shape of the fused step kernel: interior tile rows (14 or 6) and
+// planes per tile.
 struct FusedConfig {
-  int tile_y = 16;
+  int tile_y = 14;
   int kchunk = 64;
 };
 
@@ -34,36 +36,48 @@ cudaError_t launch_b_fp64(const Grid& g, const Fp64Fields& F, const double cb[3]
 cudaError_t launch_e_fp64(const Grid& g, const Fp64Fields& F, const double ce[3], double cJ,
                           bool dense_j, const SourceSet& ss, int64_t step, cudaStream_t st);
 
-// kernels_f32.cu
+// kernels_f32.cu (padded layout)
 template <class S>
-cudaError_t launch_b_f32(const Grid& g, const S& st, const CoefSet& cs, int applications,
+cudaError_t launch_b_f32(const PLayout& L, const S& st, const CoefSet& cs, int applications,
                          cudaStream_t stream);
 template <class S>
-cudaError_t launch_e_f32(const Grid& g, const S& st, const float* const J[3], bool dense_j,
+cudaError_t launch_e_f32(const PLayout& L, const S& st, const float* const J[3], bool dense_j,
                          const CoefSet& cs, const SourceSet& ss, int64_t step, cudaStream_t stream);
-// Reads the state from `st`, writes the stepped state to `out`.
+// Reads the state from `st` (through the TMA maps in `maps`, a TmaMaps
+// built by build_tma_maps for `st`'s arrays), writes the stepped state to `out`.
 template <class S>
-cudaError_t launch_fused_f32(const Grid& g, const S& st, const S& out, const float* const J[3],
-                             bool dense_j, const CoefSet& cs, const SourceSet& ss, int64_t step,
-                             int applications, const FusedConfig& cfg, cudaStream_t stream);
+cudaError_t launch_fused_f32(const PLayout& L, const S& st, const S& out, const void* maps,
+                             const float* const J[3], bool dense_j, const CoefSet& cs,
+                             const SourceSet& ss, int64_t step, int applications,
+                             const FusedConfig& cfg, int* err, cudaStream_t stream);
+template <class S>
+int fused_box_width();
+size_t tma_maps_bytes();
+
+// tma_maps.cu: tensor maps of the six hi arrays (and six lo arrays of the
+// compensated form) for a fused tile of `tile_y` interior rows.
+enum class HiType { F32, F16 };
+cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6],
+                           int8_t* const lo[6], int box_w, int tile_y);
 
 // misc.cu — conversions, diagnostics, small helpers.
 enum class Form { F64 = 0, F32 = 1, F32C = 2, F16 = 3 };
 
 struct StateView {
   Form form;
-  Grid g;
+  Grid g;      // logical grid
+  PLayout L;   // padded layout of the FP32-arithmetic forms
   double* f64[6];
   StoreF32 s32;
   StoreF32C s32c;
   StoreF16 s16;
 };
 
-// Writes component c (0..5) of the state from n FP64 values at `src` starting
-// at flat offset `off`.
+// Writes component c (0..5) of the state from n FP64 values at `src`, the
+// logical cells off .. off+n-1 (flat index i + j*Ni + k*Ni*Nj), ghosts included.
 cudaError_t launch_import(const StateView& v, int c, const double* src, int64_t off, int64_t n,
                           cudaStream_t st);
-// Reads component c (0..5) of the state as FP64 into `dst`.
+// Reads component c (0..5) of the state as FP64 into `dst` (logical cells).
 cudaError_t launch_export(const StateView& v, int c, double* dst, int64_t off, int64_t n,
                           cudaStream_t st);
 // FP64 -> FP32 conversion of n values.
@@ -76,7 +90,5 @@ constexpr int kDiagThreads = 256;
 int diag_blocks_for(int64_t cells, int max_blocks);
 cudaError_t launch_field_sums(const StateView& v, double* partials, int nblocks, double* out_dev,
                               cudaStream_t st);
-
-cudaError_t launch_set_i64(int64_t* dst, int64_t value, cudaStream_t st);
 
 }  // namespace fdtd

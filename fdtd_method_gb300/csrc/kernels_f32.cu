@@ -1,18 +1,21 @@
 // FP32-arithmetic Yee kernels of the precision forms (plain FP32,
-// compensated FP32 hi + int8 lo, FP16 with per-component scale).
+// compensated FP32 hi + int8 lo, FP16 with per-component scale), on the
+// padded layout of layout.cuh.
 //
 // Same stencil as the FP64 drop-in (kokkos_functors.h:64-90 E, :128-151 B);
 // the arithmetic comes from the policies in arith.cuh.
 //
 // Two pipelines compute identical values (the tests check bit equality):
-//  * split: one z-marching sweep per update (B half step, E step, B double
-//    half step) — 18 values moved per cell-step;
+//  * split: one z-marching sweep per update, in place (B half step, E step,
+//    B double half step) — 18 values moved per cell-step;
 //  * fused: one sweep per step.  Between the first and last half step of a
 //    run the scheme is E <- E + c curl B followed by B <- B + 2 (c/2) curl E,
-//    so one kernel does both on a 2-D tile of columns marching along z:
-//    12 values moved per cell-step (read E, B; write E, B).
+//    so one kernel does both on a tile of columns marching along z, reading
+//    plane tiles through TMA: 12 values moved per cell-step (read E, B;
+//    write E, B).
 #include "arith.cuh"
 #include "engine_internal.h"
+#include "tma.cuh"
 
 namespace fdtd {
 
@@ -43,20 +46,21 @@ template <class T> __device__ __forceinline__ const T* table_of(const SourceSet&
 template <> __device__ __forceinline__ const double* table_of<double>(const SourceSet& ss) { return ss.tables; }
 template <> __device__ __forceinline__ const float* table_of<float>(const SourceSet& ss) { return ss.tables_f; }
 
-// Sum over every source at (i, j, k) for time step s: ((amp gx) gy) gz.
+// Sum over every source at logical cell (i, j, k) for time step s:
+// ((amp gx) gy) gz, sources in registration order.
 template <class T>
 __device__ __forceinline__ bool source_sum(const SourceSet& ss, int64_t s, int i, int j, int k,
-                                           const Grid& g, T jv[3]) {
+                                           const PLayout& L, T jv[3]) {
   const T* tb = table_of<T>(ss);
   bool any = false;
   for (int q = 0; q < ss.count; ++q) {
     const DevSource& d = ss.src[q];
     if (s >= d.n_amp) continue;
-    const int dk = box_offset(k, d.k0, d.nk, g.Nk);
+    const int dk = box_offset(k, d.k0, d.nk, L.Nk);
     if (dk < 0) continue;
-    const int dj = box_offset(j, d.j0, d.nj, g.Nj);
+    const int dj = box_offset(j, d.j0, d.nj, L.Nj);
     if (dj < 0) continue;
-    const int di = box_offset(i, d.i0, d.ni, g.Ni);
+    const int di = box_offset(i, d.i0, d.ni, L.Ni);
     if (di < 0) continue;
     const T v = mul_rn(mul_rn(mul_rn(tb[d.amp_off + s], tb[d.gx_off + di]), tb[d.gy_off + dj]),
                        tb[d.gz_off + dk]);
@@ -69,25 +73,24 @@ __device__ __forceinline__ bool source_sum(const SourceSet& ss, int64_t s, int i
 }
 
 // ---------------------------------------------------------------------------
-// Split pipeline.
+// Split pipeline: z-marching sweeps, one thread per (x, y) column.  x/y
+// neighbours come from the ghost cells; z wraps by index.
 
 template <class S, class A, int kApplications>
-__global__ void __launch_bounds__(256) b_sweep(Grid g, S st, CoefSet cs, int kchunk) {
+__global__ void __launch_bounds__(256) b_sweep(PLayout L, S st, CoefSet cs, int kchunk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k0 = blockIdx.z * kchunk;
-  if (i >= g.Ni || j >= g.Nj || k0 >= g.Nk) return;
-  const int k1 = min(k0 + kchunk, g.Nk);
-  const int64_t col = i + (int64_t)j * g.Ni;
-  const int64_t col_in = wrap_next(i, g.Ni) + (int64_t)j * g.Ni;
-  const int64_t col_jn = i + (int64_t)wrap_next(j, g.Nj) * g.Ni;
+  if (i >= L.Ni || j >= L.Nj || k0 >= L.Nk) return;
+  const int k1 = min(k0 + kchunk, L.Nk);
   const Coef cx = cs.cb[0], cy = cs.cb[1], cz = cs.cb[2];
+  const int64_t col = L.at(i, j, 0), col_in = L.at(i + 1, j, 0), col_jn = L.at(i, j + 1, 0);
 
-  int64_t base = (int64_t)k0 * g.plane;
-  Pair ex = st.load(0, col + base);
-  Pair ey = st.load(1, col + base);
+  Pair ex = st.load(0, col + (int64_t)k0 * L.pplane);
+  Pair ey = st.load(1, col + (int64_t)k0 * L.pplane);
   for (int k = k0; k < k1; ++k) {
-    const int64_t nbase = (int64_t)wrap_next(k, g.Nk) * g.plane;
+    const int64_t base = (int64_t)k * L.pplane;
+    const int64_t nbase = (int64_t)wrap_next(k, L.Nk) * L.pplane;
     const Pair ex_kn = st.load(0, col + nbase);
     const Pair ey_kn = st.load(1, col + nbase);
     const Pair ez = st.load(2, col + base);
@@ -99,17 +102,16 @@ __global__ void __launch_bounds__(256) b_sweep(Grid g, S st, CoefSet cs, int kch
       ty = A::twice(ty);
       tz = A::twice(tz);
     }
-    st.store(3, col + base, A::acc(st.load(3, col + base), tx));
-    st.store(4, col + base, A::acc(st.load(4, col + base), ty));
-    st.store(5, col + base, A::acc(st.load(5, col + base), tz));
+    store_with_ghosts(st, L, 3, i, j, k, A::acc(st.load(3, col + base), tx));
+    store_with_ghosts(st, L, 4, i, j, k, A::acc(st.load(4, col + base), ty));
+    store_with_ghosts(st, L, 5, i, j, k, A::acc(st.load(5, col + base), tz));
     ex = ex_kn;
     ey = ey_kn;
-    base = nbase;
   }
 }
 
 template <class S, class A, bool kDenseJ, bool kSources>
-__global__ void __launch_bounds__(256) e_sweep(Grid g, S st, const float* __restrict__ Jx,
+__global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __restrict__ Jx,
                                                const float* __restrict__ Jy,
                                                const float* __restrict__ Jz, CoefSet cs, int kchunk,
                                                SourceSet ss, int64_t step) {
@@ -117,18 +119,18 @@ __global__ void __launch_bounds__(256) e_sweep(Grid g, S st, const float* __rest
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k0 = blockIdx.z * kchunk;
-  if (i >= g.Ni || j >= g.Nj || k0 >= g.Nk) return;
-  const int k1 = min(k0 + kchunk, g.Nk);
-  const int64_t col = i + (int64_t)j * g.Ni;
-  const int64_t col_ip = wrap_prev(i, g.Ni) + (int64_t)j * g.Ni;
-  const int64_t col_jp = i + (int64_t)wrap_prev(j, g.Nj) * g.Ni;
+  if (i >= L.Ni || j >= L.Nj || k0 >= L.Nk) return;
+  const int k1 = min(k0 + kchunk, L.Nk);
   const Coef cx = cs.ce[0], cy = cs.ce[1], cz = cs.ce[2];
+  const int64_t col = L.at(i, j, 0), col_ip = L.at(i - 1, j, 0), col_jp = L.at(i, j - 1, 0);
+  const int64_t dcol = i + (int64_t)j * L.Ni;  // dense current index
+  const int64_t dplane = (int64_t)L.Ni * L.Nj;
 
-  int64_t base = (int64_t)k0 * g.plane;
-  const int64_t pbase0 = (int64_t)wrap_prev(k0, g.Nk) * g.plane;
+  const int64_t pbase0 = (int64_t)wrap_prev(k0, L.Nk) * L.pplane;
   Pair bx_kp = st.load(3, col + pbase0);
   Pair by_kp = st.load(4, col + pbase0);
   for (int k = k0; k < k1; ++k) {
+    const int64_t base = (int64_t)k * L.pplane;
     const Pair bx = st.load(3, col + base);
     const Pair by = st.load(4, col + base);
     const Pair bz = st.load(5, col + base);
@@ -138,154 +140,196 @@ __global__ void __launch_bounds__(256) e_sweep(Grid g, S st, const float* __rest
     T jv[3] = {0, 0, 0};
     bool has_j = false;
     if (kDenseJ) {
-      jv[0] = Jx[col + base];
-      jv[1] = Jy[col + base];
-      jv[2] = Jz[col + base];
+      const int64_t d = dcol + (int64_t)k * dplane;
+      jv[0] = Jx[d];
+      jv[1] = Jy[d];
+      jv[2] = Jz[d];
       has_j = true;
     }
-    if (kSources) has_j |= source_sum<T>(ss, step, i, j, k, g, jv);
+    if (kSources) has_j |= source_sum<T>(ss, step, i, j, k, L, jv);
     if (has_j) {
       tx = A::add(tx, current_term<A>(cs, jv[0]));
       ty = A::add(ty, current_term<A>(cs, jv[1]));
       tz = A::add(tz, current_term<A>(cs, jv[2]));
     }
-    st.store(0, col + base, A::acc(st.load(0, col + base), tx));
-    st.store(1, col + base, A::acc(st.load(1, col + base), ty));
-    st.store(2, col + base, A::acc(st.load(2, col + base), tz));
+    store_with_ghosts(st, L, 0, i, j, k, A::acc(st.load(0, col + base), tx));
+    store_with_ghosts(st, L, 1, i, j, k, A::acc(st.load(1, col + base), ty));
+    store_with_ghosts(st, L, 2, i, j, k, A::acc(st.load(2, col + base), tz));
     bx_kp = bx;
     by_kp = by;
-    base += g.plane;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Fused pipeline: E step + B (double) half step in one sweep.
+// Fused pipeline.
 //
-// The sweep reads the state from `st` and writes the new state to `out` (a
-// second copy of the fields; the engine swaps the two after each step):
-// tiles read halo columns and the first plane of the next z chunk, which
-// their neighbours update in the same launch, so an in-place update would race.
-//
-// A CTA owns a tile of (32-2) x (TY-2) interior columns plus a one-column
-// halo on every side, one thread per column, and marches the planes
-// k0..k1 of its z chunk.  In iteration t it
-//   1. loads E(t), B(t) of its column and publishes B(t) in shared memory;
-//   2. computes E'(t) = E + c curl B (needs B at i-1, j-1 from shared memory
-//      and B(t-1) carried in registers) on interior and high-halo columns;
-//   3. computes B'(t-1) = B(t-1) + apps (c/2) curl E' (needs E'(t-1) at
-//      i+1, j+1 from shared memory, E'(t) in registers) on interior columns;
-//   4. stores E'(t) (t < k1) and B'(t-1); publishes E'(t).
-// Plane k1 (the next chunk's first) is read and its E' computed but not
-// stored; plane k0-1 contributes only B(k0-1) of the own column.
-// Low-halo columns (i = x0-1 or j = y0-1) only load B.
+// A CTA owns an interior tile of 32 x RY columns at (x0, y0) and marches the
+// planes k0..k1 of its z chunk, reading each plane of all six components as
+// one TMA box per array (rows y0-1 .. y0+RY, columns x0-4 .. x0+35 for FP32
+// words, x0-16 .. x0+47 for the int8 lo words, x0-8 .. x0+39 for FP16),
+// NS planes ahead through an mbarrier ring.  Warps 0..RY are rows 1..RY+1 of
+// the box (row RY+1 computes E' only, for its neighbours); warp RY+1 computes
+// E' on column x0+nx (the x halo) for rows 1..RY.  In iteration t every
+// thread
+//   1. computes E'(t) = E + c curl B of its cell (B at i-1, j-1 from the
+//      box, B(t-1) carried in registers);
+//   2. computes B'(t-1) = B(t-1) + apps (c/2) curl E' (E'(t-1) at i+1, j+1
+//      from shared memory, E'(t) in registers) on interior cells;
+//   3. stores E'(t) (t < k1) and B'(t-1), publishes E'(t), and the CTA
+//      synchronises once; thread 0 then refills the freed ring slot.
+// The sweep reads the state from `st` and writes the new state to `out`:
+// neighbouring tiles read what a tile writes, so an in-place update would race.
 
-constexpr int kFusedTX = 32;
-constexpr int kFusedMaxFastSources = 4;
+constexpr int kFusedStages = 3;
+// Sources whose per-column factor the fused kernel keeps in registers; more
+// sources take the generic per-cell loop.
+constexpr int kFastSources = 2;
 
-template <class S, class A, int TY, int kApps, bool kDenseJ, int kSrc>
-__global__ void __launch_bounds__(kFusedTX* TY) fused_step(Grid g, S st, S out, CoefSet cs, int kchunk,
-                                                          const float* __restrict__ Jx,
-                                                          const float* __restrict__ Jy,
-                                                          const float* __restrict__ Jz,
-                                                          SourceSet ss, int64_t step) {
-  constexpr int TX = kFusedTX;
-  constexpr int NV = A::kPairs ? 2 : 1;
+template <class S> struct BoxTraits;
+template <> struct BoxTraits<StoreF32> { static constexpr int kW = 40, kOff = 4, kLoW = 0; };
+template <> struct BoxTraits<StoreF32C> { static constexpr int kW = 40, kOff = 4, kLoW = 64; };
+template <> struct BoxTraits<StoreF16> { static constexpr int kW = 48, kOff = 8, kLoW = 0; };
+constexpr int kLoOff = 16;
+
+template <class S, int RY>
+struct FusedSmem {
+  using HiT = typename S::HiT;
+  static constexpr int ROWS = RY + 2;
+  static constexpr int W = BoxTraits<S>::kW;
+  static constexpr int LW = BoxTraits<S>::kLoW;
+  static constexpr int NV = S::kComp ? 2 : 1;
+  static constexpr int kHiBytes = 6 * ROWS * W * (int)sizeof(HiT);
+  static constexpr int kLoBytes = 6 * ROWS * LW;
+  static constexpr int kStageBytes = (kHiBytes + kLoBytes + 127) / 128 * 128;
+  static constexpr int kEBytes = 2 * 3 * NV * ROWS * 33 * 4;
+  static constexpr int kTotal = kFusedStages * kStageBytes + kEBytes + kFusedStages * 8;
+  static constexpr uint32_t kTx = kHiBytes + kLoBytes;
+};
+
+template <class S, class A, int RY, int kApps, bool kDenseJ, int kSrc>
+__global__ void __launch_bounds__(32 * (RY + 2))
+    fused_tma(PLayout L, S st, S out, const __grid_constant__ TmaMaps maps, CoefSet cs, int kchunk,
+              const float* __restrict__ Jx, const float* __restrict__ Jy,
+              const float* __restrict__ Jz, SourceSet ss, int64_t step, int* err) {
+  using SM = FusedSmem<S, RY>;
+  using HiT = typename S::HiT;
   using T = typename CurT<A>::T;
-  __shared__ float sB[3][NV][TY][TX];
-  __shared__ float sE[2][3][NV][TY][TX];
+  constexpr int ROWS = SM::ROWS, W = SM::W, LW = SM::LW, NV = SM::NV, OFF = BoxTraits<S>::kOff;
+  constexpr int NS = kFusedStages;
+  constexpr int EC = 33;  // columns of the E' exchange (32 interior + the x halo)
+  extern __shared__ __align__(128) unsigned char smem[];
+  float* sE = reinterpret_cast<float*>(smem + NS * SM::kStageBytes);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NS * SM::kStageBytes + SM::kEBytes);
+  auto hi_of = [&](int slot) { return reinterpret_cast<const HiT*>(smem + slot * SM::kStageBytes); };
+  auto lo_of = [&](int slot) {
+    return reinterpret_cast<const int8_t*>(smem + slot * SM::kStageBytes + SM::kHiBytes);
+  };
+  // sE[buf][c][v][row][col]
+  auto se = [&](int buf, int c, int v, int row, int col) -> float& {
+    return sE[(((buf * 3 + c) * NV + v) * ROWS + row) * EC + col];
+  };
 
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int x0 = blockIdx.x * (TX - 2), y0 = blockIdx.y * (TY - 2);
-  const int nx = min(TX - 2, g.Ni - x0), ny = min(TY - 2, g.Nj - y0);
-  const int ox = tx - 1, oy = ty - 1;
-  const bool off = ox > nx || oy > ny;
-  const bool do_e = !off && ox >= 0 && oy >= 0;
-  const bool inner = do_e && ox < nx && oy < ny;
-  int x = x0 + ox, y = y0 + oy;
-  x = x < 0 ? x + g.Ni : (x >= g.Ni ? x - g.Ni : x);
-  y = y < 0 ? y + g.Nj : (y >= g.Nj ? y - g.Nj : y);
-  if (off) x = y = 0;
-  const int64_t col = x + (int64_t)y * g.Ni;
+  const int lane = threadIdx.x, w = threadIdx.y;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * RY;
+  const int nx = min(32, L.Ni - x0), ny = min(RY, L.Nj - y0);
+  const bool halo = (w == RY + 1);
+  const int r = halo ? lane + 1 : w + 1;   // box row
+  const int cx = halo ? nx : lane;          // column within the tile (0..32)
+  const bool active = halo ? (lane < ny) : (r <= ny + 1 && lane < nx);
+  const bool interior = !halo && r <= ny && lane < nx;
+  // logical coordinates of the cell (x = Ni and y = Nj are the ghost copies of 0)
+  const int xu = x0 + cx, yu = y0 + r - 1;
+  const int xl = xu >= L.Ni ? xu - L.Ni : xu, yl = yu >= L.Nj ? yu - L.Nj : yu;
   const int k0 = blockIdx.z * kchunk;
-  const int k1 = min(k0 + kchunk, g.Nk);
+  const int k1 = min(k0 + kchunk, L.Nk);
+  const bool producer = (w == 0 && lane == 0);
 
-  // Sources: the per-column factor amp * gx * gy, once per launch.
-  T sxy[kFusedMaxFastSources];
-  int nsrc = 0;
-  if (kSrc == 1) {
-    nsrc = ss.count;
+  auto issue = [&](int t) {
+    const int slot = (t - k0) % NS;
+    const int kk = (t == L.Nk) ? 0 : t;
+    unsigned char* base = smem + slot * SM::kStageBytes;
+    mbar_arrive_expect_tx(&bar[slot], SM::kTx);
+    for (int c = 0; c < 6; ++c)
+      tma_load_3d(base + c * ROWS * W * sizeof(HiT), &maps.hi[c], x0 + kPadX - OFF, y0, kk, &bar[slot]);
+    if (S::kComp)
+      for (int c = 0; c < 6; ++c)
+        tma_load_3d(base + SM::kHiBytes + c * ROWS * LW, &maps.lo[c], x0 + kPadX - kLoOff, y0, kk,
+                    &bar[slot]);
+  };
+
+  if (producer) {
+    for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (producer)
+    for (int t = k0; t <= k1 && t < k0 + NS; ++t) issue(t);
+
+  // Sources: per-column factor amp * gx * gy, once per launch.
+  T sxy[kFastSources];
+  unsigned smask = 0;
+  if (kSrc == 1 && active) {
 #pragma unroll
-    for (int q = 0; q < kFusedMaxFastSources; ++q) {
-      sxy[q] = 0;
-      if (q < nsrc && do_e) {
+    for (int q = 0; q < kFastSources; ++q) {
+      sxy[q] = T(0);
+      if (q < ss.count) {
         const DevSource& d = ss.src[q];
-        const int di = box_offset(x, d.i0, d.ni, g.Ni);
-        const int dj = box_offset(y, d.j0, d.nj, g.Nj);
+        const int di = box_offset(xl, d.i0, d.ni, L.Ni);
+        const int dj = box_offset(yl, d.j0, d.nj, L.Nj);
         if (step < d.n_amp && di >= 0 && dj >= 0) {
           const T* tb = table_of<T>(ss);
           sxy[q] = mul_rn(mul_rn(tb[d.amp_off + step], tb[d.gx_off + di]), tb[d.gy_off + dj]);
+          smask |= 1u << q;
         }
       }
     }
   }
 
-  auto put = [&](float* a, Pair v) {
-    a[0] = v.hi;
-    if (NV == 2) a[TY * TX] = v.lo;
-  };
-  auto get = [&](const float* a) { return Pair{a[0], NV == 2 ? a[TY * TX] : 0.f}; };
-
   Pair pbx{0.f, 0.f}, pby{0.f, 0.f}, pbz{0.f, 0.f};
   Pair pex{0.f, 0.f}, pey{0.f, 0.f}, pez{0.f, 0.f};
-  if (do_e) {
-    const int64_t b0 = (int64_t)wrap_prev(k0, g.Nk) * g.plane;
-    pbx = st.load(3, col + b0);
-    pby = st.load(4, col + b0);
+  if (active) {
+    const int64_t b0 = L.at(xu, yu, wrap_prev(k0, L.Nk));
+    pbx = st.load(3, b0);
+    pby = st.load(4, b0);
   }
 
   for (int t = k0; t <= k1; ++t) {
-    const int kk = (t == g.Nk) ? 0 : t;
-    const int64_t base = (int64_t)kk * g.plane;
+    const int slot = (t - k0) % NS;
     const int cur = t & 1;
-    Pair bx{0.f, 0.f}, by{0.f, 0.f}, bz{0.f, 0.f}, ex{0.f, 0.f}, ey{0.f, 0.f}, ez{0.f, 0.f};
-    if (!off) {
-      bx = st.load(3, col + base);
-      by = st.load(4, col + base);
-      bz = st.load(5, col + base);
-      put(&sB[0][0][ty][tx], bx);
-      put(&sB[1][0][ty][tx], by);
-      put(&sB[2][0][ty][tx], bz);
-    }
-    if (do_e) {
-      ex = st.load(0, col + base);
-      ey = st.load(1, col + base);
-      ez = st.load(2, col + base);
-    }
-    __syncthreads();
+    mbar_wait_bounded(&bar[slot], ((t - k0) / NS) & 1, err);
+    const HiT* H = hi_of(slot);
+    const int8_t* Lo = lo_of(slot);
+    auto val = [&](int c, int row, int col) -> Pair {
+      const HiT h = H[(c * ROWS + row) * W + col + OFF];
+      const int8_t q = S::kComp ? Lo[(c * ROWS + row) * LW + col + kLoOff] : int8_t(0);
+      return st.decode(c, h, q);
+    };
 
-    Pair nex{0.f, 0.f}, ney{0.f, 0.f}, nez{0.f, 0.f};
-    if (do_e) {
-      const Pair bz_jp = get(&sB[2][0][ty - 1][tx]);
-      const Pair bz_ip = get(&sB[2][0][ty][tx - 1]);
-      const Pair by_ip = get(&sB[1][0][ty][tx - 1]);
-      const Pair bx_jp = get(&sB[0][0][ty - 1][tx]);
-      Pair qx = curl_term<A>(cs.ce[1], bz, bz_jp, cs.ce[2], by, pby);
-      Pair qy = curl_term<A>(cs.ce[2], bx, pbx, cs.ce[0], bz, bz_ip);
-      Pair qz = curl_term<A>(cs.ce[0], by, by_ip, cs.ce[1], bx, bx_jp);
+    Pair bx{0.f, 0.f}, by{0.f, 0.f}, bz{0.f, 0.f}, nex{0.f, 0.f}, ney{0.f, 0.f}, nez{0.f, 0.f};
+    if (active) {
+      const int kk = (t == L.Nk) ? 0 : t;
+      bx = val(3, r, cx);
+      by = val(4, r, cx);
+      bz = val(5, r, cx);
+      const Pair ex = val(0, r, cx), ey = val(1, r, cx), ez = val(2, r, cx);
+      Pair qx = curl_term<A>(cs.ce[1], bz, val(5, r - 1, cx), cs.ce[2], by, pby);
+      Pair qy = curl_term<A>(cs.ce[2], bx, pbx, cs.ce[0], bz, val(5, r, cx - 1));
+      Pair qz = curl_term<A>(cs.ce[0], by, val(4, r, cx - 1), cs.ce[1], bx, val(3, r - 1, cx));
       T jv[3] = {0, 0, 0};
       bool has_j = false;
       if (kDenseJ) {
-        jv[0] = Jx[col + base];
-        jv[1] = Jy[col + base];
-        jv[2] = Jz[col + base];
+        const int64_t d = xl + (int64_t)yl * L.Ni + (int64_t)kk * L.Ni * L.Nj;
+        jv[0] = Jx[d];
+        jv[1] = Jy[d];
+        jv[2] = Jz[d];
         has_j = true;
       }
       if (kSrc == 1) {
 #pragma unroll
-        for (int q = 0; q < kFusedMaxFastSources; ++q) {
-          if (q < nsrc && sxy[q] != T(0)) {
+        for (int q = 0; q < kFastSources; ++q) {
+          if (smask & (1u << q)) {
             const DevSource& d = ss.src[q];
-            const int dk = box_offset(kk, d.k0, d.nk, g.Nk);
+            const int dk = box_offset(kk, d.k0, d.nk, L.Nk);
             if (dk >= 0) {
               const T v = mul_rn(sxy[q], table_of<T>(ss)[d.gz_off + dk]);
               if (d.comp_mask & 1) jv[0] = add_rn(jv[0], v);
@@ -296,48 +340,48 @@ __global__ void __launch_bounds__(kFusedTX* TY) fused_step(Grid g, S st, S out, 
           }
         }
       } else if (kSrc == 2) {
-        has_j |= source_sum<T>(ss, step, x, y, kk, g, jv);
+        has_j |= source_sum<T>(ss, step, xl, yl, kk, L, jv);
       }
       if (has_j) {
         qx = A::add(qx, current_term<A>(cs, jv[0]));
         qy = A::add(qy, current_term<A>(cs, jv[1]));
         qz = A::add(qz, current_term<A>(cs, jv[2]));
       }
-      // E' as its storage form will hold it, so that the B' update sees the
-      // same values the split sweeps reload from memory.
+      // E' as its storage form will hold it (what the split sweeps reload).
       nex = st.quantize(0, A::acc(ex, qx));
       ney = st.quantize(1, A::acc(ey, qy));
       nez = st.quantize(2, A::acc(ez, qz));
-    }
 
-    if (t > k0 && inner) {
-      const int prv = cur ^ 1;
-      const Pair ez_jn = get(&sE[prv][2][0][ty + 1][tx]);
-      const Pair ez_in = get(&sE[prv][2][0][ty][tx + 1]);
-      const Pair ey_in = get(&sE[prv][1][0][ty][tx + 1]);
-      const Pair ex_jn = get(&sE[prv][0][0][ty + 1][tx]);
-      Pair ux = curl_term<A>(cs.cb[2], ney, pey, cs.cb[1], ez_jn, pez);
-      Pair uy = curl_term<A>(cs.cb[0], ez_in, pez, cs.cb[2], nex, pex);
-      Pair uz = curl_term<A>(cs.cb[1], ex_jn, pex, cs.cb[0], ey_in, pey);
-      if (kApps == 2) {
-        ux = A::twice(ux);
-        uy = A::twice(uy);
-        uz = A::twice(uz);
+      if (interior && t > k0) {
+        const int prv = cur ^ 1;
+        auto eget = [&](int c, int row, int col) {
+          return Pair{se(prv, c, 0, row, col), NV == 2 ? se(prv, c, NV - 1, row, col) : 0.f};
+        };
+        Pair ux = curl_term<A>(cs.cb[2], ney, pey, cs.cb[1], eget(2, r + 1, cx), pez);
+        Pair uy = curl_term<A>(cs.cb[0], eget(2, r, cx + 1), pez, cs.cb[2], nex, pex);
+        Pair uz = curl_term<A>(cs.cb[1], eget(0, r + 1, cx), pex, cs.cb[0], eget(1, r, cx + 1), pey);
+        if (kApps == 2) {
+          ux = A::twice(ux);
+          uy = A::twice(uy);
+          uz = A::twice(uz);
+        }
+        store_with_ghosts(out, L, 3, xl, yl, t - 1, A::acc(pbx, ux));
+        store_with_ghosts(out, L, 4, xl, yl, t - 1, A::acc(pby, uy));
+        store_with_ghosts(out, L, 5, xl, yl, t - 1, A::acc(pbz, uz));
       }
-      const int64_t pb = (int64_t)(t - 1) * g.plane;
-      out.store(3, col + pb, A::acc(pbx, ux));
-      out.store(4, col + pb, A::acc(pby, uy));
-      out.store(5, col + pb, A::acc(pbz, uz));
-    }
-    if (t < k1 && inner) {
-      out.store(0, col + base, nex);
-      out.store(1, col + base, ney);
-      out.store(2, col + base, nez);
-    }
-    if (do_e) {
-      put(&sE[cur][0][0][ty][tx], nex);
-      put(&sE[cur][1][0][ty][tx], ney);
-      put(&sE[cur][2][0][ty][tx], nez);
+      if (interior && t < k1) {
+        store_with_ghosts(out, L, 0, xl, yl, t, nex);
+        store_with_ghosts(out, L, 1, xl, yl, t, ney);
+        store_with_ghosts(out, L, 2, xl, yl, t, nez);
+      }
+      se(cur, 0, 0, r, cx) = nex.hi;
+      se(cur, 1, 0, r, cx) = ney.hi;
+      se(cur, 2, 0, r, cx) = nez.hi;
+      if (NV == 2) {
+        se(cur, 0, NV - 1, r, cx) = nex.lo;
+        se(cur, 1, NV - 1, r, cx) = ney.lo;
+        se(cur, 2, NV - 1, r, cx) = nez.lo;
+      }
     }
     pbx = bx;
     pby = by;
@@ -346,6 +390,7 @@ __global__ void __launch_bounds__(kFusedTX* TY) fused_step(Grid g, S st, S out, 
     pey = ney;
     pez = nez;
     __syncthreads();
+    if (producer && t + NS <= k1) issue(t + NS);
   }
 }
 
@@ -355,30 +400,30 @@ __global__ void __launch_bounds__(kFusedTX* TY) fused_step(Grid g, S st, S out, 
 template <class S> struct ArithOf { using type = ArithPlain; };
 template <> struct ArithOf<StoreF32C> { using type = ArithComp; };
 
-static dim3 sweep_grid(const Grid& g, int kchunk) {
-  return dim3((g.Ni + 31) / 32, (g.Nj + 7) / 8, (g.Nk + kchunk - 1) / kchunk);
+static dim3 sweep_grid(const PLayout& L, int kchunk) {
+  return dim3((L.Ni + 31) / 32, (L.Nj + 7) / 8, (L.Nk + kchunk - 1) / kchunk);
 }
 
 template <class S>
-cudaError_t launch_b_f32(const Grid& g, const S& st, const CoefSet& cs, int applications,
+cudaError_t launch_b_f32(const PLayout& L, const S& st, const CoefSet& cs, int applications,
                          cudaStream_t stream) {
   using A = typename ArithOf<S>::type;
   const int kchunk = 16;
-  dim3 block(32, 8), grid = sweep_grid(g, kchunk);
-  if (applications == 2) b_sweep<S, A, 2><<<grid, block, 0, stream>>>(g, st, cs, kchunk);
-  else b_sweep<S, A, 1><<<grid, block, 0, stream>>>(g, st, cs, kchunk);
+  dim3 block(32, 8), grid = sweep_grid(L, kchunk);
+  if (applications == 2) b_sweep<S, A, 2><<<grid, block, 0, stream>>>(L, st, cs, kchunk);
+  else b_sweep<S, A, 1><<<grid, block, 0, stream>>>(L, st, cs, kchunk);
   return cudaGetLastError();
 }
 
 template <class S>
-cudaError_t launch_e_f32(const Grid& g, const S& st, const float* const J[3], bool dense_j,
+cudaError_t launch_e_f32(const PLayout& L, const S& st, const float* const J[3], bool dense_j,
                          const CoefSet& cs, const SourceSet& ss, int64_t step, cudaStream_t stream) {
   using A = typename ArithOf<S>::type;
   const int kchunk = 16;
-  dim3 block(32, 8), grid = sweep_grid(g, kchunk);
+  dim3 block(32, 8), grid = sweep_grid(L, kchunk);
   const bool src = ss.count > 0;
 #define FDTD_E32(DJ, SRC) \
-  e_sweep<S, A, DJ, SRC><<<grid, block, 0, stream>>>(g, st, J[0], J[1], J[2], cs, kchunk, ss, step)
+  e_sweep<S, A, DJ, SRC><<<grid, block, 0, stream>>>(L, st, J[0], J[1], J[2], cs, kchunk, ss, step)
   if (dense_j && src) FDTD_E32(true, true);
   else if (dense_j) FDTD_E32(true, false);
   else if (src) FDTD_E32(false, true);
@@ -387,51 +432,69 @@ cudaError_t launch_e_f32(const Grid& g, const S& st, const float* const J[3], bo
   return cudaGetLastError();
 }
 
-template <class S, int TY>
-static cudaError_t launch_fused_ty(const Grid& g, const S& st, const S& out, const float* const J[3],
-                                   bool dense_j, const CoefSet& cs, const SourceSet& ss, int64_t step,
-                                   int applications, int kchunk, cudaStream_t stream) {
+template <class S, int RY, int APPS, bool DJ, int SRC>
+static cudaError_t launch_fused_one(dim3 grid, const PLayout& L, const S& st, const S& out,
+                                    const TmaMaps& maps, const CoefSet& cs, int kchunk,
+                                    const float* const J[3], const SourceSet& ss, int64_t step,
+                                    int* err, cudaStream_t stream) {
   using A = typename ArithOf<S>::type;
-  dim3 block(kFusedTX, TY);
-  dim3 grid((g.Ni + kFusedTX - 3) / (kFusedTX - 2), (g.Nj + TY - 3) / (TY - 2),
-            (g.Nk + kchunk - 1) / kchunk);
-  const int src = ss.count == 0 ? 0 : (ss.count <= kFusedMaxFastSources ? 1 : 2);
-#define FDTD_FUSED(APPS, DJ, SRC)                                                                 \
-  fused_step<S, A, TY, APPS, DJ, SRC><<<grid, block, 0, stream>>>(g, st, out, cs, kchunk, J[0], \
-                                                                  J[1], J[2], ss, step)
-#define FDTD_FUSED_SRC(APPS, DJ)              \
-  if (src == 0) FDTD_FUSED(APPS, DJ, 0);      \
-  else if (src == 1) FDTD_FUSED(APPS, DJ, 1); \
-  else FDTD_FUSED(APPS, DJ, 2);
-  if (applications == 2) {
-    if (dense_j) { FDTD_FUSED_SRC(2, true) } else { FDTD_FUSED_SRC(2, false) }
-  } else {
-    if (dense_j) { FDTD_FUSED_SRC(1, true) } else { FDTD_FUSED_SRC(1, false) }
-  }
-#undef FDTD_FUSED_SRC
-#undef FDTD_FUSED
+  auto kern = fused_tma<S, A, RY, APPS, DJ, SRC>;
+  const int bytes = FusedSmem<S, RY>::kTotal;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(L, st, out, maps, cs, kchunk, J[0], J[1], J[2], ss,
+                                                  step, err);
   return cudaGetLastError();
 }
 
-template <class S>
-cudaError_t launch_fused_f32(const Grid& g, const S& st, const S& out, const float* const J[3],
-                             bool dense_j, const CoefSet& cs, const SourceSet& ss, int64_t step,
-                             int applications, const FusedConfig& cfg, cudaStream_t stream) {
-  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 64;
-  switch (cfg.tile_y) {
-    case 8: return launch_fused_ty<S, 8>(g, st, out, J, dense_j, cs, ss, step, applications, kchunk, stream);
-    default: return launch_fused_ty<S, 16>(g, st, out, J, dense_j, cs, ss, step, applications, kchunk, stream);
+template <class S, int RY>
+static cudaError_t launch_fused_ry(const PLayout& L, const S& st, const S& out, const TmaMaps& maps,
+                                   const float* const J[3], bool dense_j, const CoefSet& cs,
+                                   const SourceSet& ss, int64_t step, int applications, int kchunk,
+                                   int* err, cudaStream_t stream) {
+  dim3 grid((L.Ni + 31) / 32, (L.Nj + RY - 1) / RY, (L.Nk + kchunk - 1) / kchunk);
+  const int src = ss.count == 0 ? 0 : (ss.count <= kFastSources ? 1 : 2);
+#define FDTD_F(APPS, DJ, SRC) \
+  return launch_fused_one<S, RY, APPS, DJ, SRC>(grid, L, st, out, maps, cs, kchunk, J, ss, step, err, stream)
+#define FDTD_FS(APPS, DJ)        \
+  if (src == 0) FDTD_F(APPS, DJ, 0); \
+  if (src == 1) FDTD_F(APPS, DJ, 1); \
+  FDTD_F(APPS, DJ, 2);
+  if (applications == 2) {
+    if (dense_j) { FDTD_FS(2, true) } else { FDTD_FS(2, false) }
+  } else {
+    if (dense_j) { FDTD_FS(1, true) } else { FDTD_FS(1, false) }
   }
+#undef FDTD_FS
+#undef FDTD_F
 }
 
-#define FDTD_INSTANTIATE(S)                                                                         \
-  template cudaError_t launch_b_f32<S>(const Grid&, const S&, const CoefSet&, int, cudaStream_t);  \
-  template cudaError_t launch_e_f32<S>(const Grid&, const S&, const float* const[3], bool,         \
-                                       const CoefSet&, const SourceSet&, int64_t, cudaStream_t);   \
-  template cudaError_t launch_fused_f32<S>(const Grid&, const S&, const S&, const float* const[3], \
-                                           bool,                                                   \
-                                           const CoefSet&, const SourceSet&, int64_t, int,         \
-                                           const FusedConfig&, cudaStream_t);
+template <class S>
+cudaError_t launch_fused_f32(const PLayout& L, const S& st, const S& out, const void* maps,
+                             const float* const J[3], bool dense_j, const CoefSet& cs,
+                             const SourceSet& ss, int64_t step, int applications,
+                             const FusedConfig& cfg, int* err, cudaStream_t stream) {
+  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 64;
+  const TmaMaps& m = *static_cast<const TmaMaps*>(maps);
+  if (cfg.tile_y == 6)
+    return launch_fused_ry<S, 6>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
+  return launch_fused_ry<S, 14>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
+}
+
+template <class S>
+int fused_box_width() { return BoxTraits<S>::kW; }
+
+size_t tma_maps_bytes() { return sizeof(TmaMaps); }
+
+#define FDTD_INSTANTIATE(S)                                                                            \
+  template cudaError_t launch_b_f32<S>(const PLayout&, const S&, const CoefSet&, int, cudaStream_t); \
+  template cudaError_t launch_e_f32<S>(const PLayout&, const S&, const float* const[3], bool,         \
+                                       const CoefSet&, const SourceSet&, int64_t, cudaStream_t);      \
+  template cudaError_t launch_fused_f32<S>(const PLayout&, const S&, const S&, const void*,            \
+                                           const float* const[3], bool, const CoefSet&,               \
+                                           const SourceSet&, int64_t, int, const FusedConfig&, int*,  \
+                                           cudaStream_t);                                             \
+  template int fused_box_width<S>();
 FDTD_INSTANTIATE(StoreF32)
 FDTD_INSTANTIATE(StoreF32C)
 FDTD_INSTANTIATE(StoreF16)

@@ -1,0 +1,64 @@
+// Padded field layout of the FP32-arithmetic forms.
+//
+// Each component is stored as a 3-D array with a ghost row below and above
+// the grid in y and a 16-element margin left and right of it in x, so that
+//   * every x/y neighbour of a grid cell exists in memory (the ghost cells
+//     hold periodic copies: ghost x = -1 is cell Ni-1, ghost x = Ni is cell 0,
+//     likewise in y and at the four corners), and
+//   * each row starts on a 16-byte boundary (pitch is a multiple of 16
+//     elements), which TMA tile copies require.
+// The writer of a boundary cell also writes its ghost copies, so the ghosts
+// are current whenever the cell is.  z is not padded: planes wrap by index.
+//
+// The FP64 drop-in keeps the reference's dense layout i + j*Ni + k*Ni*Nj.
+#pragma once
+
+#include <cstdint>
+
+namespace fdtd {
+
+constexpr int kPadX = 16;
+
+struct PLayout {
+  int Ni, Nj, Nk;
+  int64_t pitch;   // elements per padded row
+  int64_t pplane;  // elements per padded plane = pitch * (Nj + 2)
+
+  __host__ __device__ __forceinline__ int64_t at(int x, int y, int z) const {
+    return (int64_t)(x + kPadX) + (int64_t)(y + 1) * pitch + (int64_t)z * pplane;
+  }
+  __host__ __device__ __forceinline__ int64_t elems() const { return pplane * Nk; }
+
+  static PLayout make(int Ni, int Nj, int Nk) {
+    PLayout L;
+    L.Ni = Ni;
+    L.Nj = Nj;
+    L.Nk = Nk;
+    L.pitch = ((int64_t)Ni + 2 * kPadX + 15) / 16 * 16;
+    L.pplane = L.pitch * (Nj + 2);
+    return L;
+  }
+};
+
+// Stores v at (x, y, z) and at every ghost position that mirrors it.
+template <class S, class V>
+__device__ __forceinline__ void store_with_ghosts(const S& st, const PLayout& L, int c, int x, int y,
+                                                  int z, V v) {
+  st.store(c, L.at(x, y, z), v);
+  const bool xl = (x == 0), xh = (x == L.Ni - 1), yl = (y == 0), yh = (y == L.Nj - 1);
+  if (!(xl || xh || yl || yh)) return;
+  // ghost columns of this row, then the ghost rows (with their corners)
+  if (xl) st.store(c, L.at(L.Ni, y, z), v);
+  if (xh) st.store(c, L.at(-1, y, z), v);
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    const bool on = b == 0 ? yl : yh;
+    if (!on) continue;
+    const int yg = b == 0 ? L.Nj : -1;
+    st.store(c, L.at(x, yg, z), v);
+    if (xl) st.store(c, L.at(L.Ni, yg, z), v);
+    if (xh) st.store(c, L.at(-1, yg, z), v);
+  }
+}
+
+}  // namespace fdtd

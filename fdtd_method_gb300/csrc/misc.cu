@@ -21,29 +21,40 @@ __device__ __forceinline__ Pair split_f64(double x) {
   return Pair{h, l};
 }
 
+// Logical flat index -> (x, y, z).
+__device__ __forceinline__ void unflatten(const PLayout& L, int64_t t, int& x, int& y, int& z) {
+  const int64_t plane = (int64_t)L.Ni * L.Nj;
+  z = (int)(t / plane);
+  const int64_t r = t - (int64_t)z * plane;
+  y = (int)(r / L.Ni);
+  x = (int)(r - (int64_t)y * L.Ni);
+}
+
 template <class S>
-__global__ void import_kernel(S st, int c, const double* __restrict__ src, int64_t off, int64_t n) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    if (S::kComp) st.store(c, off + t, split_f64(src[t]));
-    else st.store(c, off + t, Pair{__double2float_rn(src[t]), 0.f});
+__global__ void import_kernel(PLayout L, S st, int c, const double* __restrict__ src, int64_t off, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    int x, y, z;
+    unflatten(L, off + t, x, y, z);
+    const Pair p = S::kComp ? split_f64(src[t]) : Pair{__double2float_rn(src[t]), 0.f};
+    store_with_ghosts(st, L, c, x, y, z, p);
   }
 }
 
 template <class S>
-__global__ void export_kernel(S st, int c, double* __restrict__ dst, int64_t off, int64_t n) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x)
-    dst[t] = st.load_f64(c, off + t);
+__global__ void export_kernel(PLayout L, S st, int c, double* __restrict__ dst, int64_t off, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    int x, y, z;
+    unflatten(L, off + t, x, y, z);
+    dst[t] = st.load_f64(c, L.at(x, y, z));
+  }
 }
 
 __global__ void to_f32_kernel(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x)
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
     dst[t] = __double2float_rn(src[t]);
 }
 
-// One FP64 value of each field at flat index idx.
+// FP64 values of the six fields at logical cell `idx`.
 struct F64Loader {
   const double* f[6];
   __device__ __forceinline__ void get(int64_t idx, double v[6]) const {
@@ -54,16 +65,20 @@ struct F64Loader {
 template <class S>
 struct StoreLoader {
   S st;
+  PLayout L;
   __device__ __forceinline__ void get(int64_t idx, double v[6]) const {
+    int x, y, z;
+    unflatten(L, idx, x, y, z);
+    const int64_t p = L.at(x, y, z);
 #pragma unroll
-    for (int c = 0; c < 6; ++c) v[c] = st.load_f64(c, idx);
+    for (int c = 0; c < 6; ++c) v[c] = st.load_f64(c, p);
   }
 };
 
 // Pass 1: every block accumulates its grid-stride share of the ten sums in
 // FP64 and writes them to partials[block * 10 + q].
-template <class L>
-__global__ void __launch_bounds__(kDiagThreads) sums_pass1(L ld, int64_t cells, double* partials) {
+template <class Ld>
+__global__ void __launch_bounds__(kDiagThreads) sums_pass1(Ld ld, int64_t cells, double* partials) {
   double acc[kDiagValues];
 #pragma unroll
   for (int q = 0; q < kDiagValues; ++q) acc[q] = 0.0;
@@ -97,8 +112,7 @@ __global__ void __launch_bounds__(kDiagThreads) sums_pass1(L ld, int64_t cells, 
 }
 
 // Pass 2: one block folds the per-block partials into out[10].
-__global__ void __launch_bounds__(kDiagThreads) sums_pass2(const double* partials, int nblocks,
-                                                          double* out) {
+__global__ void __launch_bounds__(kDiagThreads) sums_pass2(const double* partials, int nblocks, double* out) {
   __shared__ double red[kDiagThreads / 32][kDiagValues];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int q = 0; q < kDiagValues; ++q) {
@@ -115,8 +129,6 @@ __global__ void __launch_bounds__(kDiagThreads) sums_pass2(const double* partial
   }
 }
 
-__global__ void set_i64_kernel(int64_t* dst, int64_t value) { *dst = value; }
-
 }  // namespace
 
 cudaError_t launch_import(const StateView& v, int c, const double* src, int64_t off, int64_t n,
@@ -126,9 +138,9 @@ cudaError_t launch_import(const StateView& v, int c, const double* src, int64_t 
   switch (v.form) {
     case Form::F64:
       return cudaMemcpyAsync(v.f64[c] + off, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
-    case Form::F32: import_kernel<<<nb, kConvThreads, 0, st>>>(v.s32, c, src, off, n); break;
-    case Form::F32C: import_kernel<<<nb, kConvThreads, 0, st>>>(v.s32c, c, src, off, n); break;
-    case Form::F16: import_kernel<<<nb, kConvThreads, 0, st>>>(v.s16, c, src, off, n); break;
+    case Form::F32: import_kernel<<<nb, kConvThreads, 0, st>>>(v.L, v.s32, c, src, off, n); break;
+    case Form::F32C: import_kernel<<<nb, kConvThreads, 0, st>>>(v.L, v.s32c, c, src, off, n); break;
+    case Form::F16: import_kernel<<<nb, kConvThreads, 0, st>>>(v.L, v.s16, c, src, off, n); break;
   }
   return cudaGetLastError();
 }
@@ -140,9 +152,9 @@ cudaError_t launch_export(const StateView& v, int c, double* dst, int64_t off, i
   switch (v.form) {
     case Form::F64:
       return cudaMemcpyAsync(dst, v.f64[c] + off, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
-    case Form::F32: export_kernel<<<nb, kConvThreads, 0, st>>>(v.s32, c, dst, off, n); break;
-    case Form::F32C: export_kernel<<<nb, kConvThreads, 0, st>>>(v.s32c, c, dst, off, n); break;
-    case Form::F16: export_kernel<<<nb, kConvThreads, 0, st>>>(v.s16, c, dst, off, n); break;
+    case Form::F32: export_kernel<<<nb, kConvThreads, 0, st>>>(v.L, v.s32, c, dst, off, n); break;
+    case Form::F32C: export_kernel<<<nb, kConvThreads, 0, st>>>(v.L, v.s32c, c, dst, off, n); break;
+    case Form::F16: export_kernel<<<nb, kConvThreads, 0, st>>>(v.L, v.s16, c, dst, off, n); break;
   }
   return cudaGetLastError();
 }
@@ -169,23 +181,18 @@ cudaError_t launch_field_sums(const StateView& v, double* partials, int nblocks,
       break;
     }
     case Form::F32:
-      sums_pass1<<<nblocks, kDiagThreads, 0, st>>>(StoreLoader<StoreF32>{v.s32}, cells, partials);
+      sums_pass1<<<nblocks, kDiagThreads, 0, st>>>(StoreLoader<StoreF32>{v.s32, v.L}, cells, partials);
       break;
     case Form::F32C:
-      sums_pass1<<<nblocks, kDiagThreads, 0, st>>>(StoreLoader<StoreF32C>{v.s32c}, cells, partials);
+      sums_pass1<<<nblocks, kDiagThreads, 0, st>>>(StoreLoader<StoreF32C>{v.s32c, v.L}, cells, partials);
       break;
     case Form::F16:
-      sums_pass1<<<nblocks, kDiagThreads, 0, st>>>(StoreLoader<StoreF16>{v.s16}, cells, partials);
+      sums_pass1<<<nblocks, kDiagThreads, 0, st>>>(StoreLoader<StoreF16>{v.s16, v.L}, cells, partials);
       break;
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   sums_pass2<<<1, kDiagThreads, 0, st>>>(partials, nblocks, out_dev);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_set_i64(int64_t* dst, int64_t value, cudaStream_t st) {
-  set_i64_kernel<<<1, 1, 0, st>>>(dst, value);
   return cudaGetLastError();
 }
 

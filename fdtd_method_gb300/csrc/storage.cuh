@@ -28,9 +28,10 @@ struct Coef {
 // Plain FP32 storage.
 struct StoreF32 {
   static constexpr bool kComp = false;
+  using HiT = float;
   float* v[6];
+  __device__ __forceinline__ Pair decode(int, float h, int8_t) const { return Pair{h, 0.f}; }
   __device__ __forceinline__ Pair load(int c, int64_t idx) const { return Pair{v[c][idx], 0.f}; }
-  __device__ __forceinline__ float load_hi(int c, int64_t idx) const { return v[c][idx]; }
   __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const { v[c][idx] = p.hi; }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const { return (double)v[c][idx]; }
   // The value a store followed by a load returns.
@@ -40,15 +41,14 @@ struct StoreF32 {
 // FP16 storage with a power-of-two scale per component: stored = field * 2^e.
 struct StoreF16 {
   static constexpr bool kComp = false;
+  using HiT = __half;
   __half* v[6];
   float scale[6];      // 2^e
   float inv_scale[6];  // 2^-e
-  __device__ __forceinline__ Pair load(int c, int64_t idx) const {
-    return Pair{__half2float(v[c][idx]) * inv_scale[c], 0.f};
+  __device__ __forceinline__ Pair decode(int c, __half h, int8_t) const {
+    return Pair{__half2float(h) * inv_scale[c], 0.f};
   }
-  __device__ __forceinline__ float load_hi(int c, int64_t idx) const {
-    return __half2float(v[c][idx]) * inv_scale[c];
-  }
+  __device__ __forceinline__ Pair load(int c, int64_t idx) const { return decode(c, v[c][idx], 0); }
   __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const {
     v[c][idx] = __float2half_rn(p.hi * scale[c]);
   }
@@ -63,27 +63,30 @@ struct StoreF16 {
 // Compensated storage: FP32 hi word + signed 8-bit lo word.  lo is an
 // integer multiple of 2^(E-30), E the binary exponent of hi, so with
 // |lo| <= ulp(hi)/2 = 2^(E-24) the integer stays within +-64: the pair holds
-// a 30-bit significand in 5 bytes.
+// a 30-bit significand in 5 bytes.  Both scales are built from hi's exponent
+// bits with integer arithmetic; for |hi| < 2^-96 the lo word reads as 0.
 constexpr int kLoShift = 30;
 
+// 2^(E-30), or 0 when that underflows.
 __device__ __forceinline__ float lo_decode_scale(float hi) {
-  const int eb = (__float_as_int(hi) >> 23) & 0xff;
-  return (eb > kLoShift && eb < 255) ? __int_as_float((eb - kLoShift) << 23) : 0.f;
+  const int s = (__float_as_int(hi) & 0x7f800000) - (kLoShift << 23);
+  return __int_as_float(max(s, 0));
 }
+// 2^(30-E), capped at 2^127.
 __device__ __forceinline__ float lo_encode_scale(float hi) {
-  const int eb = (__float_as_int(hi) >> 23) & 0xff;
-  return (eb > kLoShift && eb < 255) ? __int_as_float((kLoShift + 254 - eb) << 23) : 0.f;
+  const int s = ((127 + 127 + kLoShift) << 23) - (__float_as_int(hi) & 0x7f800000);
+  return __int_as_float(min(s, 254 << 23));
 }
 
 struct StoreF32C {
   static constexpr bool kComp = true;
+  using HiT = float;
   float* hi[6];
   int8_t* lo[6];
-  __device__ __forceinline__ Pair load(int c, int64_t idx) const {
-    const float h = hi[c][idx];
-    return Pair{h, (float)lo[c][idx] * lo_decode_scale(h)};
+  __device__ __forceinline__ Pair decode(int, float h, int8_t q) const {
+    return Pair{h, (float)q * lo_decode_scale(h)};
   }
-  __device__ __forceinline__ float load_hi(int c, int64_t idx) const { return hi[c][idx]; }
+  __device__ __forceinline__ Pair load(int c, int64_t idx) const { return decode(c, hi[c][idx], lo[c][idx]); }
   __device__ __forceinline__ static int encode_lo(Pair p) {
     const int q = __float2int_rn(p.lo * lo_encode_scale(p.hi));
     return max(-127, min(127, q));
@@ -96,41 +99,9 @@ struct StoreF32C {
     return Pair{p.hi, (float)encode_lo(p) * lo_decode_scale(p.hi)};
   }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const {
-    const float h = hi[c][idx];
-    return (double)h + (double)((float)lo[c][idx] * lo_decode_scale(h));
+    const Pair p = load(c, idx);
+    return (double)p.hi + (double)p.lo;
   }
 };
-
-// ---------------------------------------------------------------------------
-// Arithmetic on pairs.
-
-// a - b of two stored values.  For smooth fields neighbouring hi words are
-// within a factor of two of each other, so hi_a - hi_b is exact (Sterbenz) and
-// adding the lo difference recovers the difference of the full values.
-template <bool kComp>
-__device__ __forceinline__ float diff(Pair a, Pair b) {
-  if (kComp) return (a.hi - b.hi) + (a.lo - b.lo);
-  return a.hi - b.hi;
-}
-
-template <bool kComp>
-__device__ __forceinline__ float mulc(Coef c, float d) {
-  if (kComp) return fmaf(c.hi, d, c.lo * d);
-  return c.hi * d;
-}
-
-// v + t.  Compensated: TwoSum(hi, t) moves the rounding error into lo, then a
-// Fast2Sum renormalises so that |lo| <= ulp(hi)/2.
-template <bool kComp>
-__device__ __forceinline__ Pair accumulate(Pair v, float t) {
-  if (!kComp) return Pair{v.hi + t, 0.f};
-  const float s = v.hi + t;
-  const float bp = s - v.hi;
-  const float e = (v.hi - (s - bp)) + (t - bp);
-  const float l = v.lo + e;
-  const float h2 = s + l;
-  const float l2 = l - (h2 - s);
-  return Pair{h2, l2};
-}
 
 }  // namespace fdtd

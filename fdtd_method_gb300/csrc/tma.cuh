@@ -1,0 +1,70 @@
+// TMA tile copies and mbarrier waits (inline PTX, sm_90+ / sm_103a).
+#pragma once
+
+#include <cuda.h>
+
+#include <cstdint>
+
+namespace fdtd {
+
+// Tensor maps of one copy of the state: the six hi arrays and, for the
+// compensated form, the six lo arrays (passed to the fused kernel by value).
+struct TmaMaps {
+  CUtensorMap hi[6];
+  CUtensorMap lo[6];
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+// Makes barrier initialisation visible to the async (TMA) proxy.
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Waits for phase `parity` of the barrier with a bounded number of polls; on
+// giving up it records code 1 in *err and returns false (the caller carries
+// on with whatever the buffer holds, so that no thread is left at a barrier).
+constexpr uint32_t kMaxBarrierPolls = 1u << 24;
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
+  for (uint32_t n = 0; n < kMaxBarrierPolls; ++n)
+    if (mbar_try_wait(bar, parity)) return true;
+  atomicOr(err, 1);
+  return false;
+}
+
+// 3-D tiled TMA load of the box at element coordinates (x, y, z) of `map`
+// into shared memory, completing on `bar` (transaction bytes).
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+
+}  // namespace fdtd

@@ -1,0 +1,65 @@
+// Host-side construction of the TMA tensor maps of the fused step kernel.
+// cuTensorMapEncodeTiled is taken from the driver through the runtime's
+// entry-point query, so the library needs no link against libcuda.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "engine_internal.h"
+#include "tma.cuh"
+
+namespace fdtd {
+
+namespace {
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                 CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+  static EncodeTiled fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  }
+  return fn;
+}
+
+// One 3-D map over a padded array: dims {pitch, Nj + 2, Nk}, box
+// {box_w, tile_y + 2, 1}.
+bool encode(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const PLayout& L, int box_w,
+            int tile_y) {
+  EncodeTiled fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)L.pitch, (cuuint64_t)(L.Nj + 2), (cuuint64_t)L.Nk};
+  const cuuint64_t strides[2] = {(cuuint64_t)(L.pitch * es), (cuuint64_t)(L.pplane * es)};
+  const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)(tile_y + 2), 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return fn(m, dt, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], int8_t* const lo[6],
+                           int box_w, int tile_y) {
+  TmaMaps* m = static_cast<TmaMaps*>(maps);
+  std::memset(m, 0, sizeof(TmaMaps));
+  const CUtensorMapDataType dt = ht == HiType::F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+  const size_t es = ht == HiType::F32 ? 4 : 2;
+  for (int c = 0; c < 6; ++c) {
+    if (!encode(&m->hi[c], dt, es, hi[c], L, box_w, tile_y)) return cudaErrorInvalidValue;
+    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, lo[c], L, 64, tile_y))
+      return cudaErrorInvalidValue;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace fdtd

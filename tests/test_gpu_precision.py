@@ -104,9 +104,10 @@ def _run(p, prec, vals, srcs, steps, pipeline, tile_y=0, kchunk=0, dense_j=None)
 
 
 @pytest.mark.parametrize("prec", [Precision.FP32, Precision.FP32_COMP, Precision.FP16_SCALED])
-@pytest.mark.parametrize("shape,tile_y,kchunk", [((37, 19, 23), 16, 64), ((1, 1, 1), 16, 64),
-                                                 ((60, 28, 16), 16, 8), ((31, 15, 129), 8, 64),
-                                                 ((2, 70, 3), 8, 2), ((33, 9, 40), 16, 7)])
+@pytest.mark.parametrize("shape,tile_y,kchunk", [((37, 19, 23), 14, 64), ((1, 1, 1), 14, 64),
+                                                 ((64, 28, 16), 14, 8), ((31, 15, 129), 6, 64),
+                                                 ((2, 70, 3), 6, 2), ((33, 9, 40), 14, 7),
+                                                 ((96, 42, 5), 6, 3)])
 def test_fused_step_equals_split_sweeps(prec, shape, tile_y, kchunk):
     """The one-sweep-per-step kernel and the one-sweep-per-half-step kernels
     evaluate the same arithmetic: results are bit-identical, with sources."""
