@@ -27,6 +27,20 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
 }
 
+// Double-float helpers (value = h + l): products and sums carried with an
+// FP32 error term, renormalised with Fast2Sum.
+__device__ __forceinline__ Pair df_renorm(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return Pair{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ Pair df_mul(Pair a, Pair b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_renorm(p, e);
+}
+
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
@@ -42,6 +56,17 @@ struct ArithPlain {
   __device__ __forceinline__ static Pair add(Pair p, Pair q) { return Pair{__fadd_rn(p.hi, q.hi), 0.f}; }
   __device__ __forceinline__ static Pair twice(Pair t) { return Pair{2.f * t.hi, 0.f}; }
   __device__ __forceinline__ static Pair acc(Pair v, Pair t) { return Pair{__fadd_rn(v.hi, t.hi), 0.f}; }
+
+  // Current values: FP32.
+  using Cur = float;
+  __device__ __forceinline__ static Cur cur_zero() { return 0.f; }
+  __device__ __forceinline__ static Cur cur_table(const SourceSet& ss, int64_t off) { return ss.tables_f[off]; }
+  __device__ __forceinline__ static Cur cur_dense(float j) { return j; }
+  __device__ __forceinline__ static Cur cur_mul(Cur a, Cur b) { return __fmul_rn(a, b); }
+  __device__ __forceinline__ static Cur cur_add(Cur a, Cur b) { return __fadd_rn(a, b); }
+  __device__ __forceinline__ static bool cur_nonzero(Cur a) { return a != 0.f; }
+  // cJ * J
+  __device__ __forceinline__ static Pair cur_term(Coef cj, Cur j) { return Pair{__fmul_rn(cj.hi, j), 0.f}; }
 };
 
 struct ArithComp {
@@ -72,6 +97,22 @@ struct ArithComp {
   __device__ __forceinline__ static Pair curl(Coef c1, Pair a1, Pair b1, Coef c2, Pair a2, Pair b2) {
     return sub(term(c1, diff(a1, b1)), term(c2, diff(a2, b2)));
   }
+  // Current values: double-float (hi + lo FP32 tables), so the compensated
+  // form evaluates its sources without the FP64 pipe.
+  using Cur = Pair;
+  __device__ __forceinline__ static Cur cur_zero() { return Pair{0.f, 0.f}; }
+  __device__ __forceinline__ static Cur cur_table(const SourceSet& ss, int64_t off) {
+    return Pair{ss.tables_f[off], ss.tables_f[off + ss.lo_off]};
+  }
+  __device__ __forceinline__ static Cur cur_dense(float j) { return Pair{j, 0.f}; }
+  __device__ __forceinline__ static Cur cur_mul(Cur a, Cur b) { return df_mul(a, b); }
+  __device__ __forceinline__ static Cur cur_add(Cur a, Cur b) {
+    const Pair s = add(a, b);
+    return df_renorm(s.hi, s.lo);
+  }
+  __device__ __forceinline__ static bool cur_nonzero(Cur a) { return a.hi != 0.f || a.lo != 0.f; }
+  __device__ __forceinline__ static Pair cur_term(Coef cj, Cur j) { return df_mul(Pair{cj.hi, cj.lo}, j); }
+
   // v + t, renormalised: |l| <= ulp(h)/2 afterwards.
   __device__ __forceinline__ static Pair acc(Pair v, Pair t) {
     float s, e;

@@ -35,7 +35,9 @@ struct SourceSet {
   int count;
   const DevSource* src;    // device array [count]
   const double* tables;    // device buffer holding every profile and amplitude table
-  const float* tables_f;   // the same tables rounded to FP32
+  const float* tables_f;   // the same tables split into FP32 hi (at the same
+                           // offsets) and FP32 lo parts (at offset + lo_off)
+  int64_t lo_off;
 };
 
 // Offset of index v inside the periodic window [o, o+n) of an axis of length N,

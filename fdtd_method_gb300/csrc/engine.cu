@@ -83,7 +83,8 @@ struct fdtd_handle {
   std::vector<HostSource> sources;
   DevSource* d_src = nullptr;
   double* d_tables = nullptr;
-  float* d_tables_f = nullptr;
+  float* d_tables_f = nullptr;  // FP32 hi tables, then FP32 lo tables
+  int64_t tables_lo_off = 0;
   int64_t host_step = 0;  // completed update_fields steps
 
   // Step pipeline of the FP32-arithmetic forms (FP64 always uses the split
@@ -138,6 +139,7 @@ struct fdtd_handle {
     ss.src = d_src;
     ss.tables = d_tables;
     ss.tables_f = d_tables_f;
+    ss.lo_off = tables_lo_off;
     return ss;
   }
 };
@@ -211,14 +213,16 @@ int upload_sources(fdtd_handle* h) {
   if (ds.empty()) return FDTD_OK;
   FDTD_CUDA(cudaMalloc(&h->d_src, sizeof(DevSource) * ds.size()), "source descriptors");
   FDTD_CUDA(cudaMalloc(&h->d_tables, sizeof(double) * tables.size()), "source tables");
-  FDTD_CUDA(cudaMalloc(&h->d_tables_f, sizeof(float) * tables.size()), "source tables (fp32)");
+  FDTD_CUDA(cudaMalloc(&h->d_tables_f, 2 * sizeof(float) * tables.size()), "source tables (fp32)");
   FDTD_CUDA(cudaMemcpy(h->d_src, ds.data(), sizeof(DevSource) * ds.size(), cudaMemcpyHostToDevice),
             "upload source descriptors");
   FDTD_CUDA(cudaMemcpy(h->d_tables, tables.data(), sizeof(double) * tables.size(),
                        cudaMemcpyHostToDevice),
             "upload source tables");
-  FDTD_CUDA(launch_to_f32(h->d_tables, h->d_tables_f, (int64_t)tables.size(), h->stream),
-            "convert source tables");
+  h->tables_lo_off = (int64_t)tables.size();
+  FDTD_CUDA(launch_split_f32(h->d_tables, h->d_tables_f, h->d_tables_f + h->tables_lo_off,
+                             (int64_t)tables.size(), h->stream),
+            "split source tables");
   FDTD_CUDA(cudaStreamSynchronize(h->stream), "source upload");
   return FDTD_OK;
 }

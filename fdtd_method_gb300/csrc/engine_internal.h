@@ -82,6 +82,8 @@ cudaError_t launch_export(const StateView& v, int c, double* dst, int64_t off, i
                           cudaStream_t st);
 // FP64 -> FP32 conversion of n values.
 cudaError_t launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
+// FP64 -> FP32 hi + FP32 lo (hi + lo carries the FP64 value to ~2^-48).
+cudaError_t launch_split_f32(const double* src, float* hi, float* lo, int64_t n, cudaStream_t st);
 
 // Field sums (fdtd_diag order, 10 values) in two passes through `partials`
 // (room for `max_blocks` * 10 doubles); the result lands in out_dev[10].

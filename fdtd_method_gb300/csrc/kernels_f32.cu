@@ -24,34 +24,20 @@ __device__ __forceinline__ Pair curl_term(Coef c1, Pair a1, Pair b1, Coef c2, Pa
   return A::curl(c1, a1, b1, c2, a2, b2);
 }
 
-// Current values are FP64 for the compensated form (its error budget is
-// below FP32 rounding) and FP32 for the plain forms.
-template <class A> struct CurT { using T = float; };
-template <> struct CurT<ArithComp> { using T = double; };
-
+// Current values: FP32 for the plain forms, double-float for the compensated
+// one (A::Cur).  The source product is ((amp gx) gy) gz in that order.
 template <class A>
-__device__ __forceinline__ Pair current_term(const CoefSet& cs, typename CurT<A>::T j);
-template <>
-__device__ __forceinline__ Pair current_term<ArithPlain>(const CoefSet& cs, float j) {
-  return Pair{__fmul_rn(cs.cj.hi, j), 0.f};
-}
-template <>
-__device__ __forceinline__ Pair current_term<ArithComp>(const CoefSet& cs, double j) {
-  const double s = __dmul_rn(cs.cj64, j);
-  const float h = __double2float_rn(s);
-  return Pair{h, __double2float_rn(s - (double)h)};
+__device__ __forceinline__ void add_current(typename A::Cur jv[3], int mask, typename A::Cur v) {
+  if (mask & 1) jv[0] = A::cur_add(jv[0], v);
+  if (mask & 2) jv[1] = A::cur_add(jv[1], v);
+  if (mask & 4) jv[2] = A::cur_add(jv[2], v);
 }
 
-template <class T> __device__ __forceinline__ const T* table_of(const SourceSet& ss);
-template <> __device__ __forceinline__ const double* table_of<double>(const SourceSet& ss) { return ss.tables; }
-template <> __device__ __forceinline__ const float* table_of<float>(const SourceSet& ss) { return ss.tables_f; }
-
-// Sum over every source at logical cell (i, j, k) for time step s:
-// ((amp gx) gy) gz, sources in registration order.
-template <class T>
+// Sum over every source at logical cell (i, j, k) for time step s, sources
+// in registration order.
+template <class A>
 __device__ __forceinline__ bool source_sum(const SourceSet& ss, int64_t s, int i, int j, int k,
-                                           const PLayout& L, T jv[3]) {
-  const T* tb = table_of<T>(ss);
+                                           const PLayout& L, typename A::Cur jv[3]) {
   bool any = false;
   for (int q = 0; q < ss.count; ++q) {
     const DevSource& d = ss.src[q];
@@ -62,11 +48,11 @@ __device__ __forceinline__ bool source_sum(const SourceSet& ss, int64_t s, int i
     if (dj < 0) continue;
     const int di = box_offset(i, d.i0, d.ni, L.Ni);
     if (di < 0) continue;
-    const T v = mul_rn(mul_rn(mul_rn(tb[d.amp_off + s], tb[d.gx_off + di]), tb[d.gy_off + dj]),
-                       tb[d.gz_off + dk]);
-    if (d.comp_mask & 1) jv[0] = add_rn(jv[0], v);
-    if (d.comp_mask & 2) jv[1] = add_rn(jv[1], v);
-    if (d.comp_mask & 4) jv[2] = add_rn(jv[2], v);
+    const typename A::Cur v =
+        A::cur_mul(A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + s), A::cur_table(ss, d.gx_off + di)),
+                              A::cur_table(ss, d.gy_off + dj)),
+                   A::cur_table(ss, d.gz_off + dk));
+    add_current<A>(jv, d.comp_mask, v);
     any = true;
   }
   return any;
@@ -115,7 +101,7 @@ __global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __r
                                                const float* __restrict__ Jy,
                                                const float* __restrict__ Jz, CoefSet cs, int kchunk,
                                                SourceSet ss, int64_t step) {
-  using T = typename CurT<A>::T;
+  using T = typename A::Cur;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k0 = blockIdx.z * kchunk;
@@ -137,20 +123,20 @@ __global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __r
     Pair tx = curl_term<A>(cy, bz, st.load(5, col_jp + base), cz, by, by_kp);
     Pair ty = curl_term<A>(cz, bx, bx_kp, cx, bz, st.load(5, col_ip + base));
     Pair tz = curl_term<A>(cx, by, st.load(4, col_ip + base), cy, bx, st.load(3, col_jp + base));
-    T jv[3] = {0, 0, 0};
+    T jv[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
     bool has_j = false;
     if (kDenseJ) {
       const int64_t d = dcol + (int64_t)k * dplane;
-      jv[0] = Jx[d];
-      jv[1] = Jy[d];
-      jv[2] = Jz[d];
+      jv[0] = A::cur_dense(Jx[d]);
+      jv[1] = A::cur_dense(Jy[d]);
+      jv[2] = A::cur_dense(Jz[d]);
       has_j = true;
     }
-    if (kSources) has_j |= source_sum<T>(ss, step, i, j, k, L, jv);
+    if (kSources) has_j |= source_sum<A>(ss, step, i, j, k, L, jv);
     if (has_j) {
-      tx = A::add(tx, current_term<A>(cs, jv[0]));
-      ty = A::add(ty, current_term<A>(cs, jv[1]));
-      tz = A::add(tz, current_term<A>(cs, jv[2]));
+      tx = A::add(tx, A::cur_term(cs.cj, jv[0]));
+      ty = A::add(ty, A::cur_term(cs.cj, jv[1]));
+      tz = A::add(tz, A::cur_term(cs.cj, jv[2]));
     }
     store_with_ghosts(st, L, 0, i, j, k, A::acc(st.load(0, col + base), tx));
     store_with_ghosts(st, L, 1, i, j, k, A::acc(st.load(1, col + base), ty));
@@ -213,7 +199,7 @@ __global__ void __launch_bounds__(32 * (RY + 2))
               const float* __restrict__ Jz, SourceSet ss, int64_t step, int* err) {
   using SM = FusedSmem<S, RY>;
   using HiT = typename S::HiT;
-  using T = typename CurT<A>::T;
+  using T = typename A::Cur;
   constexpr int ROWS = SM::ROWS, W = SM::W, LW = SM::LW, NV = SM::NV, OFF = BoxTraits<S>::kOff;
   constexpr int NS = kFusedStages;
   constexpr int EC = 33;  // columns of the E' exchange (32 interior + the x halo)
@@ -265,20 +251,21 @@ __global__ void __launch_bounds__(32 * (RY + 2))
   if (producer)
     for (int t = k0; t <= k1 && t < k0 + NS; ++t) issue(t);
 
-  // Sources: per-column factor amp * gx * gy, once per launch.
+  // Sources: per-column factor (amp gx) gy, once per launch.
   T sxy[kFastSources];
   unsigned smask = 0;
+#pragma unroll
+  for (int q = 0; q < kFastSources; ++q) sxy[q] = A::cur_zero();
   if (kSrc == 1 && active) {
 #pragma unroll
     for (int q = 0; q < kFastSources; ++q) {
-      sxy[q] = T(0);
       if (q < ss.count) {
         const DevSource& d = ss.src[q];
         const int di = box_offset(xl, d.i0, d.ni, L.Ni);
         const int dj = box_offset(yl, d.j0, d.nj, L.Nj);
         if (step < d.n_amp && di >= 0 && dj >= 0) {
-          const T* tb = table_of<T>(ss);
-          sxy[q] = mul_rn(mul_rn(tb[d.amp_off + step], tb[d.gx_off + di]), tb[d.gy_off + dj]);
+          sxy[q] = A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + step), A::cur_table(ss, d.gx_off + di)),
+                              A::cur_table(ss, d.gy_off + dj));
           smask |= 1u << q;
         }
       }
@@ -315,13 +302,13 @@ __global__ void __launch_bounds__(32 * (RY + 2))
       Pair qx = curl_term<A>(cs.ce[1], bz, val(5, r - 1, cx), cs.ce[2], by, pby);
       Pair qy = curl_term<A>(cs.ce[2], bx, pbx, cs.ce[0], bz, val(5, r, cx - 1));
       Pair qz = curl_term<A>(cs.ce[0], by, val(4, r, cx - 1), cs.ce[1], bx, val(3, r - 1, cx));
-      T jv[3] = {0, 0, 0};
+      T jv[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
       bool has_j = false;
       if (kDenseJ) {
         const int64_t d = xl + (int64_t)yl * L.Ni + (int64_t)kk * L.Ni * L.Nj;
-        jv[0] = Jx[d];
-        jv[1] = Jy[d];
-        jv[2] = Jz[d];
+        jv[0] = A::cur_dense(Jx[d]);
+        jv[1] = A::cur_dense(Jy[d]);
+        jv[2] = A::cur_dense(Jz[d]);
         has_j = true;
       }
       if (kSrc == 1) {
@@ -331,21 +318,18 @@ __global__ void __launch_bounds__(32 * (RY + 2))
             const DevSource& d = ss.src[q];
             const int dk = box_offset(kk, d.k0, d.nk, L.Nk);
             if (dk >= 0) {
-              const T v = mul_rn(sxy[q], table_of<T>(ss)[d.gz_off + dk]);
-              if (d.comp_mask & 1) jv[0] = add_rn(jv[0], v);
-              if (d.comp_mask & 2) jv[1] = add_rn(jv[1], v);
-              if (d.comp_mask & 4) jv[2] = add_rn(jv[2], v);
+              add_current<A>(jv, d.comp_mask, A::cur_mul(sxy[q], A::cur_table(ss, d.gz_off + dk)));
               has_j = true;
             }
           }
         }
       } else if (kSrc == 2) {
-        has_j |= source_sum<T>(ss, step, xl, yl, kk, L, jv);
+        has_j |= source_sum<A>(ss, step, xl, yl, kk, L, jv);
       }
       if (has_j) {
-        qx = A::add(qx, current_term<A>(cs, jv[0]));
-        qy = A::add(qy, current_term<A>(cs, jv[1]));
-        qz = A::add(qz, current_term<A>(cs, jv[2]));
+        qx = A::add(qx, A::cur_term(cs.cj, jv[0]));
+        qy = A::add(qy, A::cur_term(cs.cj, jv[1]));
+        qz = A::add(qz, A::cur_term(cs.cj, jv[2]));
       }
       // E' as its storage form will hold it (what the split sweeps reload).
       nex = st.quantize(0, A::acc(ex, qx));

@@ -54,6 +54,15 @@ __global__ void to_f32_kernel(const double* __restrict__ src, float* __restrict_
     dst[t] = __double2float_rn(src[t]);
 }
 
+__global__ void split_f32_kernel(const double* __restrict__ src, float* __restrict__ hi,
+                                 float* __restrict__ lo, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const Pair p = split_f64(src[t]);
+    hi[t] = p.hi;
+    lo[t] = p.lo;
+  }
+}
+
 // FP64 values of the six fields at logical cell `idx`.
 struct F64Loader {
   const double* f[6];
@@ -162,6 +171,12 @@ cudaError_t launch_export(const StateView& v, int c, double* dst, int64_t off, i
 cudaError_t launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   to_f32_kernel<<<conv_blocks(n), kConvThreads, 0, st>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_split_f32(const double* src, float* hi, float* lo, int64_t n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  split_f32_kernel<<<conv_blocks(n), kConvThreads, 0, st>>>(src, hi, lo, n);
   return cudaGetLastError();
 }
 

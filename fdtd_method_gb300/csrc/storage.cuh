@@ -78,25 +78,37 @@ __device__ __forceinline__ float lo_encode_scale(float hi) {
   return __int_as_float(min(s, 254 << 23));
 }
 
+// Integer <-> float for |q| < 2^22 without the conversion unit: a float of
+// the form 1.5 * 2^23 + q holds q in its low mantissa bits.
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+__device__ __forceinline__ float small_int_to_float(int q) {
+  return __fsub_rn(__int_as_float(kMagicBits + q), kMagic);
+}
+// Round-to-nearest-even of x, |x| < 2^22.
+__device__ __forceinline__ int float_to_small_int(float x) {
+  return __float_as_int(__fadd_rn(x, kMagic)) - kMagicBits;
+}
+
 struct StoreF32C {
   static constexpr bool kComp = true;
   using HiT = float;
   float* hi[6];
   int8_t* lo[6];
   __device__ __forceinline__ Pair decode(int, float h, int8_t q) const {
-    return Pair{h, (float)q * lo_decode_scale(h)};
+    return Pair{h, __fmul_rn(small_int_to_float(q), lo_decode_scale(h))};
   }
   __device__ __forceinline__ Pair load(int c, int64_t idx) const { return decode(c, hi[c][idx], lo[c][idx]); }
   __device__ __forceinline__ static int encode_lo(Pair p) {
-    const int q = __float2int_rn(p.lo * lo_encode_scale(p.hi));
-    return max(-127, min(127, q));
+    const float x = fminf(fmaxf(__fmul_rn(p.lo, lo_encode_scale(p.hi)), -127.f), 127.f);
+    return float_to_small_int(x);
   }
   __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const {
     hi[c][idx] = p.hi;
     lo[c][idx] = (int8_t)encode_lo(p);
   }
   __device__ __forceinline__ Pair quantize(int, Pair p) const {
-    return Pair{p.hi, (float)encode_lo(p) * lo_decode_scale(p.hi)};
+    return Pair{p.hi, __fmul_rn(small_int_to_float(encode_lo(p)), lo_decode_scale(p.hi))};
   }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const {
     const Pair p = load(c, idx);
