@@ -53,6 +53,11 @@ Coef split_coef(double c) {
 
 }  // namespace
 
+namespace fdtd {
+// Lets other translation units of the library report through fdtd_last_error().
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace fdtd
+
 struct fdtd_handle {
   fdtd_params p{};
   double dt = 0;

@@ -193,6 +193,20 @@ enum fdtd_pipeline { FDTD_PIPELINE_AUTO = 0, FDTD_PIPELINE_SPLIT = 1, FDTD_PIPEL
 int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk);
 int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t launches[FDTD_KERNEL_KINDS]);
 
+/* No counterpart in the reference.  The ten field sums of fdtd_field_sums,
+ * for callers that cannot allocate device memory (an application whose pool
+ * allocator owns every device allocation, a monitor that must not call
+ * cudaMalloc beside a running simulation): no handle, no allocation.  Inputs:
+ * six FP64 device arrays Ex..Bz of `cells` values (dense drop-in layout);
+ * output: 10 doubles at out_device (fdtd_diag order), written on `stream`
+ * (a cudaStream_t, 0 = default stream).  Scratch is a fixed device array of
+ * 65536 block partials built into the library (5 MiB per device that loads
+ * it, held until exit), which caps `cells` at 268,435,456; larger grids give
+ * FDTD_ERR_INVALID_ARGUMENT.  The first call on a device resolves that array's
+ * device address (make it before any stream capture).  Calls share the array:
+ * calls that overlap on the GPU race. */
+int fdtd_field_sums_noalloc(const double* const fields[6], int64_t cells, double* out_device, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
