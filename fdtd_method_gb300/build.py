@@ -30,7 +30,9 @@ def sources():
 
 def _newest_input():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files += [os.path.join(HERE, "cpp", f) for f in os.listdir(os.path.join(HERE, "cpp"))]
     files.append(os.path.join(HERE, "..", "include", "fdtd_gb300.h"))
+    files.append(os.path.join(HERE, "..", "include", "fdtd_gb300.hpp"))
     files.append(__file__)
     return max(os.path.getmtime(f) for f in files if os.path.exists(f))
 
@@ -65,7 +67,25 @@ def build(force=False, verbose=False, extra_flags=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
+    build_programs()
     return LIB
+
+
+CPP = os.path.join(HERE, "cpp")
+PROGRAMS = ("fdtd_sample", "convergence_tests")
+
+
+def build_programs():
+    """C++ programs over the drop-in header include/fdtd_gb300.hpp: the GPU
+    twin of the reference's sample driver and its convergence tests."""
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    inc = os.path.join(HERE, "..", "include")
+    for name in PROGRAMS:
+        cmd = [cxx, "-O2", "-std=c++17", "-I" + inc, os.path.join(CPP, name + ".cpp"), "-L" + HERE,
+               "-lfdtd_gb300", "-Wl,-rpath,$ORIGIN", "-o", os.path.join(HERE, name)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("build of %s failed:\n%s" % (name, r.stderr))
 
 
 if __name__ == "__main__":

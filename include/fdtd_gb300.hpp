@@ -1,0 +1,174 @@
+// fdtd_gb300.hpp — header-only C++ drop-in for the reference's Kokkos solver
+// class FDTD_kokkos::FDTD (Amazingkivas/FDTD_Method,
+// include/FDTD_kokkos/FDTD_kokkos.h:7-36), over the C ABI in fdtd_gb300.h.
+//
+// Same names, argument meaning and error behaviour:
+//   FDTD(Parameters, FP dt)     throws std::invalid_argument("ERROR: invalid parameters")
+//                               (src/FDTD_kokkos/FDTD_kokkos.cpp:7-12)
+//   Field& get_field(Component) throws std::logic_error("ERROR: Invalid field component")
+//                               (src/FDTD_kokkos/FDTD_kokkos.cpp:75-89)
+//   virtual void update_fields() one step B/2, E, B/2 (src/FDTD_kokkos/FDTD_kokkos.cpp:91-104)
+//   void zeroed_currents()      (src/FDTD_kokkos/FDTD_kokkos.cpp:69-73)
+// Fields live on the GPU: a Field handle aliases the solver's device array as
+// the reference's View does; host access goes through create_mirror_view +
+// deep_copy, as the reference sample does (perf-tests/kokkos_sample/kokkos_sample.cpp:135-139).
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "fdtd_gb300.h"
+
+namespace FDTD_gb300 {
+
+using FP = double;  // include/FP.h:3
+
+namespace FDTD_const {  // include/Constants.h:4-12
+const double C = 3e10;
+const double R = 1e-12;
+const double EPS0 = 1.0;
+const double MU0 = EPS0;
+const double N = 4.0;
+const double PI = 3.14159265358;
+}  // namespace FDTD_const
+
+enum class Component { EX, EY, EZ, BX, BY, BZ, JX, JY, JZ };  // include/Enums.h:5
+enum class Axis { X, Y, Z };                                   // include/Enums.h:6
+
+enum class Precision { FP64 = FDTD_PRECISION_FP64, FP32 = FDTD_PRECISION_FP32,
+                       FP32_COMP = FDTD_PRECISION_FP32_COMP, FP16_SCALED = FDTD_PRECISION_FP16_SCALED };
+
+struct SelectedFields {  // include/Structures.h:8-11
+  Component selected_E;
+  Component selected_B;
+};
+
+struct CurrentParameters {  // include/Structures.h:13-21
+  int period;
+  int m;
+  FP dt;
+  int iterations;
+  FP period_x = static_cast<FP>(m) * FDTD_const::C;
+  FP period_y = static_cast<FP>(m) * FDTD_const::C;
+  FP period_z = static_cast<FP>(m) * FDTD_const::C;
+};
+
+struct Parameters {  // include/Structures.h:23-38
+  int Ni;
+  int Nj;
+  int Nk;
+  FP ax;
+  FP bx;
+  FP ay;
+  FP by;
+  FP az;
+  FP bz;
+  FP dx;
+  FP dy;
+  FP dz;
+};
+
+// Throws the reference's exception type for a C-ABI status.
+inline void check(int rc) {
+  if (rc == FDTD_OK) return;
+  const std::string msg = fdtd_last_error();
+  if (rc == FDTD_ERR_INVALID_ARGUMENT) throw std::invalid_argument(msg);
+  if (rc == FDTD_ERR_LOGIC) throw std::logic_error(msg);
+  throw std::runtime_error(msg);
+}
+
+class FDTD;
+
+// A component of a solver's state (the reference's Kokkos::View member).
+class Field {
+ public:
+  Field() = default;
+  // Device address of the Ni*Nj*Nk doubles (FP64 form only).
+  double* data() const {
+    double* p = nullptr;
+    check(fdtd_get_field(h_, static_cast<int>(comp_), &p));
+    return p;
+  }
+  std::size_t size() const { return n_; }
+  std::size_t extent(int) const { return n_; }
+  Component component() const { return comp_; }
+  fdtd_handle* handle() const { return h_; }
+
+ private:
+  friend class FDTD;
+  Field(fdtd_handle* h, Component c, std::size_t n) : h_(h), comp_(c), n_(n) {}
+  fdtd_handle* h_ = nullptr;
+  Component comp_ = Component::EX;
+  std::size_t n_ = 0;
+};
+
+// Host copy of a Field (Kokkos::create_mirror_view).
+class HostMirror {
+ public:
+  explicit HostMirror(std::size_t n = 0) : v_(n) {}
+  double& operator()(long i) { return v_[static_cast<std::size_t>(i)]; }
+  double operator()(long i) const { return v_[static_cast<std::size_t>(i)]; }
+  double& operator[](long i) { return v_[static_cast<std::size_t>(i)]; }
+  double* data() { return v_.data(); }
+  const double* data() const { return v_.data(); }
+  std::size_t size() const { return v_.size(); }
+
+ private:
+  std::vector<double> v_;
+};
+
+inline HostMirror create_mirror_view(const Field& f) { return HostMirror(f.size()); }
+// Kokkos::deep_copy(host, device) / deep_copy(device, host)
+inline void deep_copy(HostMirror& dst, const Field& src) {
+  check(fdtd_copy_field_to_host(src.handle(), static_cast<int>(src.component()), dst.data(), dst.size()));
+}
+inline void deep_copy(const Field& dst, const HostMirror& src) {
+  check(fdtd_copy_field_from_host(dst.handle(), static_cast<int>(dst.component()), src.data(), src.size()));
+}
+
+class FDTD {
+ public:
+  FDTD(Parameters parameters, FP dt, Precision precision = Precision::FP64) : parameters_(parameters), dt_(dt) {
+    fdtd_params p{parameters.Ni, parameters.Nj, parameters.Nk, parameters.ax, parameters.bx, parameters.ay,
+                  parameters.by, parameters.az, parameters.bz, parameters.dx, parameters.dy, parameters.dz};
+    check(fdtd_create(&p, dt, static_cast<int>(precision), &h_));
+    const std::size_t n = static_cast<std::size_t>(parameters.Ni) * parameters.Nj * parameters.Nk;
+    for (int c = 0; c < 9; ++c) fields_[c] = Field(h_, static_cast<Component>(c), n);
+  }
+  FDTD(const FDTD&) = delete;
+  FDTD& operator=(const FDTD&) = delete;
+  virtual ~FDTD() { fdtd_destroy(h_); }
+
+  Field& get_field(Component c) {
+    const int i = static_cast<int>(c);
+    if (i < 0 || i > 8) throw std::logic_error("ERROR: Invalid field component");
+    return fields_[i];
+  }
+
+  virtual void update_fields() { check(fdtd_update_fields(h_)); }
+  void zeroed_currents() { check(fdtd_zeroed_currents(h_)); }
+
+  // Extensions.
+  void step(int64_t n) { check(fdtd_step(h_, n)); }
+  void fence() { check(fdtd_synchronize(h_)); }
+  int add_source(const fdtd_source& s) {
+    int idx = -1;
+    check(fdtd_add_source(h_, &s, &idx));
+    return idx;
+  }
+  void field_sums(double out[FDTD_DIAG_COUNT]) { check(fdtd_field_sums(h_, out)); }
+  const Parameters& parameters() const { return parameters_; }
+  FP dt() const { return dt_; }
+  fdtd_handle* handle() const { return h_; }
+
+ private:
+  Parameters parameters_;
+  FP dt_;
+  fdtd_handle* h_ = nullptr;
+  Field fields_[9];
+};
+
+}  // namespace FDTD_gb300
