@@ -57,6 +57,7 @@ def parse_args():
     ap.add_argument("--pipeline", default="auto", choices=["auto", "fused", "split"])
     ap.add_argument("--tile-y", type=int, default=0)
     ap.add_argument("--kchunk", type=int, default=0)
+    ap.add_argument("--cells-per-thread", type=int, default=0)
     ap.add_argument("--run-length", type=int, default=1000, help="steps of the accuracy run")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -271,7 +272,7 @@ def run_ours(args):
 
     # --- chosen form, device-timed ---------------------------------------
     sim = FDTD(p, COURANT_DT, PREC[args.precision])
-    sim.set_pipeline(args.pipeline, args.tile_y, args.kchunk)
+    sim.set_pipeline(args.pipeline, args.tile_y, args.kchunk, args.cells_per_thread)
     sim.set_stream(stream.cuda_stream)
     sim.add_source(src)
     sim.step(W)
@@ -324,7 +325,7 @@ def run_ours(args):
     if not args.no_e2e:
         host = [torch.zeros(cells, dtype=torch.float64).pin_memory().numpy() for _ in range(6)]
         s = FDTD(p, COURANT_DT, PREC[args.precision])
-        s.set_pipeline(args.pipeline, args.tile_y, args.kchunk)
+        s.set_pipeline(args.pipeline, args.tile_y, args.kchunk, args.cells_per_thread)
         s.add_source(src)
         for c in range(6):  # warm-up job (not timed)
             s.copy_from_host(c, host[c])
@@ -354,7 +355,7 @@ def run_ours(args):
     if not args.no_accuracy and rank == 0:
         a = FDTD(p, COURANT_DT, Precision.FP64)
         b = FDTD(p, COURANT_DT, PREC[args.precision])
-        b.set_pipeline(args.pipeline, args.tile_y, args.kchunk)
+        b.set_pipeline(args.pipeline, args.tile_y, args.kchunk, args.cells_per_thread)
         for x in (a, b):
             x.add_source(src)
             x.step(args.run_length)

@@ -86,7 +86,7 @@ SIGNATURES = {
     "fdtd_set_fp16_exponents": [_H, ctypes.POINTER(ctypes.c_int)],
     "fdtd_set_kernel_timing": [_H, ctypes.c_int],
     "fdtd_kernel_times": [_H, _D, ctypes.POINTER(ctypes.c_int64)],
-    "fdtd_set_pipeline": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+    "fdtd_set_pipeline": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "fdtd_field_sums_noalloc": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p],
 }
 _RESTYPES = {"fdtd_last_error": ctypes.c_char_p}

@@ -1,0 +1,160 @@
+// Two-cell (float2) forms of the arithmetic policies of arith.cuh and of the
+// storage codecs of storage.cuh, for the fused kernel that gives each thread
+// two neighbouring x cells.  Every packed operation is the IEEE operation of
+// the one-cell code applied to both lanes (__fadd2_rn, __fmul2_rn,
+// __ffma2_rn, sm_100+), so the two-cell kernel reproduces the one-cell
+// sweeps bit for bit.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "arith.cuh"
+
+namespace fdtd {
+
+struct P2 {
+  float2 hi, lo;
+};
+
+struct Coef2 {
+  float2 hi, lo;
+};
+__device__ __forceinline__ Coef2 bcast(Coef c) {
+  return Coef2{make_float2(c.hi, c.hi), make_float2(c.lo, c.lo)};
+}
+
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+// a - b, correctly rounded (one rounding of a + (-b)).
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+
+__device__ __forceinline__ P2 make_p2(Pair a, Pair b) {
+  return P2{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)};
+}
+__device__ __forceinline__ Pair lane0(P2 p) { return Pair{p.hi.x, p.lo.x}; }
+__device__ __forceinline__ Pair lane1(P2 p) { return Pair{p.hi.y, p.lo.y}; }
+
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = add2(a, b);
+  const float2 bp = sub2(s, a);
+  const float2 ap = sub2(s, bp);
+  e = add2(sub2(a, ap), sub2(b, bp));
+}
+
+template <class A> struct Arith2;
+
+template <>
+struct Arith2<ArithPlain> {
+  // fma(c1, a1 - b1, -(c2 (a2 - b2))), as ArithPlain::curl
+  __device__ __forceinline__ static P2 curl(Coef2 c1, P2 a1, P2 b1, Coef2 c2, P2 a2, P2 b2) {
+    const float2 m = mul2(c2.hi, sub2(a2.hi, b2.hi));
+    return P2{fma2(c1.hi, sub2(a1.hi, b1.hi), neg2(m)), make_float2(0.f, 0.f)};
+  }
+  __device__ __forceinline__ static P2 add(P2 p, P2 q) { return P2{add2(p.hi, q.hi), make_float2(0.f, 0.f)}; }
+  __device__ __forceinline__ static P2 twice(P2 t) { return P2{mul2(t.hi, make_float2(2.f, 2.f)), t.lo}; }
+  __device__ __forceinline__ static P2 acc(P2 v, P2 t) { return P2{add2(v.hi, t.hi), make_float2(0.f, 0.f)}; }
+};
+
+template <>
+struct Arith2<ArithComp> {
+  __device__ __forceinline__ static P2 diff(P2 a, P2 b) { return P2{sub2(a.hi, b.hi), sub2(a.lo, b.lo)}; }
+  __device__ __forceinline__ static P2 term(Coef2 c, P2 d) {
+    const float2 p = mul2(c.hi, d.hi);
+    float2 e = fma2(c.hi, d.hi, neg2(p));
+    e = fma2(c.hi, d.lo, e);
+    e = fma2(c.lo, d.hi, e);
+    return P2{p, e};
+  }
+  __device__ __forceinline__ static P2 sub(P2 p, P2 q) {
+    float2 s, e;
+    two_sum2(p.hi, neg2(q.hi), s, e);
+    return P2{s, add2(e, sub2(p.lo, q.lo))};
+  }
+  __device__ __forceinline__ static P2 add(P2 p, P2 q) {
+    float2 s, e;
+    two_sum2(p.hi, q.hi, s, e);
+    return P2{s, add2(e, add2(p.lo, q.lo))};
+  }
+  __device__ __forceinline__ static P2 twice(P2 t) {
+    return P2{mul2(t.hi, make_float2(2.f, 2.f)), mul2(t.lo, make_float2(2.f, 2.f))};
+  }
+  __device__ __forceinline__ static P2 curl(Coef2 c1, P2 a1, P2 b1, Coef2 c2, P2 a2, P2 b2) {
+    return sub(term(c1, diff(a1, b1)), term(c2, diff(a2, b2)));
+  }
+  __device__ __forceinline__ static P2 acc(P2 v, P2 t) {
+    float2 s, e;
+    two_sum2(v.hi, t.hi, s, e);
+    const float2 l = add2(add2(v.lo, e), t.lo);
+    const float2 h2 = add2(s, l);
+    return P2{h2, sub2(l, sub2(h2, s))};
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Two-cell codecs.  RawLo is the packed lo word of two cells (0 if none).
+
+template <class S> struct Codec2;
+
+template <>
+struct Codec2<StoreF32> {
+  using HiT = float;
+  using Raw = float2;
+  __device__ __forceinline__ static P2 decode(const StoreF32&, int, float2 h, uint32_t) {
+    return P2{h, make_float2(0.f, 0.f)};
+  }
+  __device__ __forceinline__ static P2 quantize(const StoreF32&, int, P2 p) { return P2{p.hi, make_float2(0.f, 0.f)}; }
+  // Stores both cells (8-byte aligned pair).
+  __device__ __forceinline__ static void store(const StoreF32& s, int c, int64_t idx, P2 p) {
+    *reinterpret_cast<float2*>(s.v[c] + idx) = p.hi;
+  }
+};
+
+template <>
+struct Codec2<StoreF16> {
+  using HiT = __half;
+  using Raw = __half2;
+  __device__ __forceinline__ static P2 decode(const StoreF16& s, int c, __half2 h, uint32_t) {
+    const float2 f = __half22float2(h);
+    return P2{mul2(f, make_float2(s.inv_scale[c], s.inv_scale[c])), make_float2(0.f, 0.f)};
+  }
+  __device__ __forceinline__ static __half2 encode(const StoreF16& s, int c, P2 p) {
+    return __float22half2_rn(mul2(p.hi, make_float2(s.scale[c], s.scale[c])));
+  }
+  __device__ __forceinline__ static P2 quantize(const StoreF16& s, int c, P2 p) {
+    return decode(s, c, encode(s, c, p), 0);
+  }
+  __device__ __forceinline__ static void store(const StoreF16& s, int c, int64_t idx, P2 p) {
+    *reinterpret_cast<__half2*>(s.v[c] + idx) = encode(s, c, p);
+  }
+};
+
+template <>
+struct Codec2<StoreF32C> {
+  using HiT = float;
+  using Raw = float2;
+  // lo words of the two cells: low byte = cell 0, next byte = cell 1.
+  __device__ __forceinline__ static P2 decode(const StoreF32C&, int, float2 h, uint32_t q2) {
+    const int q0 = (int)(int8_t)(q2 & 0xffu), q1 = (int)(int8_t)((q2 >> 8) & 0xffu);
+    const float2 f = sub2(make_float2(__int_as_float(kMagicBits + q0), __int_as_float(kMagicBits + q1)),
+                          make_float2(kMagic, kMagic));
+    return P2{h, mul2(f, make_float2(lo_decode_scale(h.x), lo_decode_scale(h.y)))};
+  }
+  __device__ __forceinline__ static uint32_t encode(P2 p) {
+    const float2 x = mul2(p.lo, make_float2(lo_encode_scale(p.hi.x), lo_encode_scale(p.hi.y)));
+    const float2 m = add2(make_float2(fminf(fmaxf(x.x, -127.f), 127.f), fminf(fmaxf(x.y, -127.f), 127.f)),
+                          make_float2(kMagic, kMagic));
+    const int q0 = __float_as_int(m.x) - kMagicBits, q1 = __float_as_int(m.y) - kMagicBits;
+    return (uint32_t)(q0 & 0xff) | ((uint32_t)(q1 & 0xff) << 8);
+  }
+  __device__ __forceinline__ static P2 quantize(const StoreF32C& s, int c, P2 p) {
+    return decode(s, c, p.hi, encode(p));
+  }
+  __device__ __forceinline__ static void store(const StoreF32C& s, int c, int64_t idx, P2 p) {
+    *reinterpret_cast<float2*>(s.hi[c] + idx) = p.hi;
+    *reinterpret_cast<uint16_t*>(s.lo[c] + idx) = (uint16_t)encode(p);
+  }
+};
+
+}  // namespace fdtd

@@ -337,15 +337,19 @@ int ensure_alt(fdtd_handle* h) {
     }
     h->maps_tile_y = 0;
   }
-  if (h->maps_tile_y != h->fused_cfg.tile_y) {
+  const int key = h->fused_cfg.tile_y * 10 + h->fused_cfg.cells_per_thread;
+  if (h->maps_tile_y != key) {
     const HiType ht = h->form == Form::F16 ? HiType::F16 : HiType::F32;
-    const int bw = h->form == Form::F16 ? fused_box_width<StoreF16>() : fused_box_width<StoreF32>();
+    const bool two = h->fused_cfg.cells_per_thread == 2;
+    const int bw = h->form == Form::F16 ? (two ? fused_box_width<StoreF16>() : fused1_box_width<StoreF16>())
+                                        : (two ? fused_box_width<StoreF32>() : fused1_box_width<StoreF32>());
+    const int lbw = two ? fused_lo_box_width() : fused1_lo_box_width();
     int8_t* const* lo_cur = h->form == Form::F32C ? h->lo : nullptr;
     int8_t* const* lo_alt = h->form == Form::F32C ? h->alt_lo : nullptr;
-    if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, h->fused_cfg.tile_y) != cudaSuccess ||
-        build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, h->fused_cfg.tile_y) != cudaSuccess)
+    if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, lbw, h->fused_cfg.tile_y) != cudaSuccess ||
+        build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, h->fused_cfg.tile_y) != cudaSuccess)
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
-    h->maps_tile_y = h->fused_cfg.tile_y;
+    h->maps_tile_y = key;
   }
   return FDTD_OK;
 }
@@ -363,12 +367,19 @@ int run_fused(fdtd_handle* h, int64_t step, int apps) {
   const FusedConfig& cf = h->fused_cfg;
   const void* m = &h->maps_cur;
   cudaError_t e = cudaSuccess;
-  switch (h->form) {
-    case Form::F32: e = launch_fused_f32(h->L, v.s32, w.s32, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;
-    case Form::F32C: e = launch_fused_f32(h->L, v.s32c, w.s32c, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;
-    case Form::F16: e = launch_fused_f32(h->L, v.s16, w.s16, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;
-    default: e = cudaErrorInvalidValue; break;
+#define FDTD_FUSED_LAUNCH(FN)                                                                                  \
+  switch (h->form) {                                                                                         \
+    case Form::F32: e = FN(h->L, v.s32, w.s32, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;    \
+    case Form::F32C: e = FN(h->L, v.s32c, w.s32c, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break; \
+    case Form::F16: e = FN(h->L, v.s16, w.s16, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;    \
+    default: e = cudaErrorInvalidValue; break;                                                               \
   }
+  if (cf.cells_per_thread == 2) {
+    FDTD_FUSED_LAUNCH(launch_fused_f32)
+  } else {
+    FDTD_FUSED_LAUNCH(launch_fused1_f32)
+  }
+#undef FDTD_FUSED_LAUNCH
   lt.done();
   if (e != cudaSuccess) return cuda_fail(e, "fused step launch");
   for (int c = 0; c < 6; ++c) {
@@ -702,16 +713,19 @@ int fdtd_set_step(fdtd_handle* h, int64_t step) {
   return FDTD_OK;
 }
 
-int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk) {
+int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int cells_per_thread) {
   if (int rc = check_handle(h)) return rc;
   if (pipeline < FDTD_PIPELINE_AUTO || pipeline > FDTD_PIPELINE_FUSED)
     return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid pipeline");
   if (tile_y != 0 && tile_y != 6 && tile_y != 14)
     return fail(FDTD_ERR_INVALID_ARGUMENT, "tile_y must be 0 (default), 6 or 14");
   if (kchunk < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "kchunk must be >= 0");
+  if (cells_per_thread < 0 || cells_per_thread > 2)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "cells_per_thread must be 0 (default), 1 or 2");
   h->pipeline = pipeline;
   h->fused_cfg.tile_y = tile_y ? tile_y : 14;
   h->fused_cfg.kchunk = kchunk ? kchunk : 64;
+  h->fused_cfg.cells_per_thread = cells_per_thread ? cells_per_thread : 1;
   return FDTD_OK;
 }
 

@@ -28,6 +28,7 @@ struct CoefSet {
 struct FusedConfig {
   int tile_y = 14;
   int kchunk = 64;
+  int cells_per_thread = 1;  // 1: 32-wide tiles (kernels_fused1.cu); 2: 64-wide, packed float2
 };
 
 // kernels_fp64.cu
@@ -52,13 +53,22 @@ cudaError_t launch_fused_f32(const PLayout& L, const S& st, const S& out, const 
                              const FusedConfig& cfg, int* err, cudaStream_t stream);
 template <class S>
 int fused_box_width();
-size_t tma_maps_bytes();
+int fused_lo_box_width();
+// kernels_fused1.cu: the same sweep with one cell per thread (32-wide tiles).
+template <class S>
+cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const void* maps,
+                              const float* const J[3], bool dense_j, const CoefSet& cs,
+                              const SourceSet& ss, int64_t step, int applications,
+                              const FusedConfig& cfg, int* err, cudaStream_t stream);
+template <class S>
+int fused1_box_width();
+int fused1_lo_box_width();
 
 // tma_maps.cu: tensor maps of the six hi arrays (and six lo arrays of the
 // compensated form) for a fused tile of `tile_y` interior rows.
 enum class HiType { F32, F16 };
 cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6],
-                           int8_t* const lo[6], int box_w, int tile_y);
+                           int8_t* const lo[6], int box_w, int lo_box_w, int tile_y);
 
 // misc.cu — conversions, diagnostics, small helpers.
 enum class Form { F64 = 0, F32 = 1, F32C = 2, F16 = 3 };

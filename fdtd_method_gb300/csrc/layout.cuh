@@ -1,12 +1,14 @@
 // Padded field layout of the FP32-arithmetic forms.
 //
 // Each component is stored as a 3-D array with a ghost row below and above
-// the grid in y and a 16-element margin left and right of it in x, so that
+// the grid in y and a 32-element margin left and right of it in x, so that
 //   * every x/y neighbour of a grid cell exists in memory (the ghost cells
 //     hold periodic copies: ghost x = -1 is cell Ni-1, ghost x = Ni is cell 0,
 //     likewise in y and at the four corners), and
-//   * each row starts on a 16-byte boundary (pitch is a multiple of 16
-//     elements), which TMA tile copies require.
+//   * cell x = 0 of every row starts a 32-byte memory sector for every
+//     element size (pitch is a multiple of 32 elements), so the stores of a
+//     warp's row segment cover whole sectors (no read-modify-write in L2)
+//     and the tile copies start on the 16-byte boundaries TMA requires.
 // The writer of a boundary cell also writes its ghost copies, so the ghosts
 // are current whenever the cell is.  z is not padded: planes wrap by index.
 //
@@ -17,7 +19,7 @@
 
 namespace fdtd {
 
-constexpr int kPadX = 16;
+constexpr int kPadX = 32;
 
 struct PLayout {
   int Ni, Nj, Nk;
@@ -34,17 +36,16 @@ struct PLayout {
     L.Ni = Ni;
     L.Nj = Nj;
     L.Nk = Nk;
-    L.pitch = ((int64_t)Ni + 2 * kPadX + 15) / 16 * 16;
+    L.pitch = ((int64_t)Ni + 2 * kPadX + 31) / 32 * 32;
     L.pplane = L.pitch * (Nj + 2);
     return L;
   }
 };
 
-// Stores v at (x, y, z) and at every ghost position that mirrors it.
+// Stores v at every ghost position that mirrors cell (x, y, z).
 template <class S, class V>
-__device__ __forceinline__ void store_with_ghosts(const S& st, const PLayout& L, int c, int x, int y,
-                                                  int z, V v) {
-  st.store(c, L.at(x, y, z), v);
+__device__ __forceinline__ void store_ghost_copies(const S& st, const PLayout& L, int c, int x, int y,
+                                                   int z, V v) {
   const bool xl = (x == 0), xh = (x == L.Ni - 1), yl = (y == 0), yh = (y == L.Nj - 1);
   if (!(xl || xh || yl || yh)) return;
   // ghost columns of this row, then the ghost rows (with their corners)
@@ -59,6 +60,14 @@ __device__ __forceinline__ void store_with_ghosts(const S& st, const PLayout& L,
     if (xl) st.store(c, L.at(L.Ni, yg, z), v);
     if (xh) st.store(c, L.at(-1, yg, z), v);
   }
+}
+
+// Stores v at (x, y, z) and at every ghost position that mirrors it.
+template <class S, class V>
+__device__ __forceinline__ void store_with_ghosts(const S& st, const PLayout& L, int c, int x, int y,
+                                                  int z, V v) {
+  st.store(c, L.at(x, y, z), v);
+  store_ghost_copies(st, L, c, x, y, z, v);
 }
 
 }  // namespace fdtd

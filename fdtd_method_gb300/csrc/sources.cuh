@@ -1,0 +1,88 @@
+// Current-source evaluation of the FP32-arithmetic kernels.  Current values
+// are A::Cur: FP32 for the plain forms, double-float for the compensated one.
+// A source contributes ((amp[s] gx[di]) gy[dj]) gz[dk], sources added in
+// registration order (the oracle's and the reference sample's order).
+#pragma once
+
+#include "arith.cuh"
+#include "layout.cuh"
+
+namespace fdtd {
+
+// Sources whose per-column factor a kernel keeps in registers.
+constexpr int kFastSources = 2;
+
+template <class A>
+__device__ __forceinline__ void add_current(typename A::Cur jv[3], int mask, typename A::Cur v) {
+  if (mask & 1) jv[0] = A::cur_add(jv[0], v);
+  if (mask & 2) jv[1] = A::cur_add(jv[1], v);
+  if (mask & 4) jv[2] = A::cur_add(jv[2], v);
+}
+
+// Every source at logical cell (i, j, k), time step s.
+template <class A>
+__device__ __forceinline__ bool source_sum(const SourceSet& ss, int64_t s, int i, int j, int k,
+                                           const PLayout& L, typename A::Cur jv[3]) {
+  bool any = false;
+  for (int q = 0; q < ss.count; ++q) {
+    const DevSource& d = ss.src[q];
+    if (s >= d.n_amp) continue;
+    const int dk = box_offset(k, d.k0, d.nk, L.Nk);
+    if (dk < 0) continue;
+    const int dj = box_offset(j, d.j0, d.nj, L.Nj);
+    if (dj < 0) continue;
+    const int di = box_offset(i, d.i0, d.ni, L.Ni);
+    if (di < 0) continue;
+    const typename A::Cur v =
+        A::cur_mul(A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + s), A::cur_table(ss, d.gx_off + di)),
+                              A::cur_table(ss, d.gy_off + dj)),
+                   A::cur_table(ss, d.gz_off + dk));
+    add_current<A>(jv, d.comp_mask, v);
+    any = true;
+  }
+  return any;
+}
+
+// Per-column state of the first kFastSources sources: (amp gx) gy, computed
+// once per launch.
+template <class A>
+struct ColumnSources {
+  typename A::Cur xy[kFastSources];
+  unsigned mask = 0;
+
+  __device__ __forceinline__ void init(const SourceSet& ss, int x, int y, int64_t step, const PLayout& L) {
+#pragma unroll
+    for (int q = 0; q < kFastSources; ++q) {
+      xy[q] = A::cur_zero();
+      if (q < ss.count) {
+        const DevSource& d = ss.src[q];
+        const int di = box_offset(x, d.i0, d.ni, L.Ni);
+        const int dj = box_offset(y, d.j0, d.nj, L.Nj);
+        if (step < d.n_amp && di >= 0 && dj >= 0) {
+          xy[q] = A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + step), A::cur_table(ss, d.gx_off + di)),
+                             A::cur_table(ss, d.gy_off + dj));
+          mask |= 1u << q;
+        }
+      }
+    }
+  }
+  // Adds the contributions at plane k; true if any source covers the cell.
+  __device__ __forceinline__ bool eval(const SourceSet& ss, int k, const PLayout& L,
+                                       typename A::Cur jv[3]) const {
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < kFastSources; ++q) {
+      if (mask & (1u << q)) {
+        const DevSource& d = ss.src[q];
+        const int dk = box_offset(k, d.k0, d.nk, L.Nk);
+        if (dk >= 0) {
+          add_current<A>(jv, d.comp_mask, A::cur_mul(xy[q], A::cur_table(ss, d.gz_off + dk)));
+          any = true;
+        }
+      }
+    }
+    return any;
+  }
+};
+
+}  // namespace fdtd

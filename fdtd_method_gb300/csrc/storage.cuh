@@ -46,17 +46,17 @@ struct StoreF16 {
   float scale[6];      // 2^e
   float inv_scale[6];  // 2^-e
   __device__ __forceinline__ Pair decode(int c, __half h, int8_t) const {
-    return Pair{__half2float(h) * inv_scale[c], 0.f};
+    return Pair{__fmul_rn(__half2float(h), inv_scale[c]), 0.f};
   }
   __device__ __forceinline__ Pair load(int c, int64_t idx) const { return decode(c, v[c][idx], 0); }
   __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const {
-    v[c][idx] = __float2half_rn(p.hi * scale[c]);
+    v[c][idx] = __float2half_rn(__fmul_rn(p.hi, scale[c]));
   }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const {
     return (double)__half2float(v[c][idx]) * (double)inv_scale[c];
   }
   __device__ __forceinline__ Pair quantize(int c, Pair p) const {
-    return Pair{__half2float(__float2half_rn(p.hi * scale[c])) * inv_scale[c], 0.f};
+    return Pair{__fmul_rn(__half2float(__float2half_rn(__fmul_rn(p.hi, scale[c]))), inv_scale[c]), 0.f};
   }
 };
 

@@ -49,14 +49,14 @@ bool encode(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const
 }  // namespace
 
 cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], int8_t* const lo[6],
-                           int box_w, int tile_y) {
+                           int box_w, int lo_box_w, int tile_y) {
   TmaMaps* m = static_cast<TmaMaps*>(maps);
   std::memset(m, 0, sizeof(TmaMaps));
   const CUtensorMapDataType dt = ht == HiType::F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
   const size_t es = ht == HiType::F32 ? 4 : 2;
   for (int c = 0; c < 6; ++c) {
     if (!encode(&m->hi[c], dt, es, hi[c], L, box_w, tile_y)) return cudaErrorInvalidValue;
-    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, lo[c], L, 64, tile_y))
+    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, lo[c], L, lo_box_w, tile_y))
       return cudaErrorInvalidValue;
   }
   return cudaSuccess;

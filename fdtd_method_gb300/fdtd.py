@@ -301,10 +301,13 @@ class FDTD:
     KERNEL_KINDS = ("e_update", "b_half", "b_double", "fused_step")
     PIPELINES = {"auto": 0, "split": 1, "fused": 2}
 
-    def set_pipeline(self, pipeline="auto", tile_y=0, kchunk=0):
+    def set_pipeline(self, pipeline="auto", tile_y=0, kchunk=0, cells_per_thread=0):
         """Step pipeline of the FP32-arithmetic forms: 'fused' (one sweep per
-        step, the default) or 'split' (one sweep per half step); same results."""
-        _lib.check(self._lib.fdtd_set_pipeline(self._handle(), self.PIPELINES[pipeline], int(tile_y), int(kchunk)))
+        step, the default) or 'split' (one sweep per half step); same results.
+        tile_y (14 or 6), kchunk and cells_per_thread (1 or 2) shape the fused
+        launch; 0 keeps the default."""
+        _lib.check(self._lib.fdtd_set_pipeline(self._handle(), self.PIPELINES[pipeline], int(tile_y), int(kchunk),
+                                               int(cells_per_thread)))
 
     def set_kernel_timing(self, enabled):
         """Bracket every step-pipeline kernel launch with CUDA events."""

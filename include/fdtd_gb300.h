@@ -185,12 +185,13 @@ int fdtd_set_kernel_timing(fdtd_handle* h, int enabled);
 
 /* Step pipeline of the FP32-arithmetic forms (new; tuning and testing).
  * AUTO and FUSED: one sweep per step (E step + double B half step); SPLIT:
- * one sweep per half step.  Both give bit-identical results.  tile_y (rows
- * of a fused tile: 0 = default 16, or 8) and kchunk (planes per fused tile:
- * 0 = default 64) shape the fused launch.  The FP64 form always uses the
- * split sweeps. */
+ * one sweep per half step.  All give bit-identical results.  The fused
+ * launch is shaped by tile_y (interior rows of a tile: 14 or 6; 0 = 14),
+ * kchunk (planes per tile; 0 = 64) and cells_per_thread (1: 32-wide tiles,
+ * 2: 64-wide tiles with packed two-cell arithmetic; 0 = 1).  The FP64 form
+ * always uses the split sweeps. */
 enum fdtd_pipeline { FDTD_PIPELINE_AUTO = 0, FDTD_PIPELINE_SPLIT = 1, FDTD_PIPELINE_FUSED = 2 };
-int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk);
+int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int cells_per_thread);
 int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t launches[FDTD_KERNEL_KINDS]);
 
 /* No counterpart in the reference.  The ten field sums of fdtd_field_sums,

@@ -87,11 +87,11 @@ def test_compensated_beats_plain_fp32(fp64_pulse):
     assert errs[Precision.FP32_COMP] < errs[Precision.FP32]
 
 
-def _run(p, prec, vals, srcs, steps, pipeline, tile_y=0, kchunk=0, dense_j=None):
+def _run(p, prec, vals, srcs, steps, pipeline, tile_y=0, kchunk=0, dense_j=None, cpt=0):
     s = FDTD(p, COURANT_DT, prec)
     if prec == Precision.FP16_SCALED:
         s.set_fp16_exponents([4] * 6)
-    s.set_pipeline(pipeline, tile_y, kchunk)
+    s.set_pipeline(pipeline, tile_y, kchunk, cpt)
     for c, v in enumerate(vals):
         s.get_field(c).assign(v)
     if dense_j is not None:
@@ -103,12 +103,13 @@ def _run(p, prec, vals, srcs, steps, pipeline, tile_y=0, kchunk=0, dense_j=None)
     return fields(s)
 
 
+@pytest.mark.parametrize("cpt", [1, 2])
 @pytest.mark.parametrize("prec", [Precision.FP32, Precision.FP32_COMP, Precision.FP16_SCALED])
 @pytest.mark.parametrize("shape,tile_y,kchunk", [((37, 19, 23), 14, 64), ((1, 1, 1), 14, 64),
                                                  ((64, 28, 16), 14, 8), ((31, 15, 129), 6, 64),
                                                  ((2, 70, 3), 6, 2), ((33, 9, 40), 14, 7),
                                                  ((96, 42, 5), 6, 3)])
-def test_fused_step_equals_split_sweeps(prec, shape, tile_y, kchunk):
+def test_fused_step_equals_split_sweeps(prec, shape, tile_y, kchunk, cpt):
     """The one-sweep-per-step kernel and the one-sweep-per-half-step kernels
     evaluate the same arithmetic: results are bit-identical, with sources."""
     p = normalised_parameters(*shape)
@@ -118,13 +119,14 @@ def test_fused_step_equals_split_sweeps(prec, shape, tile_y, kchunk):
     srcs = [sources.gaussian_pulse(p, c, 2.0, 1.0, 20.0, 3.0, 4.0, 20, comp="z"),
             sources.gaussian_pulse(p, (0, 0, 0), 1.5, 0.8, 25.0, 2.0, 3.0, 20, phase=0.5, comp="x")]
     a = _run(p, prec, vals, srcs, 5, "split")
-    b = _run(p, prec, vals, srcs, 5, "fused", tile_y, kchunk)
+    b = _run(p, prec, vals, srcs, 5, "fused", tile_y, kchunk, cpt=cpt)
     for q in range(6):
         np.testing.assert_array_equal(a[q], b[q], err_msg="component %d" % q)
 
 
+@pytest.mark.parametrize("cpt", [1, 2])
 @pytest.mark.parametrize("prec", [Precision.FP32, Precision.FP32_COMP])
-def test_fused_many_sources_and_dense_current(prec):
+def test_fused_many_sources_and_dense_current(prec, cpt):
     """More sources than the fused kernel keeps in registers (generic path),
     plus a dense current written by the host."""
     p = normalised_parameters(40, 24, 20)
@@ -133,7 +135,7 @@ def test_fused_many_sources_and_dense_current(prec):
     dj = [rng.standard_normal(p.cells) * 0.01 for _ in range(3)]
     srcs = sources.random_pulses(p, 6, seed=4, n_steps=30, sigma=2.0)
     a = _run(p, prec, vals, srcs, 6, "split", dense_j=dj)
-    b = _run(p, prec, vals, srcs, 6, "fused", dense_j=dj)
+    b = _run(p, prec, vals, srcs, 6, "fused", dense_j=dj, cpt=cpt)
     for q in range(6):
         np.testing.assert_array_equal(a[q], b[q])
 
