@@ -253,7 +253,7 @@ def timed_steps(sim, stream, steps, world):
 
 
 PREC = {"fp32_comp": 2, "fp32": 1, "fp16_scaled": 3}
-BYTES_PER_VALUE = {"fp32_comp": 5, "fp32": 4, "fp16_scaled": 2, "fp64": 8}
+BYTES_PER_VALUE = {"fp32_comp": 6, "fp32": 4, "fp16_scaled": 2, "fp64": 8}
 
 
 def run_ours(args):

@@ -134,26 +134,20 @@ template <>
 struct Codec2<StoreF32C> {
   using HiT = float;
   using Raw = float2;
-  // lo words of the two cells: low byte = cell 0, next byte = cell 1.
+  // BF16 lo words of the two cells: low half = cell 0, high half = cell 1.
   __device__ __forceinline__ static P2 decode(const StoreF32C&, int, float2 h, uint32_t q2) {
-    const int q0 = (int)(int8_t)(q2 & 0xffu), q1 = (int)(int8_t)((q2 >> 8) & 0xffu);
-    const float2 f = sub2(make_float2(__int_as_float(kMagicBits + q0), __int_as_float(kMagicBits + q1)),
-                          make_float2(kMagic, kMagic));
-    return P2{h, mul2(f, make_float2(lo_decode_scale(h.x), lo_decode_scale(h.y)))};
+    return P2{h, make_float2(__uint_as_float(q2 << 16), __uint_as_float(q2 & 0xffff0000u))};
   }
   __device__ __forceinline__ static uint32_t encode(P2 p) {
-    const float2 x = mul2(p.lo, make_float2(lo_encode_scale(p.hi.x), lo_encode_scale(p.hi.y)));
-    const float2 m = add2(make_float2(fminf(fmaxf(x.x, -127.f), 127.f), fminf(fmaxf(x.y, -127.f), 127.f)),
-                          make_float2(kMagic, kMagic));
-    const int q0 = __float_as_int(m.x) - kMagicBits, q1 = __float_as_int(m.y) - kMagicBits;
-    return (uint32_t)(q0 & 0xff) | ((uint32_t)(q1 & 0xff) << 8);
+    const __nv_bfloat162 b = __floats2bfloat162_rn(p.lo.x, p.lo.y);
+    return *reinterpret_cast<const uint32_t*>(&b);
   }
   __device__ __forceinline__ static P2 quantize(const StoreF32C& s, int c, P2 p) {
     return decode(s, c, p.hi, encode(p));
   }
   __device__ __forceinline__ static void store(const StoreF32C& s, int c, int64_t idx, P2 p) {
     *reinterpret_cast<float2*>(s.hi[c] + idx) = p.hi;
-    *reinterpret_cast<uint16_t*>(s.lo[c] + idx) = (uint16_t)encode(p);
+    *reinterpret_cast<uint32_t*>(s.lo[c] + idx) = encode(p);
   }
 };
 

@@ -75,11 +75,11 @@ struct fdtd_handle {
   // field[0..5] hold the E/B words of the form, lo[0..5] the compensation
   // words (FP32_COMP), jf[0..2] FP32 current arrays (allocated on first use).
   void* field[9] = {nullptr};
-  int8_t* lo[6] = {nullptr};
+  LoT* lo[6] = {nullptr};
   // Second copy of E/B (and lo) that the fused sweep writes into; swapped
   // with field/lo after every fused step.
   void* alt_field[6] = {nullptr};
-  int8_t* alt_lo[6] = {nullptr};
+  LoT* alt_lo[6] = {nullptr};
   float* jf[3] = {nullptr};
   bool dense_j = false;  // the E update reads the dense J arrays
   int fp16_exp[6] = {0, 0, 0, 0, 0, 0};
@@ -120,7 +120,7 @@ struct fdtd_handle {
   std::vector<TimedLaunch> timed;
   std::vector<cudaEvent_t> event_pool;
 
-  StateView make_view(void* const* f, int8_t* const* l) const {
+  StateView make_view(void* const* f, LoT* const* l) const {
     StateView v{};
     v.form = form;
     v.g = g;
@@ -331,8 +331,8 @@ int ensure_alt(fdtd_handle* h) {
       FDTD_CUDA(dev_alloc(h, &h->alt_field[c], eb * h->L.elems()), "second field copy");
       FDTD_CUDA(cudaMemsetAsync(h->alt_field[c], 0, eb * h->L.elems(), h->stream), "zero second copy");
       if (h->form == Form::F32C) {
-        FDTD_CUDA(dev_alloc(h, (void**)&h->alt_lo[c], h->L.elems()), "second compensation copy");
-        FDTD_CUDA(cudaMemsetAsync(h->alt_lo[c], 0, h->L.elems(), h->stream), "zero second copy");
+        FDTD_CUDA(dev_alloc(h, (void**)&h->alt_lo[c], sizeof(LoT) * h->L.elems()), "second compensation copy");
+        FDTD_CUDA(cudaMemsetAsync(h->alt_lo[c], 0, sizeof(LoT) * h->L.elems(), h->stream), "zero second copy");
       }
     }
     h->maps_tile_y = 0;
@@ -344,8 +344,8 @@ int ensure_alt(fdtd_handle* h) {
     const int bw = h->form == Form::F16 ? (two ? fused_box_width<StoreF16>() : fused1_box_width<StoreF16>())
                                         : (two ? fused_box_width<StoreF32>() : fused1_box_width<StoreF32>());
     const int lbw = two ? fused_lo_box_width() : fused1_lo_box_width();
-    int8_t* const* lo_cur = h->form == Form::F32C ? h->lo : nullptr;
-    int8_t* const* lo_alt = h->form == Form::F32C ? h->alt_lo : nullptr;
+    LoT* const* lo_cur = h->form == Form::F32C ? h->lo : nullptr;
+    LoT* const* lo_alt = h->form == Form::F32C ? h->alt_lo : nullptr;
     if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, lbw, h->fused_cfg.tile_y) != cudaSuccess ||
         build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, h->fused_cfg.tile_y) != cudaSuccess)
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
@@ -468,8 +468,8 @@ int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle
   }
   if (h->form == Form::F32C) {
     for (int c = 0; c < 6; ++c) {
-      e = dev_alloc(h, (void**)&h->lo[c], per_field);
-      if (e == cudaSuccess) e = cudaMemsetAsync(h->lo[c], 0, per_field, h->stream);
+      e = dev_alloc(h, (void**)&h->lo[c], sizeof(LoT) * per_field);
+      if (e == cudaSuccess) e = cudaMemsetAsync(h->lo[c], 0, sizeof(LoT) * per_field, h->stream);
       if (e != cudaSuccess) {
         int rc = cuda_fail(e, "compensation allocation");
         release(h);

@@ -68,7 +68,7 @@ int fused1_lo_box_width();
 // compensated form) for a fused tile of `tile_y` interior rows.
 enum class HiType { F32, F16 };
 cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6],
-                           int8_t* const lo[6], int box_w, int lo_box_w, int tile_y);
+                           LoT* const lo[6], int box_w, int lo_box_w, int tile_y);
 
 // misc.cu — conversions, diagnostics, small helpers.
 enum class Form { F64 = 0, F32 = 1, F32C = 2, F16 = 3 };

@@ -36,12 +36,12 @@ namespace {
 
 constexpr int kStages = 3;
 constexpr int kTileX = 64;
-constexpr int kLoOff = 16;
+constexpr int kLoOff = 8;  // BF16 lo box starts 8 columns left of the tile
 constexpr int kEC = 68;  // columns of the E' exchange rows (64 + halo, padded)
 
 template <class S> struct BoxOf;
 template <> struct BoxOf<StoreF32> { static constexpr int kW = 72, kOff = 4, kLoW = 0; };
-template <> struct BoxOf<StoreF32C> { static constexpr int kW = 72, kOff = 4, kLoW = 96; };
+template <> struct BoxOf<StoreF32C> { static constexpr int kW = 72, kOff = 4, kLoW = 80; };
 template <> struct BoxOf<StoreF16> { static constexpr int kW = 80, kOff = 8, kLoW = 0; };
 
 template <class S, int RY>
@@ -52,7 +52,7 @@ struct SmemPlan {
   static constexpr int LW = BoxOf<S>::kLoW;
   static constexpr int NV = S::kComp ? 2 : 1;
   static constexpr int kHiBytes = 6 * ROWS * W * (int)sizeof(HiT);
-  static constexpr int kLoBytes = 6 * ROWS * LW;
+  static constexpr int kLoBytes = 6 * ROWS * LW * (int)sizeof(LoT);
   static constexpr int kStageBytes = (kHiBytes + kLoBytes + 127) / 128 * 128;
   static constexpr int kEBytes = 2 * 3 * NV * ROWS * kEC * 4;
   static constexpr int kTotal = kStages * kStageBytes + kEBytes + kStages * 8;
@@ -142,7 +142,8 @@ __global__ void __launch_bounds__(32 * (RY + 2))
       tma_load_3d(base + c * ROWS * W * sizeof(HiT), &maps.hi[c], x0 + kPadX - OFF, y0, kk, &bar[slot]);
     if (S::kComp)
       for (int c = 0; c < 6; ++c)
-        tma_load_3d(base + SP::kHiBytes + c * ROWS * LW, &maps.lo[c], x0 + kPadX - kLoOff, y0, kk, &bar[slot]);
+        tma_load_3d(base + SP::kHiBytes + c * ROWS * LW * sizeof(LoT), &maps.lo[c], x0 + kPadX - kLoOff, y0, kk,
+                    &bar[slot]);
   };
 
   if (producer) {
@@ -198,15 +199,15 @@ __global__ void __launch_bounds__(32 * (RY + 2))
     const int cur = t & 1;
     mbar_wait_bounded(&bar[slot], ((t - k0) / kStages) & 1, err);
     const HiT* H = reinterpret_cast<const HiT*>(smem + slot * SP::kStageBytes);
-    const int8_t* Lo = reinterpret_cast<const int8_t*>(smem + slot * SP::kStageBytes + SP::kHiBytes);
+    const LoT* Lo = reinterpret_cast<const LoT*>(smem + slot * SP::kStageBytes + SP::kHiBytes);
     auto ld2 = [&](int c, int row, int col) -> P2 {  // cells col, col+1 (col even)
       const Raw h = *reinterpret_cast<const Raw*>(H + (c * ROWS + row) * W + col + OFF);
-      const uint32_t q = S::kComp ? *reinterpret_cast<const uint16_t*>(Lo + (c * ROWS + row) * LW + col + kLoOff) : 0u;
+      const uint32_t q = S::kComp ? *reinterpret_cast<const uint32_t*>(Lo + (c * ROWS + row) * LW + col + kLoOff) : 0u;
       return C2::decode(st, c, h, q);
     };
     auto ld1 = [&](int c, int row, int col) -> Pair {
       const HiT h = H[(c * ROWS + row) * W + col + OFF];
-      const int8_t q = S::kComp ? Lo[(c * ROWS + row) * LW + col + kLoOff] : int8_t(0);
+      const LoT q = S::kComp ? Lo[(c * ROWS + row) * LW + col + kLoOff] : LoT(0);
       return st.decode(c, h, q);
     };
 

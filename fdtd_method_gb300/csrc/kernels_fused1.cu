@@ -40,9 +40,9 @@ constexpr int kStages1 = 3;
 
 template <class S> struct Box1;
 template <> struct Box1<StoreF32> { static constexpr int kW = 40, kOff = 4, kLoW = 0; };
-template <> struct Box1<StoreF32C> { static constexpr int kW = 40, kOff = 4, kLoW = 64; };
+template <> struct Box1<StoreF32C> { static constexpr int kW = 40, kOff = 4, kLoW = 48; };
 template <> struct Box1<StoreF16> { static constexpr int kW = 48, kOff = 8, kLoW = 0; };
-constexpr int kLoOff1 = 16;
+constexpr int kLoOff1 = 8;  // BF16 lo box starts 8 columns left of the tile
 
 template <class S, int RY>
 struct Smem1 {
@@ -52,7 +52,7 @@ struct Smem1 {
   static constexpr int LW = Box1<S>::kLoW;
   static constexpr int NV = S::kComp ? 2 : 1;
   static constexpr int kHiBytes = 6 * ROWS * W * (int)sizeof(HiT);
-  static constexpr int kLoBytes = 6 * ROWS * LW;
+  static constexpr int kLoBytes = 6 * ROWS * LW * (int)sizeof(LoT);
   static constexpr int kStageBytes = (kHiBytes + kLoBytes + 127) / 128 * 128;
   static constexpr int kEBytes = 2 * 3 * NV * ROWS * 33 * 4;
   static constexpr int kTotal = kStages1 * kStageBytes + kEBytes + kStages1 * 8;
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(32 * (RY + 2))
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NS * SM::kStageBytes + SM::kEBytes);
   auto hi_of = [&](int slot) { return reinterpret_cast<const HiT*>(smem + slot * SM::kStageBytes); };
   auto lo_of = [&](int slot) {
-    return reinterpret_cast<const int8_t*>(smem + slot * SM::kStageBytes + SM::kHiBytes);
+    return reinterpret_cast<const LoT*>(smem + slot * SM::kStageBytes + SM::kHiBytes);
   };
   // sE[buf][c][v][row][col]
   auto se = [&](int buf, int c, int v, int row, int col) -> float& {
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(32 * (RY + 2))
       tma_load_3d(base + c * ROWS * W * sizeof(HiT), &maps.hi[c], x0 + kPadX - OFF, y0, kk, &bar[slot]);
     if (S::kComp)
       for (int c = 0; c < 6; ++c)
-        tma_load_3d(base + SM::kHiBytes + c * ROWS * LW, &maps.lo[c], x0 + kPadX - kLoOff1, y0, kk,
+        tma_load_3d(base + SM::kHiBytes + c * ROWS * LW * sizeof(LoT), &maps.lo[c], x0 + kPadX - kLoOff1, y0, kk,
                     &bar[slot]);
   };
 
@@ -152,10 +152,10 @@ __global__ void __launch_bounds__(32 * (RY + 2))
     const int cur = t & 1;
     mbar_wait_bounded(&bar[slot], ((t - k0) / NS) & 1, err);
     const HiT* H = hi_of(slot);
-    const int8_t* Lo = lo_of(slot);
+    const LoT* Lo = lo_of(slot);
     auto val = [&](int c, int row, int col) -> Pair {
       const HiT h = H[(c * ROWS + row) * W + col + OFF];
-      const int8_t q = S::kComp ? Lo[(c * ROWS + row) * LW + col + kLoOff1] : int8_t(0);
+      const LoT q = S::kComp ? Lo[(c * ROWS + row) * LW + col + kLoOff1] : LoT(0);
       return st.decode(c, h, q);
     };
 

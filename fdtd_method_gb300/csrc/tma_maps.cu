@@ -48,7 +48,7 @@ bool encode(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const
 
 }  // namespace
 
-cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], int8_t* const lo[6],
+cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], LoT* const lo[6],
                            int box_w, int lo_box_w, int tile_y) {
   TmaMaps* m = static_cast<TmaMaps*>(maps);
   std::memset(m, 0, sizeof(TmaMaps));
@@ -56,7 +56,7 @@ cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const 
   const size_t es = ht == HiType::F32 ? 4 : 2;
   for (int c = 0; c < 6; ++c) {
     if (!encode(&m->hi[c], dt, es, hi[c], L, box_w, tile_y)) return cudaErrorInvalidValue;
-    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, lo[c], L, lo_box_w, tile_y))
+    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, sizeof(LoT), lo[c], L, lo_box_w, tile_y))
       return cudaErrorInvalidValue;
   }
   return cudaSuccess;

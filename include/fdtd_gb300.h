@@ -50,9 +50,9 @@ enum fdtd_component {
  *                 results are bit-identical to the reference's.
  *   FP32        — FP32 storage and arithmetic.
  *   FP32_COMP   — compensated: each E/B value stored as an FP32 "hi" word plus
- *                 a signed 8-bit "lo" word in units of 2^-30 of hi's binary
- *                 exponent (a 30-bit significand in 5 bytes), updated with
- *                 error-free FP32 transformations (TwoSum, FMA products).
+ *                 a BF16 "lo" word holding what FP32 rounds away (at least a
+ *                 32-bit significand in 6 bytes), updated with error-free
+ *                 FP32 transformations (TwoSum, FMA products).
  *   FP16_SCALED — FP16 storage with a power-of-two scale per component and
  *                 FP32 arithmetic. */
 enum fdtd_precision {
