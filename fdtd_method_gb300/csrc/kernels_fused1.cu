@@ -147,10 +147,20 @@ __global__ void __launch_bounds__(32 * (RY + 2))
     pby = st.load(4, b0);
   }
 
+  // Output of an interior cell: its own position and, on the grid's edges,
+  // its ghost copies.
+  const int64_t obase = L.at(xl, yl, 0);
+  const bool edge = interior && (xl == 0 || xl == L.Ni - 1 || yl == 0 || yl == L.Nj - 1);
+  auto put = [&](int c, int z, Pair v) {
+    out.store(c, obase + (int64_t)z * L.pplane, v);
+    if (edge) store_ghost_copies(out, L, c, xl, yl, z, v);
+  };
+
+  int slot = 0;
+  uint32_t phase = 0;
   for (int t = k0; t <= k1; ++t) {
-    const int slot = (t - k0) % NS;
     const int cur = t & 1;
-    mbar_wait_bounded(&bar[slot], ((t - k0) / NS) & 1, err);
+    mbar_wait_bounded(&bar[slot], phase, err);
     const HiT* H = hi_of(slot);
     const LoT* Lo = lo_of(slot);
     auto val = [&](int c, int row, int col) -> Pair {
@@ -216,14 +226,14 @@ __global__ void __launch_bounds__(32 * (RY + 2))
           uy = A::twice(uy);
           uz = A::twice(uz);
         }
-        store_with_ghosts(out, L, 3, xl, yl, t - 1, A::acc(pbx, ux));
-        store_with_ghosts(out, L, 4, xl, yl, t - 1, A::acc(pby, uy));
-        store_with_ghosts(out, L, 5, xl, yl, t - 1, A::acc(pbz, uz));
+        put(3, t - 1, A::acc(pbx, ux));
+        put(4, t - 1, A::acc(pby, uy));
+        put(5, t - 1, A::acc(pbz, uz));
       }
       if (interior && t < k1) {
-        store_with_ghosts(out, L, 0, xl, yl, t, nex);
-        store_with_ghosts(out, L, 1, xl, yl, t, ney);
-        store_with_ghosts(out, L, 2, xl, yl, t, nez);
+        put(0, t, nex);
+        put(1, t, ney);
+        put(2, t, nez);
       }
       se(cur, 0, 0, r, cx) = nex.hi;
       se(cur, 1, 0, r, cx) = ney.hi;
@@ -242,6 +252,10 @@ __global__ void __launch_bounds__(32 * (RY + 2))
     pez = nez;
     __syncthreads();
     if (producer && t + NS <= k1) issue(t + NS);
+    if (++slot == NS) {
+      slot = 0;
+      phase ^= 1u;
+    }
   }
 }
 
