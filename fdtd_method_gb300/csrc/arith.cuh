@@ -8,8 +8,8 @@
 //               exactly with FMA (p = c*d rounded, e = fma(c, d, -p)), sums
 //               use TwoSum, and the accumulated field is renormalised so the
 //               stored pair loses nothing but its final rounding.  This is
-//               the compensated form (about 2^-30 relative per update with an
-//               int8 l word, against 2^-24 for plain FP32).
+//               the compensated form (a BF16 l word keeps the pair's significand at
+//               32 bits or more, against 24 for plain FP32).
 //
 // Every error-free step is written with __fadd_rn / __fsub_rn / __fmul_rn,
 // which the compiler never contracts or reassociates.

@@ -1,5 +1,5 @@
 // FP32-arithmetic Yee sweeps of the precision forms (plain FP32, compensated
-// FP32 hi + int8 lo, FP16 with per-component scale), on the padded layout of
+// FP32 hi + BF16 lo, FP16 with per-component scale), on the padded layout of
 // layout.cuh: one z-marching sweep per update, in place, one thread per
 // (x, y) column (B half step, E step, B double half step) — 18 values moved
 // per cell-step.  x/y neighbours come from the ghost cells; z wraps by index.

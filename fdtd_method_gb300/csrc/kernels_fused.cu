@@ -11,7 +11,7 @@
 // A CTA owns an interior tile of 64 x RY columns at (x0, y0) and marches the
 // planes k0..k1 of its z chunk.  Each plane of all six components reaches
 // shared memory as one TMA box per array (rows y0-1 .. y0+RY, columns
-// x0-4 .. x0+67 of the FP32 words, x0-16 .. x0+79 of the int8 lo words,
+// x0-4 .. x0+67 of the FP32 words, x0-8 .. x0+71 of the BF16 lo words,
 // x0-8 .. x0+71 of FP16 words), kStages planes ahead, through an mbarrier ring.
 // Every thread owns two neighbouring x cells and works on both with packed
 // float2 instructions (arith2.cuh).  Warps 0..RY are box rows 1..RY+1 (row

@@ -22,7 +22,7 @@ __device__ __forceinline__ Pair curl_term(Coef c1, Pair a1, Pair b1, Coef c2, Pa
 // A CTA owns an interior tile of 32 x RY columns at (x0, y0) and marches the
 // planes k0..k1 of its z chunk, reading each plane of all six components as
 // one TMA box per array (rows y0-1 .. y0+RY, columns x0-4 .. x0+35 for FP32
-// words, x0-16 .. x0+47 for the int8 lo words, x0-8 .. x0+39 for FP16),
+// words, x0-8 .. x0+39 for the BF16 lo words, x0-8 .. x0+39 for FP16),
 // NS planes ahead through an mbarrier ring.  Warps 0..RY are rows 1..RY+1 of
 // the box (row RY+1 computes E' only, for its neighbours); warp RY+1 computes
 // E' on column x0+nx (the x halo) for rows 1..RY.  In iteration t every

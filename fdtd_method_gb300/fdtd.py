@@ -60,7 +60,7 @@ class Axis(enum.IntEnum):
 class Precision(enum.IntEnum):
     FP64 = 0          # the drop-in: bit-identical to the reference
     FP32 = 1
-    FP32_COMP = 2     # FP32 hi + int8 lo compensated storage
+    FP32_COMP = 2     # FP32 hi + BF16 lo compensated storage
     FP16_SCALED = 3   # FP16 storage, power-of-two scale per component
 
 
