@@ -4,12 +4,14 @@
 // policies differ in how much of l they carry through an update:
 //
 //   ArithPlain  l is always 0: plain FP32 (also the FP16 storage form).
-//   ArithComp   error-free: differences keep the l parts, products are split
-//               exactly with FMA (p = c*d rounded, e = fma(c, d, -p)), sums
-//               use TwoSum, and the accumulated field is renormalised so the
-//               stored pair loses nothing but its final rounding.  This is
-//               the compensated form (a BF16 l word keeps the pair's significand at
-//               32 bits or more, against 24 for plain FP32).
+//   ArithComp   compensated accumulation: the curl increment is one float
+//               formed from differences that keep both words of each pair,
+//               and it is added to the stored pair error-free (TwoSum, then
+//               renormalisation), so the accumulated field loses nothing but
+//               its final rounding.  Source terms are double-float products
+//               (FMA splits).  This is the compensated form (a BF16 l word
+//               keeps the pair's significand at 32 bits or more, against 24
+//               for plain FP32).
 //
 // Every error-free step is written with __fadd_rn / __fsub_rn / __fmul_rn,
 // which the compiler never contracts or reassociates.
@@ -71,22 +73,20 @@ struct ArithPlain {
 
 struct ArithComp {
   static constexpr bool kPairs = true;
-  __device__ __forceinline__ static Pair diff(Pair a, Pair b) {
-    return Pair{__fsub_rn(a.hi, b.hi), __fsub_rn(a.lo, b.lo)};
+  // a - b of two stored pairs as one float: the hi words and the lo words
+  // are subtracted separately, so the difference keeps what the lo words hold
+  // (a field's accumulated precision) and is rounded relative to itself.
+  __device__ __forceinline__ static float dif(Pair a, Pair b) {
+    return __fadd_rn(__fsub_rn(a.hi, b.hi), __fsub_rn(a.lo, b.lo));
   }
-  // (c.h + c.l) * (d.h + d.l) as p + e with p = fl(c.h d.h) and e carrying
-  // the exact rounding error of p plus the cross terms.
-  __device__ __forceinline__ static Pair term(Coef c, Pair d) {
-    const float p = __fmul_rn(c.hi, d.hi);
-    float e = __fmaf_rn(c.hi, d.hi, -p);
-    e = __fmaf_rn(c.hi, d.lo, e);
-    e = __fmaf_rn(c.lo, d.hi, e);
-    return Pair{p, e};
-  }
-  __device__ __forceinline__ static Pair sub(Pair p, Pair q) {
-    float s, e;
-    two_sum(p.hi, -q.hi, s, e);
-    return Pair{s, __fadd_rn(e, __fsub_rn(p.lo, q.lo))};
+  // The curl increment c1 (a1 - b1) - c2 (a2 - b2) as one float (lo = 0),
+  // with the coefficients' lo parts folded in.  Its rounding error is
+  // relative to the increment, a small fraction of the field it is added
+  // to; the accumulation (acc) is the error-free part.
+  __device__ __forceinline__ static Pair curl(Coef c1, Pair a1, Pair b1, Coef c2, Pair a2, Pair b2) {
+    const float d1 = dif(a1, b1), d2 = dif(a2, b2);
+    const float m = __fmaf_rn(c2.hi, d2, __fmul_rn(c2.lo, d2));
+    return Pair{__fmaf_rn(c1.hi, d1, __fmaf_rn(c1.lo, d1, -m)), 0.f};
   }
   __device__ __forceinline__ static Pair add(Pair p, Pair q) {
     float s, e;
@@ -94,9 +94,6 @@ struct ArithComp {
     return Pair{s, __fadd_rn(e, __fadd_rn(p.lo, q.lo))};
   }
   __device__ __forceinline__ static Pair twice(Pair t) { return Pair{2.f * t.hi, 2.f * t.lo}; }
-  __device__ __forceinline__ static Pair curl(Coef c1, Pair a1, Pair b1, Coef c2, Pair a2, Pair b2) {
-    return sub(term(c1, diff(a1, b1)), term(c2, diff(a2, b2)));
-  }
   // Current values: double-float (hi + lo FP32 tables), so the compensated
   // form evaluates its sources without the FP64 pipe.
   using Cur = Pair;

@@ -59,18 +59,12 @@ struct Arith2<ArithPlain> {
 
 template <>
 struct Arith2<ArithComp> {
-  __device__ __forceinline__ static P2 diff(P2 a, P2 b) { return P2{sub2(a.hi, b.hi), sub2(a.lo, b.lo)}; }
-  __device__ __forceinline__ static P2 term(Coef2 c, P2 d) {
-    const float2 p = mul2(c.hi, d.hi);
-    float2 e = fma2(c.hi, d.hi, neg2(p));
-    e = fma2(c.hi, d.lo, e);
-    e = fma2(c.lo, d.hi, e);
-    return P2{p, e};
-  }
-  __device__ __forceinline__ static P2 sub(P2 p, P2 q) {
-    float2 s, e;
-    two_sum2(p.hi, neg2(q.hi), s, e);
-    return P2{s, add2(e, sub2(p.lo, q.lo))};
+  // ArithComp::dif and ArithComp::curl on both lanes.
+  __device__ __forceinline__ static float2 dif(P2 a, P2 b) { return add2(sub2(a.hi, b.hi), sub2(a.lo, b.lo)); }
+  __device__ __forceinline__ static P2 curl(Coef2 c1, P2 a1, P2 b1, Coef2 c2, P2 a2, P2 b2) {
+    const float2 d1 = dif(a1, b1), d2 = dif(a2, b2);
+    const float2 m = fma2(c2.hi, d2, mul2(c2.lo, d2));
+    return P2{fma2(c1.hi, d1, fma2(c1.lo, d1, neg2(m))), make_float2(0.f, 0.f)};
   }
   __device__ __forceinline__ static P2 add(P2 p, P2 q) {
     float2 s, e;
@@ -79,9 +73,6 @@ struct Arith2<ArithComp> {
   }
   __device__ __forceinline__ static P2 twice(P2 t) {
     return P2{mul2(t.hi, make_float2(2.f, 2.f)), mul2(t.lo, make_float2(2.f, 2.f))};
-  }
-  __device__ __forceinline__ static P2 curl(Coef2 c1, P2 a1, P2 b1, Coef2 c2, P2 a2, P2 b2) {
-    return sub(term(c1, diff(a1, b1)), term(c2, diff(a2, b2)));
   }
   __device__ __forceinline__ static P2 acc(P2 v, P2 t) {
     float2 s, e;

@@ -717,14 +717,16 @@ int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int 
   if (int rc = check_handle(h)) return rc;
   if (pipeline < FDTD_PIPELINE_AUTO || pipeline > FDTD_PIPELINE_FUSED)
     return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid pipeline");
-  if (tile_y != 0 && tile_y != 6 && tile_y != 14)
-    return fail(FDTD_ERR_INVALID_ARGUMENT, "tile_y must be 0 (default), 6 or 14");
+  if (tile_y != 0 && tile_y != 6 && tile_y != 14 && tile_y != 30)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "tile_y must be 0 (default), 6, 14 or 30");
+  if (tile_y == 30 && cells_per_thread == 2)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "tile_y 30 needs cells_per_thread 1");
   if (kchunk < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "kchunk must be >= 0");
   if (cells_per_thread < 0 || cells_per_thread > 2)
     return fail(FDTD_ERR_INVALID_ARGUMENT, "cells_per_thread must be 0 (default), 1 or 2");
   h->pipeline = pipeline;
   h->fused_cfg.tile_y = tile_y ? tile_y : 14;
-  h->fused_cfg.kchunk = kchunk ? kchunk : 64;
+  h->fused_cfg.kchunk = kchunk ? kchunk : 32;
   h->fused_cfg.cells_per_thread = cells_per_thread ? cells_per_thread : 1;
   return FDTD_OK;
 }

@@ -27,7 +27,7 @@ struct CoefSet {
 // planes per tile.
 struct FusedConfig {
   int tile_y = 14;
-  int kchunk = 64;
+  int kchunk = 32;  // short chunks keep neighbouring tiles in step, so halo sectors hit in L2
   int cells_per_thread = 1;  // 1: 32-wide tiles (kernels_fused1.cu); 2: 64-wide, packed float2
 };
 

@@ -356,7 +356,7 @@ cudaError_t launch_fused_f32(const PLayout& L, const S& st, const S& out, const 
                              const float* const J[3], bool dense_j, const CoefSet& cs,
                              const SourceSet& ss, int64_t step, int applications,
                              const FusedConfig& cfg, int* err, cudaStream_t stream) {
-  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 64;
+  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 32;
   const TmaMaps& m = *static_cast<const TmaMaps*>(maps);
   if (cfg.tile_y == 6)
     return launch_ry<S, 6>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);

@@ -1,7 +1,8 @@
 // Fused step kernel, one cell per thread (the variant for storage forms whose
 // arithmetic is light enough that occupancy matters more than packed math).
 // Same algorithm and results as kernels_fused.cu (two cells per thread); see
-// there for the description of the sweep.  Tiles are 32 x RY cells.
+// there for the description of the sweep.  Tiles are 32 x RY cells (RY = 6,
+// 14 or 30; 30 makes a 1024-thread CTA, one per SM).
 #include "arith.cuh"
 #include "engine_internal.h"
 #include "sources.cuh"
@@ -303,10 +304,12 @@ cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const
                              const float* const J[3], bool dense_j, const CoefSet& cs,
                              const SourceSet& ss, int64_t step, int applications,
                              const FusedConfig& cfg, int* err, cudaStream_t stream) {
-  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 64;
+  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 32;
   const TmaMaps& m = *static_cast<const TmaMaps*>(maps);
   if (cfg.tile_y == 6)
     return launch1_ry<S, 6>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
+  if (cfg.tile_y == 30)
+    return launch1_ry<S, 30>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
   return launch1_ry<S, 14>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
 }
 

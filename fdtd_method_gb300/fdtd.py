@@ -304,7 +304,7 @@ class FDTD:
     def set_pipeline(self, pipeline="auto", tile_y=0, kchunk=0, cells_per_thread=0):
         """Step pipeline of the FP32-arithmetic forms: 'fused' (one sweep per
         step, the default) or 'split' (one sweep per half step); same results.
-        tile_y (14 or 6), kchunk and cells_per_thread (1 or 2) shape the fused
+        tile_y (6, 14 or 30), kchunk and cells_per_thread (1 or 2) shape the fused
         launch; 0 keeps the default."""
         _lib.check(self._lib.fdtd_set_pipeline(self._handle(), self.PIPELINES[pipeline], int(tile_y), int(kchunk),
                                                int(cells_per_thread)))

@@ -186,8 +186,9 @@ int fdtd_set_kernel_timing(fdtd_handle* h, int enabled);
 /* Step pipeline of the FP32-arithmetic forms (new; tuning and testing).
  * AUTO and FUSED: one sweep per step (E step + double B half step); SPLIT:
  * one sweep per half step.  All give bit-identical results.  The fused
- * launch is shaped by tile_y (interior rows of a tile: 14 or 6; 0 = 14),
- * kchunk (planes per tile; 0 = 64) and cells_per_thread (1: 32-wide tiles,
+ * launch is shaped by tile_y (interior rows of a tile: 6, 14 or 30; 0 = 14;
+ * 30 only with cells_per_thread 1),
+ * kchunk (planes per tile; 0 = 32) and cells_per_thread (1: 32-wide tiles,
  * 2: 64-wide tiles with packed two-cell arithmetic; 0 = 1).  The FP64 form
  * always uses the split sweeps. */
 enum fdtd_pipeline { FDTD_PIPELINE_AUTO = 0, FDTD_PIPELINE_SPLIT = 1, FDTD_PIPELINE_FUSED = 2 };
