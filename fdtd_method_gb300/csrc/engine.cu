@@ -101,6 +101,10 @@ struct fdtd_handle {
   // shape changes; swapped with the copies).
   TmaMaps maps_cur;
   TmaMaps maps_alt;
+  // Store maps (grid cells only) of both copies, for the one-cell-per-thread
+  // fused kernel.
+  TmaMaps smaps_cur;
+  TmaMaps smaps_alt;
   int maps_tile_y = 0;
   int* d_err = nullptr;  // device status word (bounded waits that gave up)
 
@@ -349,6 +353,9 @@ int ensure_alt(fdtd_handle* h) {
     if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, lbw, h->fused_cfg.tile_y) != cudaSuccess ||
         build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, h->fused_cfg.tile_y) != cudaSuccess)
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
+    if (!two && (build_tma_store_maps(&h->smaps_cur, h->L, ht, h->field, lo_cur, h->fused_cfg.tile_y) != cudaSuccess ||
+                 build_tma_store_maps(&h->smaps_alt, h->L, ht, h->alt_field, lo_alt, h->fused_cfg.tile_y) != cudaSuccess))
+      return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
     h->maps_tile_y = key;
   }
   return FDTD_OK;
@@ -365,7 +372,10 @@ int run_fused(fdtd_handle* h, int64_t step, int apps) {
   const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
   const bool dj = h->dense_j && h->jf[0];
   const FusedConfig& cf = h->fused_cfg;
-  const void* m = &h->maps_cur;
+  StepMaps sm;
+  sm.ld = h->maps_cur;
+  sm.st = h->smaps_alt;
+  const void* m = cf.cells_per_thread == 2 ? static_cast<const void*>(&h->maps_cur) : static_cast<const void*>(&sm);
   cudaError_t e = cudaSuccess;
 #define FDTD_FUSED_LAUNCH(FN)                                                                                  \
   switch (h->form) {                                                                                         \
@@ -387,6 +397,7 @@ int run_fused(fdtd_handle* h, int64_t step, int apps) {
     std::swap(h->lo[c], h->alt_lo[c]);
   }
   std::swap(h->maps_cur, h->maps_alt);
+  std::swap(h->smaps_cur, h->smaps_alt);
   return FDTD_OK;
 }
 
@@ -726,7 +737,7 @@ int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int 
     return fail(FDTD_ERR_INVALID_ARGUMENT, "cells_per_thread must be 0 (default), 1 or 2");
   h->pipeline = pipeline;
   h->fused_cfg.tile_y = tile_y ? tile_y : 14;
-  h->fused_cfg.kchunk = kchunk ? kchunk : 32;
+  h->fused_cfg.kchunk = kchunk ? kchunk : 24;
   h->fused_cfg.cells_per_thread = cells_per_thread ? cells_per_thread : 1;
   return FDTD_OK;
 }

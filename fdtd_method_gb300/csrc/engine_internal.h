@@ -27,7 +27,7 @@ struct CoefSet {
 // planes per tile.
 struct FusedConfig {
   int tile_y = 14;
-  int kchunk = 32;  // short chunks keep neighbouring tiles in step, so halo sectors hit in L2
+  int kchunk = 24;  // short chunks keep neighbouring tiles in step, so halo sectors hit in L2
   int cells_per_thread = 1;  // 1: 32-wide tiles (kernels_fused1.cu); 2: 64-wide, packed float2
 };
 
@@ -54,7 +54,8 @@ cudaError_t launch_fused_f32(const PLayout& L, const S& st, const S& out, const 
 template <class S>
 int fused_box_width();
 int fused_lo_box_width();
-// kernels_fused1.cu: the same sweep with one cell per thread (32-wide tiles).
+// kernels_fused1.cu: the same sweep with one cell per thread (32-wide tiles);
+// `maps` is a StepMaps: load maps of `st`'s arrays, store maps of `out`'s.
 template <class S>
 cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const void* maps,
                               const float* const J[3], bool dense_j, const CoefSet& cs,
@@ -67,6 +68,10 @@ int fused1_lo_box_width();
 // tma_maps.cu: tensor maps of the six hi arrays (and six lo arrays of the
 // compensated form) for a fused tile of `tile_y` interior rows.
 enum class HiType { F32, F16 };
+// Store maps of the fused1 kernel: the grid cells of each array (ghosts and
+// margins excluded), box 32 x tile_y.
+cudaError_t build_tma_store_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], LoT* const lo[6],
+                                 int tile_y);
 cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6],
                            LoT* const lo[6], int box_w, int lo_box_w, int tile_y);
 

@@ -1,8 +1,38 @@
-// Fused step kernel, one cell per thread (the variant for storage forms whose
-// arithmetic is light enough that occupancy matters more than packed math).
-// Same algorithm and results as kernels_fused.cu (two cells per thread); see
-// there for the description of the sweep.  Tiles are 32 x RY cells (RY = 6,
-// 14 or 30; 30 makes a 1024-thread CTA, one per SM).
+// Fused step kernel, one cell per thread: the default step of the
+// FP32-arithmetic forms.  One sweep advances one update_fields step (the E
+// step and the B half steps around it); the arithmetic is that of the split
+// sweeps (kernels_f32.cu, the reference's functors kokkos_functors.h:64-90 E
+// and :128-151 B), reproduced bit for bit.
+//
+// A CTA owns a tile of 32 x RY cells at (x0, y0) (RY = 6, 14 or 30) and
+// marches the planes k0..k1 of its z chunk.  Warps 0..RY are the box rows
+// 1..RY+1 (the last computes E' only, for the B update of the row below it);
+// warp RY+1 computes E' on the x halo column for rows 1..RY.
+//
+// Data movement, per plane:
+//   in   one 3-D TMA box per stored array (hi words: columns x0-4 .. x0+35,
+//        BF16 lo and FP16 words: x0-8 .. x0+39; rows y0-1 .. y0+RY), NS
+//        planes ahead through an mbarrier ring;
+//   out  E'(t) and B'(t-1) are written to shared staging boxes of 32 x RY in
+//        their stored encoding; one thread stores them with TMA through
+//        interior-only tensor maps (the copy engine clips rows past the
+//        grid; a tile narrower than 32 columns stores with plain stores,
+//        since clipping along x is in 16-byte units).  Tiles on the grid's
+//        edges also write the ghost copies of their edge cells with plain
+//        stores.
+// The E' staging box doubles as the exchange plane from which the next
+// iteration reads E'(t-1) at i+1 and j+1; it has two extra rows, holding the
+// halo row's and the halo column's E'.
+//
+// In iteration t every thread
+//   1. computes E'(t) = E + c curl B of its cell (B at i-1, j-1 from the box,
+//      B(t-1) carried in registers);
+//   2. on interior cells (t > k0), computes B'(t-1) = B(t-1) + apps (c/2) curl E'
+//      (E'(t-1) at i+1, j+1 from the exchange plane, E'(t) in registers);
+//   3. writes both to staging, and the CTA synchronises once; thread 0 then
+//      stores the staged boxes and refills the freed ring slot.
+// The sweep reads the state from `st` and writes the new state to `out`:
+// neighbouring tiles read what a tile writes, so an in-place update would race.
 #include "arith.cuh"
 #include "engine_internal.h"
 #include "sources.cuh"
@@ -13,132 +43,141 @@ namespace fdtd {
 template <class S> struct ArithOf1 { using type = ArithPlain; };
 template <> struct ArithOf1<StoreF32C> { using type = ArithComp; };
 
-template <class A>
-__device__ __forceinline__ Pair curl_term(Coef c1, Pair a1, Pair b1, Coef c2, Pair a2, Pair b2) {
-  return A::curl(c1, a1, b1, c2, a2, b2);
-}
-
-// Fused pipeline.
-//
-// A CTA owns an interior tile of 32 x RY columns at (x0, y0) and marches the
-// planes k0..k1 of its z chunk, reading each plane of all six components as
-// one TMA box per array (rows y0-1 .. y0+RY, columns x0-4 .. x0+35 for FP32
-// words, x0-8 .. x0+39 for the BF16 lo words, x0-8 .. x0+39 for FP16),
-// NS planes ahead through an mbarrier ring.  Warps 0..RY are rows 1..RY+1 of
-// the box (row RY+1 computes E' only, for its neighbours); warp RY+1 computes
-// E' on column x0+nx (the x halo) for rows 1..RY.  In iteration t every
-// thread
-//   1. computes E'(t) = E + c curl B of its cell (B at i-1, j-1 from the
-//      box, B(t-1) carried in registers);
-//   2. computes B'(t-1) = B(t-1) + apps (c/2) curl E' (E'(t-1) at i+1, j+1
-//      from shared memory, E'(t) in registers) on interior cells;
-//   3. stores E'(t) (t < k1) and B'(t-1), publishes E'(t), and the CTA
-//      synchronises once; thread 0 then refills the freed ring slot.
-// The sweep reads the state from `st` and writes the new state to `out`:
-// neighbouring tiles read what a tile writes, so an in-place update would race.
-
 constexpr int kStages1 = 3;
+constexpr int kLoOff1 = 8;  // BF16 lo boxes start 8 columns left of the tile
 
 template <class S> struct Box1;
 template <> struct Box1<StoreF32> { static constexpr int kW = 40, kOff = 4, kLoW = 0; };
 template <> struct Box1<StoreF32C> { static constexpr int kW = 40, kOff = 4, kLoW = 48; };
 template <> struct Box1<StoreF16> { static constexpr int kW = 48, kOff = 8, kLoW = 0; };
-constexpr int kLoOff1 = 8;  // BF16 lo box starts 8 columns left of the tile
 
+constexpr int round128(int b) { return (b + 127) / 128 * 128; }
+
+// Shared-memory plan (byte offsets).
 template <class S, int RY>
-struct Smem1 {
+struct Plan1 {
   using HiT = typename S::HiT;
+  static constexpr bool kLo = S::kComp;
   static constexpr int ROWS = RY + 2;
-  static constexpr int W = Box1<S>::kW;
-  static constexpr int LW = Box1<S>::kLoW;
-  static constexpr int NV = S::kComp ? 2 : 1;
-  static constexpr int kHiBytes = 6 * ROWS * W * (int)sizeof(HiT);
-  static constexpr int kLoBytes = 6 * ROWS * LW * (int)sizeof(LoT);
-  static constexpr int kStageBytes = (kHiBytes + kLoBytes + 127) / 128 * 128;
-  static constexpr int kEBytes = 2 * 3 * NV * ROWS * 33 * 4;
-  static constexpr int kTotal = kStages1 * kStageBytes + kEBytes + kStages1 * 8;
-  static constexpr uint32_t kTx = kHiBytes + kLoBytes;
+  static constexpr int W = Box1<S>::kW, LW = Box1<S>::kLoW, OFF = Box1<S>::kOff;
+  static constexpr int HS = (int)sizeof(HiT), LS = (int)sizeof(LoT);
+  // ring stage: 6 hi boxes, then 6 lo boxes
+  static constexpr int kHiBox = ROWS * W * HS;
+  static constexpr int kLoBox = ROWS * LW * LS;
+  static constexpr uint32_t kTx = 6 * kHiBox + 6 * kLoBox;
+  static constexpr int kStage = round128(6 * kHiBox + 6 * kLoBox);
+  // E' exchange / staging buffer: per component RY+2 rows of 32 (rows 0..RY-1
+  // the tile, row RY the halo row, row RY+1 the halo column by row), hi words
+  // then lo words.
+  static constexpr int kXComp = (RY + 2) * 32;  // elements per component
+  static constexpr int kXHi = 0;
+  static constexpr int kXLo = round128(3 * kXComp * HS);
+  static constexpr int kXBytes = kXLo + (kLo ? round128(3 * kXComp * LS) : 0);
+  // B' staging buffer: per component RY rows of 32, hi words then lo words.
+  static constexpr int kBComp = RY * 32;
+  static constexpr int kBLo = round128(3 * kBComp * HS);
+  static constexpr int kBBytes = kBLo + (kLo ? round128(3 * kBComp * LS) : 0);
+  static constexpr int kRing = 0;
+  static constexpr int kExch = kStages1 * kStage;
+  static constexpr int kBst = kExch + 2 * kXBytes;
+  static constexpr int kBar = kBst + 2 * kBBytes;
+  static constexpr int kList = kBar + kStages1 * 8;
+  static constexpr int kTotal = kList + 4 * (kMaxSources + 1);
+  static_assert((kXComp * HS) % 128 == 0 && (kXComp * LS) % 128 == 0, "staging boxes must stay 128-byte aligned");
+  static_assert((kBComp * HS) % 128 == 0 && (kBComp * LS) % 128 == 0, "staging boxes must stay 128-byte aligned");
 };
 
-template <class S, class A, int RY, int kApps, bool kDenseJ, int kSrc>
+// Whether the periodic window [o, o+n) of an axis of length N meets the m
+// consecutive cells a, a+1, .. (taken mod N).
+__device__ __forceinline__ bool window_meets(int o, int n, int N, int a, int m) {
+  int s = a - o;
+  if (s < 0) s += N;
+  return s < n || s + m > N;
+}
+
+template <class S, class A, int RY, int kApps, bool kDenseJ>
 __global__ void __launch_bounds__(32 * (RY + 2))
-    fused1(PLayout L, S st, S out, const __grid_constant__ TmaMaps maps, CoefSet cs, int kchunk,
-              const float* __restrict__ Jx, const float* __restrict__ Jy,
-              const float* __restrict__ Jz, SourceSet ss, int64_t step, int* err) {
-  using SM = Smem1<S, RY>;
+    fused1(PLayout L, S st, S out, const __grid_constant__ StepMaps maps, CoefSet cs, int kchunk,
+           const float* __restrict__ Jx, const float* __restrict__ Jy, const float* __restrict__ Jz,
+           SourceSet ss, int64_t step, int* err) {
+  using P = Plan1<S, RY>;
   using HiT = typename S::HiT;
   using T = typename A::Cur;
-  constexpr int ROWS = SM::ROWS, W = SM::W, LW = SM::LW, NV = SM::NV, OFF = Box1<S>::kOff;
   constexpr int NS = kStages1;
-  constexpr int EC = 33;  // columns of the E' exchange (32 interior + the x halo)
   extern __shared__ __align__(128) unsigned char smem[];
-  float* sE = reinterpret_cast<float*>(smem + NS * SM::kStageBytes);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NS * SM::kStageBytes + SM::kEBytes);
-  auto hi_of = [&](int slot) { return reinterpret_cast<const HiT*>(smem + slot * SM::kStageBytes); };
-  auto lo_of = [&](int slot) {
-    return reinterpret_cast<const LoT*>(smem + slot * SM::kStageBytes + SM::kHiBytes);
-  };
-  // sE[buf][c][v][row][col]
-  auto se = [&](int buf, int c, int v, int row, int col) -> float& {
-    return sE[(((buf * 3 + c) * NV + v) * ROWS + row) * EC + col];
-  };
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + P::kBar);
+  int* list = reinterpret_cast<int*>(smem + P::kList);
 
   const int lane = threadIdx.x, w = threadIdx.y;
   const int x0 = blockIdx.x * 32, y0 = blockIdx.y * RY;
   const int nx = min(32, L.Ni - x0), ny = min(RY, L.Nj - y0);
-  const bool halo = (w == RY + 1);
-  const int r = halo ? lane + 1 : w + 1;   // box row
-  const int cx = halo ? nx : lane;          // column within the tile (0..32)
-  const bool active = halo ? (lane < ny) : (r <= ny + 1 && lane < nx);
-  const bool interior = !halo && r <= ny && lane < nx;
-  // logical coordinates of the cell (x = Ni and y = Nj are the ghost copies of 0)
+  const bool hcol = (w == RY + 1);
+  // box row (lanes of the halo-column warp past the tile's rows are clamped
+  // onto its last row: they compute but never publish)
+  const int r = hcol ? min(lane, RY - 1) + 1 : w + 1;
+  const int cx = hcol ? nx : lane;        // column within the tile (0..32)
+  const bool active = hcol ? (lane < ny) : (r <= ny + 1 && lane < nx);
+  const bool interior = !hcol && r <= ny && lane < nx;
+  // logical coordinates (x = Ni and y = Nj are the ghost copies of 0)
   const int xu = x0 + cx, yu = y0 + r - 1;
   const int xl = xu >= L.Ni ? xu - L.Ni : xu, yl = yu >= L.Nj ? yu - L.Nj : yu;
   const int k0 = blockIdx.z * kchunk;
   const int k1 = min(k0 + kchunk, L.Nk);
-  const bool producer = (w == 0 && lane == 0);
+  const bool leader = (w == 0 && lane == 0);
+  const bool tile_edge = x0 == 0 || x0 + nx == L.Ni || y0 == 0 || y0 + ny == L.Nj;
+  // The copy engine clips a store along x in 16-byte units, not elements: a
+  // tile narrower than 32 columns would overwrite the ghost column past the
+  // grid's last cell.  Such tiles (the last tile column when Ni is not a
+  // multiple of 32) store with plain per-thread stores instead.
+  const bool tma_out = (nx == 32);
+  const bool edge_cell = interior && (xl == 0 || xl == L.Ni - 1 || yl == 0 || yl == L.Nj - 1);
+
+  // Element offsets of this thread in the exchange rows: where it publishes
+  // E', and where it finds E' at (r+1, cx) and (r, cx+1).
+  const int xo_own = hcol ? (RY + 1) * 32 + (r - 1) : (r == ny + 1 ? RY * 32 + cx : (r - 1) * 32 + cx);
+  const int xo_up = (r == ny) ? RY * 32 + cx : r * 32 + cx;
+  const int xo_right = (cx + 1 == nx) ? (RY + 1) * 32 + (r - 1) : (r - 1) * 32 + cx + 1;
+  const int bo_own = (r - 1) * 32 + cx;
+  const int hi_own = r * P::W + cx + P::OFF;     // ring box offsets (elements)
+  const int lo_own = r * P::LW + cx + kLoOff1;
 
   auto issue = [&](int t) {
     const int slot = (t - k0) % NS;
     const int kk = (t == L.Nk) ? 0 : t;
-    unsigned char* base = smem + slot * SM::kStageBytes;
-    mbar_arrive_expect_tx(&bar[slot], SM::kTx);
-    for (int c = 0; c < 6; ++c)
-      tma_load_3d(base + c * ROWS * W * sizeof(HiT), &maps.hi[c], x0 + kPadX - OFF, y0, kk, &bar[slot]);
-    if (S::kComp)
+    unsigned char* base = smem + P::kRing + slot * P::kStage;
+    mbar_arrive_expect_tx(&bar[slot], P::kTx);
+    for (int c = 0; c < 6; ++c) tma_load_3d(base + c * P::kHiBox, &maps.ld.hi[c], x0 + kPadX - P::OFF, y0, kk, &bar[slot]);
+    if (P::kLo)
       for (int c = 0; c < 6; ++c)
-        tma_load_3d(base + SM::kHiBytes + c * ROWS * LW * sizeof(LoT), &maps.lo[c], x0 + kPadX - kLoOff1, y0, kk,
-                    &bar[slot]);
+        tma_load_3d(base + 6 * P::kHiBox + c * P::kLoBox, &maps.ld.lo[c], x0 + kPadX - kLoOff1, y0, kk, &bar[slot]);
   };
 
-  if (producer) {
+  // Sources that can touch this tile's cells (its E' halo included), in
+  // registration order; the exact per-cell test comes later.
+  if (w == 0) {
+    int n = 0;
+    for (int b = 0; b < ss.count; b += 32) {
+      const int q = b + lane;
+      bool hit = false;
+      if (q < ss.count) {
+        const DevSource& d = ss.src[q];
+        hit = step < d.n_amp && window_meets(d.i0, d.ni, L.Ni, x0, nx + 1) &&
+              window_meets(d.j0, d.nj, L.Nj, y0, ny + 1);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (hit) list[n + __popc(m & ((1u << lane) - 1u))] = q;
+      n += __popc(m);
+    }
+    if (lane == 0) list[kMaxSources] = n;
+  }
+  if (leader) {
     for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
     mbar_init_fence();
   }
   __syncthreads();
-  if (producer)
+  const int nsrc = list[kMaxSources];
+  if (leader)
     for (int t = k0; t <= k1 && t < k0 + NS; ++t) issue(t);
-
-  // Sources: per-column factor (amp gx) gy, once per launch.
-  T sxy[kFastSources];
-  unsigned smask = 0;
-#pragma unroll
-  for (int q = 0; q < kFastSources; ++q) sxy[q] = A::cur_zero();
-  if (kSrc == 1 && active) {
-#pragma unroll
-    for (int q = 0; q < kFastSources; ++q) {
-      if (q < ss.count) {
-        const DevSource& d = ss.src[q];
-        const int di = box_offset(xl, d.i0, d.ni, L.Ni);
-        const int dj = box_offset(yl, d.j0, d.nj, L.Nj);
-        if (step < d.n_amp && di >= 0 && dj >= 0) {
-          sxy[q] = A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + step), A::cur_table(ss, d.gx_off + di)),
-                              A::cur_table(ss, d.gy_off + dj));
-          smask |= 1u << q;
-        }
-      }
-    }
-  }
 
   Pair pbx{0.f, 0.f}, pby{0.f, 0.f}, pbz{0.f, 0.f};
   Pair pex{0.f, 0.f}, pey{0.f, 0.f}, pez{0.f, 0.f};
@@ -148,164 +187,208 @@ __global__ void __launch_bounds__(32 * (RY + 2))
     pby = st.load(4, b0);
   }
 
-  // Output of an interior cell: its own position and, on the grid's edges,
-  // its ghost copies.
-  const int64_t obase = L.at(xl, yl, 0);
-  const bool edge = interior && (xl == 0 || xl == L.Ni - 1 || yl == 0 || yl == L.Nj - 1);
-  auto put = [&](int c, int z, Pair v) {
-    out.store(c, obase + (int64_t)z * L.pplane, v);
-    if (edge) store_ghost_copies(out, L, c, xl, yl, z, v);
-  };
-
   int slot = 0;
   uint32_t phase = 0;
   for (int t = k0; t <= k1; ++t) {
     const int cur = t & 1;
+    const int kk = (t == L.Nk) ? 0 : t;
     mbar_wait_bounded(&bar[slot], phase, err);
-    const HiT* H = hi_of(slot);
-    const LoT* Lo = lo_of(slot);
-    auto val = [&](int c, int row, int col) -> Pair {
-      const HiT h = H[(c * ROWS + row) * W + col + OFF];
-      const LoT q = S::kComp ? Lo[(c * ROWS + row) * LW + col + kLoOff1] : LoT(0);
+    const unsigned char* stage = smem + P::kRing + slot * P::kStage;
+    const HiT* H = reinterpret_cast<const HiT*>(stage) + hi_own;
+    const LoT* Q = reinterpret_cast<const LoT*>(stage + 6 * P::kHiBox) + lo_own;
+    // component c at box offset (dr rows, dc columns) from this thread's cell
+    auto V = [&](int c, int dr, int dc) -> Pair {
+      const HiT h = H[c * P::ROWS * P::W + dr * P::W + dc];
+      const LoT q = P::kLo ? Q[c * P::ROWS * P::LW + dr * P::LW + dc] : LoT(0);
       return st.decode(c, h, q);
     };
 
-    Pair bx{0.f, 0.f}, by{0.f, 0.f}, bz{0.f, 0.f}, nex{0.f, 0.f}, ney{0.f, 0.f}, nez{0.f, 0.f};
-    if (active) {
-      const int kk = (t == L.Nk) ? 0 : t;
-      bx = val(3, r, cx);
-      by = val(4, r, cx);
-      bz = val(5, r, cx);
-      const Pair ex = val(0, r, cx), ey = val(1, r, cx), ez = val(2, r, cx);
-      Pair qx = curl_term<A>(cs.ce[1], bz, val(5, r - 1, cx), cs.ce[2], by, pby);
-      Pair qy = curl_term<A>(cs.ce[2], bx, pbx, cs.ce[0], bz, val(5, r, cx - 1));
-      Pair qz = curl_term<A>(cs.ce[0], by, val(4, r, cx - 1), cs.ce[1], bx, val(3, r - 1, cx));
+    // 1. E'(t)
+    const Pair bx = V(3, 0, 0), by = V(4, 0, 0), bz = V(5, 0, 0);
+    Pair qx = A::curl(cs.ce[1], bz, V(5, -1, 0), cs.ce[2], by, pby);
+    Pair qy = A::curl(cs.ce[2], bx, pbx, cs.ce[0], bz, V(5, 0, -1));
+    Pair qz = A::curl(cs.ce[0], by, V(4, 0, -1), cs.ce[1], bx, V(3, -1, 0));
+    if (kDenseJ || nsrc > 0) {
       T jv[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
       bool has_j = false;
-      if (kDenseJ) {
+      if (kDenseJ && active) {
         const int64_t d = xl + (int64_t)yl * L.Ni + (int64_t)kk * L.Ni * L.Nj;
         jv[0] = A::cur_dense(Jx[d]);
         jv[1] = A::cur_dense(Jy[d]);
         jv[2] = A::cur_dense(Jz[d]);
         has_j = true;
       }
-      if (kSrc == 1) {
-#pragma unroll
-        for (int q = 0; q < kFastSources; ++q) {
-          if (smask & (1u << q)) {
-            const DevSource& d = ss.src[q];
-            const int dk = box_offset(kk, d.k0, d.nk, L.Nk);
-            if (dk >= 0) {
-              add_current<A>(jv, d.comp_mask, A::cur_mul(sxy[q], A::cur_table(ss, d.gz_off + dk)));
-              has_j = true;
-            }
-          }
+      for (int i = 0; i < nsrc; ++i) {
+        const DevSource& d = ss.src[list[i]];
+        const int dk = box_offset(kk, d.k0, d.nk, L.Nk);
+        if (dk < 0) continue;
+        const int di = box_offset(xl, d.i0, d.ni, L.Ni);
+        const int dj = box_offset(yl, d.j0, d.nj, L.Nj);
+        if (active && di >= 0 && dj >= 0) {
+          add_current<A>(jv, d.comp_mask,
+                         A::cur_mul(A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + step),
+                                                          A::cur_table(ss, d.gx_off + di)),
+                                               A::cur_table(ss, d.gy_off + dj)),
+                                    A::cur_table(ss, d.gz_off + dk)));
+          has_j = true;
         }
-      } else if (kSrc == 2) {
-        has_j |= source_sum<A>(ss, step, xl, yl, kk, L, jv);
       }
       if (has_j) {
         qx = A::add(qx, A::cur_term(cs.cj, jv[0]));
         qy = A::add(qy, A::cur_term(cs.cj, jv[1]));
         qz = A::add(qz, A::cur_term(cs.cj, jv[2]));
       }
-      // E' as its storage form will hold it (what the split sweeps reload).
-      nex = st.quantize(0, A::acc(ex, qx));
-      ney = st.quantize(1, A::acc(ey, qy));
-      nez = st.quantize(2, A::acc(ez, qz));
+    }
+    const Pair ax = A::acc(V(0, 0, 0), qx), ay = A::acc(V(1, 0, 0), qy), az = A::acc(V(2, 0, 0), qz);
+    // E' in its stored words; the B update uses the value they hold.
+    const HiT ehx = st.enc_hi(0, ax), ehy = st.enc_hi(1, ay), ehz = st.enc_hi(2, az);
+    const LoT elx = st.enc_lo(ax), ely = st.enc_lo(ay), elz = st.enc_lo(az);
+    const Pair nex = st.decode(0, ehx, elx), ney = st.decode(1, ehy, ely), nez = st.decode(2, ehz, elz);
 
-      if (interior && t > k0) {
-        const int prv = cur ^ 1;
-        auto eget = [&](int c, int row, int col) {
-          return Pair{se(prv, c, 0, row, col), NV == 2 ? se(prv, c, NV - 1, row, col) : 0.f};
-        };
-        Pair ux = curl_term<A>(cs.cb[2], ney, pey, cs.cb[1], eget(2, r + 1, cx), pez);
-        Pair uy = curl_term<A>(cs.cb[0], eget(2, r, cx + 1), pez, cs.cb[2], nex, pex);
-        Pair uz = curl_term<A>(cs.cb[1], eget(0, r + 1, cx), pex, cs.cb[0], eget(1, r, cx + 1), pey);
-        if (kApps == 2) {
-          ux = A::twice(ux);
-          uy = A::twice(uy);
-          uz = A::twice(uz);
-        }
-        put(3, t - 1, A::acc(pbx, ux));
-        put(4, t - 1, A::acc(pby, uy));
-        put(5, t - 1, A::acc(pbz, uz));
-      }
-      if (interior && t < k1) {
-        put(0, t, nex);
-        put(1, t, ney);
-        put(2, t, nez);
-      }
-      se(cur, 0, 0, r, cx) = nex.hi;
-      se(cur, 1, 0, r, cx) = ney.hi;
-      se(cur, 2, 0, r, cx) = nez.hi;
-      if (NV == 2) {
-        se(cur, 0, NV - 1, r, cx) = nex.lo;
-        se(cur, 1, NV - 1, r, cx) = ney.lo;
-        se(cur, 2, NV - 1, r, cx) = nez.lo;
+    unsigned char* xb = smem + P::kExch + cur * P::kXBytes;
+    if (active) {
+      HiT* xh = reinterpret_cast<HiT*>(xb + P::kXHi) + xo_own;
+      xh[0] = ehx;
+      xh[P::kXComp] = ehy;
+      xh[2 * P::kXComp] = ehz;
+      if (P::kLo) {
+        LoT* xq = reinterpret_cast<LoT*>(xb + P::kXLo) + xo_own;
+        xq[0] = elx;
+        xq[P::kXComp] = ely;
+        xq[2 * P::kXComp] = elz;
       }
     }
+
+    // 2. B'(t-1)
+    Pair nbx{0.f, 0.f}, nby{0.f, 0.f}, nbz{0.f, 0.f};
+    unsigned char* bb = smem + P::kBst + cur * P::kBBytes;
+    if (t > k0 && interior) {
+      const unsigned char* pb = smem + P::kExch + (cur ^ 1) * P::kXBytes;
+      const HiT* ph = reinterpret_cast<const HiT*>(pb + P::kXHi);
+      const LoT* pq = reinterpret_cast<const LoT*>(pb + P::kXLo);
+      auto E = [&](int c, int off) -> Pair {
+        return st.decode(c, ph[c * P::kXComp + off], P::kLo ? pq[c * P::kXComp + off] : LoT(0));
+      };
+      Pair ux = A::curl(cs.cb[2], ney, pey, cs.cb[1], E(2, xo_up), pez);
+      Pair uy = A::curl(cs.cb[0], E(2, xo_right), pez, cs.cb[2], nex, pex);
+      Pair uz = A::curl(cs.cb[1], E(0, xo_up), pex, cs.cb[0], E(1, xo_right), pey);
+      if (kApps == 2) {
+        ux = A::twice(ux);
+        uy = A::twice(uy);
+        uz = A::twice(uz);
+      }
+      nbx = A::acc(pbx, ux);
+      nby = A::acc(pby, uy);
+      nbz = A::acc(pbz, uz);
+      HiT* bh = reinterpret_cast<HiT*>(bb) + bo_own;
+      bh[0] = st.enc_hi(3, nbx);
+      bh[P::kBComp] = st.enc_hi(4, nby);
+      bh[2 * P::kBComp] = st.enc_hi(5, nbz);
+      if (P::kLo) {
+        LoT* bq = reinterpret_cast<LoT*>(bb + P::kBLo) + bo_own;
+        bq[0] = st.enc_lo(nbx);
+        bq[P::kBComp] = st.enc_lo(nby);
+        bq[2 * P::kBComp] = st.enc_lo(nbz);
+      }
+    }
+    if (!tma_out && interior) {
+      const int64_t o = L.at(xl, yl, 0);
+      if (t < k1) {
+        out.store(0, o + (int64_t)t * L.pplane, nex);
+        out.store(1, o + (int64_t)t * L.pplane, ney);
+        out.store(2, o + (int64_t)t * L.pplane, nez);
+      }
+      if (t > k0) {
+        out.store(3, o + (int64_t)(t - 1) * L.pplane, nbx);
+        out.store(4, o + (int64_t)(t - 1) * L.pplane, nby);
+        out.store(5, o + (int64_t)(t - 1) * L.pplane, nbz);
+      }
+    }
+    // Ghost copies of edge cells (their tiles only).
+    if (tile_edge && edge_cell) {
+      if (t < k1) {
+        store_ghost_copies(out, L, 0, xl, yl, t, nex);
+        store_ghost_copies(out, L, 1, xl, yl, t, ney);
+        store_ghost_copies(out, L, 2, xl, yl, t, nez);
+      }
+      if (t > k0) {
+        store_ghost_copies(out, L, 3, xl, yl, t - 1, nbx);
+        store_ghost_copies(out, L, 4, xl, yl, t - 1, nby);
+        store_ghost_copies(out, L, 5, xl, yl, t - 1, nbz);
+      }
+    }
+
     pbx = bx;
     pby = by;
     pbz = bz;
     pex = nex;
     pey = ney;
     pez = nez;
+    fence_async_smem();
+    // The previous iteration's stores must have read their staging (written
+    // again next iteration) before anyone passes this barrier.
+    if (leader) bulk_wait_read_all();
     __syncthreads();
-    if (producer && t + NS <= k1) issue(t + NS);
+    if (leader) {
+      if (tma_out && t < k1)
+        for (int c = 0; c < 3; ++c) {
+          tma_store_3d(&maps.st.hi[c], xb + P::kXHi + c * P::kXComp * P::HS, x0, y0, t);
+          if (P::kLo) tma_store_3d(&maps.st.lo[c], xb + P::kXLo + c * P::kXComp * P::LS, x0, y0, t);
+        }
+      if (tma_out && t > k0)
+        for (int c = 0; c < 3; ++c) {
+          tma_store_3d(&maps.st.hi[3 + c], bb + c * P::kBComp * P::HS, x0, y0, t - 1);
+          if (P::kLo) tma_store_3d(&maps.st.lo[3 + c], bb + P::kBLo + c * P::kBComp * P::LS, x0, y0, t - 1);
+        }
+      bulk_commit();
+      if (t + NS <= k1) issue(t + NS);
+    }
     if (++slot == NS) {
       slot = 0;
       phase ^= 1u;
     }
   }
+  if (leader) bulk_wait_all();
 }
 
 // ---------------------------------------------------------------------------
 
-template <class S, int RY, int APPS, bool DJ, int SRC>
-static cudaError_t launch1_one(dim3 grid, const PLayout& L, const S& st, const S& out,
-                                    const TmaMaps& maps, const CoefSet& cs, int kchunk,
-                                    const float* const J[3], const SourceSet& ss, int64_t step,
-                                    int* err, cudaStream_t stream) {
+template <class S, int RY, int APPS, bool DJ>
+static cudaError_t launch1_one(dim3 grid, const PLayout& L, const S& st, const S& out, const StepMaps& maps,
+                               const CoefSet& cs, int kchunk, const float* const J[3], const SourceSet& ss,
+                               int64_t step, int* err, cudaStream_t stream) {
   using A = typename ArithOf1<S>::type;
-  auto kern = fused1<S, A, RY, APPS, DJ, SRC>;
-  const int bytes = Smem1<S, RY>::kTotal;
+  auto kern = fused1<S, A, RY, APPS, DJ>;
+  const int bytes = Plan1<S, RY>::kTotal;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
-  kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(L, st, out, maps, cs, kchunk, J[0], J[1], J[2], ss,
-                                                  step, err);
+  kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(L, st, out, maps, cs, kchunk, J[0], J[1], J[2], ss, step, err);
   return cudaGetLastError();
 }
 
 template <class S, int RY>
-static cudaError_t launch1_ry(const PLayout& L, const S& st, const S& out, const TmaMaps& maps,
-                                   const float* const J[3], bool dense_j, const CoefSet& cs,
-                                   const SourceSet& ss, int64_t step, int applications, int kchunk,
-                                   int* err, cudaStream_t stream) {
+static cudaError_t launch1_ry(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
+                              const float* const J[3], bool dense_j, const CoefSet& cs, const SourceSet& ss,
+                              int64_t step, int applications, int kchunk, int* err, cudaStream_t stream) {
+  if (ss.count > kMaxSources) return cudaErrorInvalidValue;
   dim3 grid((L.Ni + 31) / 32, (L.Nj + RY - 1) / RY, (L.Nk + kchunk - 1) / kchunk);
-  const int src = ss.count == 0 ? 0 : (ss.count <= kFastSources ? 1 : 2);
-#define FDTD_F(APPS, DJ, SRC) \
-  return launch1_one<S, RY, APPS, DJ, SRC>(grid, L, st, out, maps, cs, kchunk, J, ss, step, err, stream)
-#define FDTD_FS(APPS, DJ)        \
-  if (src == 0) FDTD_F(APPS, DJ, 0); \
-  if (src == 1) FDTD_F(APPS, DJ, 1); \
-  FDTD_F(APPS, DJ, 2);
+#define FDTD_F(APPS, DJ) return launch1_one<S, RY, APPS, DJ>(grid, L, st, out, maps, cs, kchunk, J, ss, step, err, stream)
   if (applications == 2) {
-    if (dense_j) { FDTD_FS(2, true) } else { FDTD_FS(2, false) }
-  } else {
-    if (dense_j) { FDTD_FS(1, true) } else { FDTD_FS(1, false) }
+    if (dense_j) FDTD_F(2, true);
+    FDTD_F(2, false);
   }
-#undef FDTD_FS
+  if (dense_j) FDTD_F(1, true);
+  FDTD_F(1, false);
 #undef FDTD_F
 }
 
 template <class S>
 cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const void* maps,
-                             const float* const J[3], bool dense_j, const CoefSet& cs,
-                             const SourceSet& ss, int64_t step, int applications,
-                             const FusedConfig& cfg, int* err, cudaStream_t stream) {
-  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 32;
-  const TmaMaps& m = *static_cast<const TmaMaps*>(maps);
+                              const float* const J[3], bool dense_j, const CoefSet& cs, const SourceSet& ss,
+                              int64_t step, int applications, const FusedConfig& cfg, int* err,
+                              cudaStream_t stream) {
+  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 24;
+  const StepMaps& m = *static_cast<const StepMaps*>(maps);
   if (cfg.tile_y == 6)
     return launch1_ry<S, 6>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
   if (cfg.tile_y == 30)
@@ -313,16 +396,14 @@ cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const
   return launch1_ry<S, 14>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
 }
 
-
 template <class S>
 int fused1_box_width() { return Box1<S>::kW; }
 int fused1_lo_box_width() { return Box1<StoreF32C>::kLoW; }
 
-#define FDTD_INSTANTIATE(S)                                                                           \
-  template cudaError_t launch_fused1_f32<S>(const PLayout&, const S&, const S&, const void*,         \
-                                            const float* const[3], bool, const CoefSet&,             \
-                                            const SourceSet&, int64_t, int, const FusedConfig&, int*, \
-                                            cudaStream_t);                                           \
+#define FDTD_INSTANTIATE(S)                                                                              \
+  template cudaError_t launch_fused1_f32<S>(const PLayout&, const S&, const S&, const void*,            \
+                                            const float* const[3], bool, const CoefSet&, const SourceSet&, \
+                                            int64_t, int, const FusedConfig&, int*, cudaStream_t);       \
   template int fused1_box_width<S>();
 FDTD_INSTANTIATE(StoreF32)
 FDTD_INSTANTIATE(StoreF32C)

@@ -36,6 +36,9 @@ struct StoreF32 {
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const { return (double)v[c][idx]; }
   // The value a store followed by a load returns.
   __device__ __forceinline__ Pair quantize(int, Pair p) const { return Pair{p.hi, 0.f}; }
+  // The stored words of a value (quantize(c, p) == decode(c, enc_hi(c, p), enc_lo(p))).
+  __device__ __forceinline__ float enc_hi(int, Pair p) const { return p.hi; }
+  __device__ __forceinline__ uint16_t enc_lo(Pair) const { return 0; }
 };
 
 // FP16 storage with a power-of-two scale per component: stored = field * 2^e.
@@ -58,6 +61,8 @@ struct StoreF16 {
   __device__ __forceinline__ Pair quantize(int c, Pair p) const {
     return Pair{__fmul_rn(__half2float(__float2half_rn(__fmul_rn(p.hi, scale[c]))), inv_scale[c]), 0.f};
   }
+  __device__ __forceinline__ __half enc_hi(int c, Pair p) const { return __float2half_rn(__fmul_rn(p.hi, scale[c])); }
+  __device__ __forceinline__ uint16_t enc_lo(Pair) const { return 0; }
 };
 
 // Compensated storage: FP32 hi word + BF16 lo word.  After every update
@@ -86,6 +91,8 @@ struct StoreF32C {
   __device__ __forceinline__ Pair quantize(int, Pair p) const {
     return Pair{p.hi, bf16_bits_to_float(float_to_bf16_bits(p.lo))};
   }
+  __device__ __forceinline__ float enc_hi(int, Pair p) const { return p.hi; }
+  __device__ __forceinline__ LoT enc_lo(Pair p) const { return float_to_bf16_bits(p.lo); }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const {
     const Pair p = load(c, idx);
     return (double)p.hi + (double)p.lo;

@@ -14,6 +14,14 @@ struct TmaMaps {
   CUtensorMap lo[6];
 };
 
+// Maps of one fused step launch: tile loads from the current copy and tile
+// stores into the second copy (interior-only maps, so stores past the grid's
+// last row or column are clipped by the copy engine).
+struct StepMaps {
+  TmaMaps ld;
+  TmaMaps st;
+};
+
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
@@ -66,5 +74,31 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
       : "memory");
 }
+
+// 3-D tiled TMA store of a box from shared memory to element coordinates
+// (x, y, z) of `map`; completes as part of the thread's bulk async-group.
+// Elements outside the map's extent are not written.
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* src, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+          reinterpret_cast<uint64_t>(map)),
+      "r"(smem_addr(src)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// Waits until every committed bulk store of this thread has read its shared
+// memory source (the buffer may then be rewritten).
+__device__ __forceinline__ void bulk_wait_read_all() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
+// Waits until every committed bulk store of this thread has completed.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// Orders this thread's shared-memory writes before later async-proxy (TMA)
+// reads of them.
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 }  // namespace fdtd

@@ -188,7 +188,7 @@ int fdtd_set_kernel_timing(fdtd_handle* h, int enabled);
  * one sweep per half step.  All give bit-identical results.  The fused
  * launch is shaped by tile_y (interior rows of a tile: 6, 14 or 30; 0 = 14;
  * 30 only with cells_per_thread 1),
- * kchunk (planes per tile; 0 = 32) and cells_per_thread (1: 32-wide tiles,
+ * kchunk (planes per tile; 0 = 24) and cells_per_thread (1: 32-wide tiles,
  * 2: 64-wide tiles with packed two-cell arithmetic; 0 = 1).  The FP64 form
  * always uses the split sweeps. */
 enum fdtd_pipeline { FDTD_PIPELINE_AUTO = 0, FDTD_PIPELINE_SPLIT = 1, FDTD_PIPELINE_FUSED = 2 };

@@ -108,8 +108,11 @@ def _run(p, prec, vals, srcs, steps, pipeline, tile_y=0, kchunk=0, dense_j=None,
 @pytest.mark.parametrize("shape,tile_y,kchunk", [((37, 19, 23), 14, 64), ((1, 1, 1), 14, 64),
                                                  ((64, 28, 16), 14, 8), ((31, 15, 129), 6, 64),
                                                  ((2, 70, 3), 6, 2), ((33, 9, 40), 14, 7),
-                                                 ((96, 42, 5), 6, 3)])
+                                                 ((96, 42, 5), 6, 3), ((70, 61, 9), 30, 4),
+                                                 ((33, 31, 6), 30, 64)])
 def test_fused_step_equals_split_sweeps(prec, shape, tile_y, kchunk, cpt):
+    if tile_y == 30 and cpt == 2:
+        pytest.skip("30-row tiles exist for one cell per thread only")
     """The one-sweep-per-step kernel and the one-sweep-per-half-step kernels
     evaluate the same arithmetic: results are bit-identical, with sources."""
     p = normalised_parameters(*shape)
