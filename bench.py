@@ -18,6 +18,9 @@ update_fields (B/2, E, B/2) over the whole grid.
              duration against the measured HBM copy bandwidth.
   cpu_baseline  the reference's CPU path (restated in oracle/, OpenMP on all
              host cores, the reference driver's loop) on a bounded sample.
+  batched    the batched form on its own workload (256 domains with edges
+             uniform in 32..160 cells, plane wave + one pulse each), CUDA-graph
+             step groups, one persistent launch per fused sweep.
 
 --impl reference runs only that CPU path on the same workload and prints its
 own line.  Under torchrun every rank runs its own replica (no data exchange;
@@ -63,6 +66,10 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=0, help="timed FP64 steps (default max(20, K/5))")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-form leg")
+    ap.add_argument("--batch-only", action="store_true", help="run only the batched-form leg and print it")
+    ap.add_argument("--batch-domains", type=int, default=256)
+    ap.add_argument("--batch-group", type=int, default=50, help="steps per CUDA-graph step group of the batch")
     ap.add_argument("--cpu-worker", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--cpu-steps", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--cpu-warmup", type=int, default=1, help=argparse.SUPPRESS)
@@ -256,6 +263,55 @@ PREC = {"fp32_comp": 2, "fp32": 1, "fp16_scaled": 3}
 BYTES_PER_VALUE = {"fp32_comp": 6, "fp32": 4, "fp16_scaled": 2, "fp64": 8}
 
 
+def run_batched(args, stream, world):
+    """The batched form on its own workload: `--batch-domains` periodic domains
+    with edges uniform in 32..160 cells, a plane wave along a random axis and
+    one Gaussian pulse each (seeded), stepped in CUDA-graph step groups of
+    `--batch-group` steps (one persistent launch per fused sweep)."""
+    import torch
+    from fdtd_method_gb300 import FDTDBatch
+    from fdtd_method_gb300.sources import COURANT_DT, batch_workload
+    G = max(2, args.batch_group // 2 * 2)  # even: replays start from the same copy
+    groups = max(1, args.steps // G)
+    wl = batch_workload(count=args.batch_domains, seed=args.seed, n_steps=500)
+    b = FDTDBatch([w[0] for w in wl], COURANT_DT, PREC[args.precision])
+    b.set_stream(stream.cuda_stream)
+    for q, (p, init, src) in enumerate(wl):
+        for c, v in init.items():
+            b.copy_from_host(q, int(c), v)
+        b.add_source(q, src)
+    cells = sum(w[0].cells for w in wl)
+    b.step(G)  # captures the group's graph and warms up
+    b.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(groups):
+        b.step(G)
+    t1.record(stream)
+    t1.synchronize()
+    b.synchronize()
+    barrier(world)
+    ms = max_over_ranks(world, t0.elapsed_time(t1))
+    steps = groups * G
+    tiles = b.tiles()
+    b.close()
+    bpv = BYTES_PER_VALUE[args.precision]
+    gbs = 12 * bpv * cells * steps / (ms / 1e3) / 1e9
+    hbm, note = measured_peaks()
+    edges = [w[0].Ni for w in wl] + [w[0].Nj for w in wl] + [w[0].Nk for w in wl]
+    return {"value": world * cells * steps / (ms / 1e3) / 1e9, "unit": UNIT, "domains": len(wl), "cells": cells,
+            "edge_min": min(edges), "edge_max": max(edges), "tiles_per_sweep": tiles, "steps": steps,
+            "group_steps": G, "ms_per_step": ms / steps, "launches_per_group": G + 2,
+            "step_roofline": {"algorithmic_bytes_per_cell_step": 12 * bpv, "achieved": gbs, "peak": hbm,
+                              "frac": gbs / hbm, "peak_note": note},
+            "workload": "%d periodic domains, edges uniform in 32..160 cells, plane wave (random axis, mode 1-4) "
+                        "+ 1 Gaussian pulse each (A in [0.5,2], T in [20,60] steps), seed %d, %s"
+                        % (len(wl), args.seed, args.precision)}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -263,6 +319,12 @@ def run_ours(args):
     from fdtd_method_gb300.sources import COURANT_DT
 
     world, rank, local = dist_init(args)
+    if args.batch_only:
+        stream = torch.cuda.Stream()
+        out = run_batched(args, stream, world)
+        if rank == 0:
+            print(json.dumps(out))
+        return
     p, src = workload(args)
     cells = p.cells
     K, W = args.steps, args.warmup
@@ -308,6 +370,12 @@ def run_ours(args):
                  "achieved": step_alg * cells * K / (ms / 1e3) / 1e9, "frac": step_alg * cells * K / (ms / 1e3) / 1e9 / hbm}
     del sim
     torch.cuda.empty_cache()
+
+    # --- batched form ------------------------------------------------------
+    batched = None
+    if not args.no_batch:
+        batched = run_batched(args, stream, world)
+        torch.cuda.empty_cache()
 
     # --- FP64 drop-in ------------------------------------------------------
     K64 = args.fp64_steps or max(20, K // 5)
@@ -398,7 +466,7 @@ def run_ours(args):
                          "roofline": {"bound": "fp64-pipe", "achieved_instr_per_s": v64 * 1e9 * FP64_INSTR_PER_CELL_STEP / world,
                                       "peak_instr_per_s": FP64_PIPE_PEAK,
                                       "frac": v64 * 1e9 * FP64_INSTR_PER_CELL_STEP / world / FP64_PIPE_PEAK}},
-                "accuracy": acc}
+                "accuracy": acc, "batched": batched}
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

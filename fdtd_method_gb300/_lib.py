@@ -88,6 +88,22 @@ SIGNATURES = {
     "fdtd_kernel_times": [_H, _D, ctypes.POINTER(ctypes.c_int64)],
     "fdtd_set_pipeline": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "fdtd_field_sums_noalloc": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p],
+    # batched form
+    "fdtd_batch_create": [ctypes.POINTER(Params), ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(_H)],
+    "fdtd_batch_destroy": [_H],
+    "fdtd_batch_size": [_H, ctypes.POINTER(ctypes.c_int)],
+    "fdtd_batch_domain_params": [_H, ctypes.c_int, ctypes.POINTER(Params)],
+    "fdtd_batch_add_source": [_H, ctypes.c_int, ctypes.POINTER(Source), ctypes.POINTER(ctypes.c_int)],
+    "fdtd_batch_copy_field_to_host": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t],
+    "fdtd_batch_copy_field_from_host": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t],
+    "fdtd_batch_field_sums": [_H, ctypes.c_int, _D],
+    "fdtd_batch_set_fp16_exponents": [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
+    "fdtd_batch_set_config": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+    "fdtd_batch_step": [_H, ctypes.c_int64],
+    "fdtd_batch_get_step": [_H, ctypes.POINTER(ctypes.c_int64)],
+    "fdtd_batch_tiles": [_H, ctypes.POINTER(ctypes.c_int64)],
+    "fdtd_batch_set_stream": [_H, ctypes.c_void_p],
+    "fdtd_batch_synchronize": [_H],
 }
 _RESTYPES = {"fdtd_last_error": ctypes.c_char_p}
 

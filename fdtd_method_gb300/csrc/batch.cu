@@ -1,0 +1,425 @@
+// Batched form of the engine: many independent periodic domains of uneven
+// sizes advanced together.  Each domain is an ordinary handle (storage,
+// sources, host copies and diagnostics are the single-domain code's); the
+// batch adds device tables that describe every domain to one persistent
+// fused-step kernel, and runs a step group as one CUDA graph:
+//
+//   leading B half step of every domain      (one launch, kernels_f32.cu)
+//   n fused sweeps of every domain           (n persistent launches over the
+//                                             tile table, kernels_fused1.cu)
+//   step counter += n                        (one thread)
+//
+// The per-domain tile table lists (domain, bx, by, bz) for every tile of every
+// domain, domain by domain; the persistent CTAs take tiles from it in order.
+// A graph is captured once per (step count, parity) and replayed; the source
+// step index is read from device memory, so a replay needs no new arguments.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "handle.h"
+
+using namespace fdtd;
+
+namespace {
+
+int bfail(int code, const std::string& msg) {
+  set_last_error(msg);
+  return code;
+}
+int bcuda(cudaError_t e, const char* what) {
+  return bfail(e == cudaErrorMemoryAllocation ? FDTD_ERR_OUT_OF_MEMORY : FDTD_ERR_CUDA,
+               std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define FDTD_BCUDA(call, what)                 \
+  do {                                         \
+    cudaError_t e_ = (call);                   \
+    if (e_ != cudaSuccess) return bcuda(e_, what); \
+  } while (0)
+
+__global__ void advance_step(int64_t* step, int64_t n) { *step += n; }
+
+}  // namespace
+
+struct fdtd_batch {
+  std::vector<fdtd_handle*> doms;
+  int precision = 0;
+  Form form = Form::F32C;
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  FusedConfig cfg;
+  bool use_graphs = true;
+  int parity = 0;     // which copy of the tables' two is current
+  int64_t step = 0;   // completed steps
+  bool dirty = true;  // device tables out of date
+  // device tables
+  void* d_doms = nullptr;        // BatchDomain<S>[n]
+  StepMaps* d_maps = nullptr;    // [2 n]
+  int4* d_tiles = nullptr;
+  int n_tiles = 0;
+  int64_t* d_bstart = nullptr;   // [n + 1]
+  int64_t n_bblocks = 0;
+  int* d_counters = nullptr;     // 2 ints, zero between launches
+  int64_t* d_step = nullptr;
+  int* d_err = nullptr;
+  std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
+};
+
+namespace {
+
+void drop_graphs(fdtd_batch* b) {
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.second);
+  b->graphs.clear();
+}
+
+void free_tables(fdtd_batch* b) {
+  drop_graphs(b);
+  cudaFree(b->d_doms);
+  cudaFree(b->d_maps);
+  cudaFree(b->d_tiles);
+  cudaFree(b->d_bstart);
+  b->d_doms = nullptr;
+  b->d_maps = nullptr;
+  b->d_tiles = nullptr;
+  b->d_bstart = nullptr;
+}
+
+template <class S>
+S store_of(const StateView& v);
+template <>
+StoreF32 store_of<StoreF32>(const StateView& v) { return v.s32; }
+template <>
+StoreF32C store_of<StoreF32C>(const StateView& v) { return v.s32c; }
+template <>
+StoreF16 store_of<StoreF16>(const StateView& v) { return v.s16; }
+
+template <class S>
+int upload_domains(fdtd_batch* b) {
+  std::vector<BatchDomain<S>> recs(b->doms.size());
+  for (size_t d = 0; d < b->doms.size(); ++d) {
+    fdtd_handle* h = b->doms[d];
+    BatchDomain<S>& r = recs[d];
+    r.L = h->L;
+    r.s[0] = store_of<S>(h->view());
+    r.s[1] = store_of<S>(h->view_alt());
+    r.cs = h->cs;
+    r.ss = h->source_set();
+  }
+  FDTD_BCUDA(cudaMalloc(&b->d_doms, sizeof(BatchDomain<S>) * recs.size()), "batch domain table");
+  FDTD_BCUDA(cudaMemcpy(b->d_doms, recs.data(), sizeof(BatchDomain<S>) * recs.size(), cudaMemcpyHostToDevice),
+             "upload batch domain table");
+  return FDTD_OK;
+}
+
+// Rebuilds every device table from the domains' current state: copy 0 of
+// each domain is its current copy.
+int build_tables(fdtd_batch* b) {
+  free_tables(b);
+  const int n = (int)b->doms.size();
+  std::vector<StepMaps> maps(2 * n);
+  std::vector<int4> tiles;
+  std::vector<int64_t> bstart(n + 1, 0);
+  for (int d = 0; d < n; ++d) {
+    fdtd_handle* h = b->doms[d];
+    h->fused_cfg = b->cfg;
+    if (int rc = ensure_alt(h)) return rc;
+    maps[2 * d].ld = h->maps_cur;
+    maps[2 * d].st = h->smaps_alt;
+    maps[2 * d + 1].ld = h->maps_alt;
+    maps[2 * d + 1].st = h->smaps_cur;
+    const int tx = (h->g.Ni + 31) / 32, ty = (h->g.Nj + b->cfg.tile_y - 1) / b->cfg.tile_y;
+    const int tz = (h->g.Nk + b->cfg.kchunk - 1) / b->cfg.kchunk;
+    for (int z = 0; z < tz; ++z)
+      for (int y = 0; y < ty; ++y)
+        for (int x = 0; x < tx; ++x) tiles.push_back(make_int4(d, x, y, z));
+    const int64_t nb = (int64_t)((h->g.Ni + 31) / 32) * ((h->g.Nj + 7) / 8) *
+                       ((h->g.Nk + kBatchBChunk - 1) / kBatchBChunk);
+    bstart[d + 1] = bstart[d] + nb;
+  }
+  if (tiles.size() > 0x7fffffff) return bfail(FDTD_ERR_INVALID_ARGUMENT, "batch has too many tiles");
+  int rc = FDTD_OK;
+  switch (b->form) {
+    case Form::F32: rc = upload_domains<StoreF32>(b); break;
+    case Form::F32C: rc = upload_domains<StoreF32C>(b); break;
+    case Form::F16: rc = upload_domains<StoreF16>(b); break;
+    default: rc = bfail(FDTD_ERR_UNSUPPORTED, "batched form needs an FP32-arithmetic precision");
+  }
+  if (rc) return rc;
+  FDTD_BCUDA(cudaMalloc(&b->d_maps, sizeof(StepMaps) * maps.size()), "batch tensor maps");
+  FDTD_BCUDA(cudaMemcpy(b->d_maps, maps.data(), sizeof(StepMaps) * maps.size(), cudaMemcpyHostToDevice),
+             "upload batch tensor maps");
+  FDTD_BCUDA(cudaMalloc(&b->d_tiles, sizeof(int4) * tiles.size()), "batch tile table");
+  FDTD_BCUDA(cudaMemcpy(b->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice),
+             "upload batch tile table");
+  FDTD_BCUDA(cudaMalloc(&b->d_bstart, sizeof(int64_t) * bstart.size()), "batch block table");
+  FDTD_BCUDA(cudaMemcpy(b->d_bstart, bstart.data(), sizeof(int64_t) * bstart.size(), cudaMemcpyHostToDevice),
+             "upload batch block table");
+  FDTD_BCUDA(cudaMemcpy(b->d_step, &b->step, sizeof(int64_t), cudaMemcpyHostToDevice), "batch step counter");
+  b->n_tiles = (int)tiles.size();
+  b->n_bblocks = bstart[n];
+  b->parity = 0;
+  b->dirty = false;
+  return FDTD_OK;
+}
+
+cudaError_t launch_fused_all(fdtd_batch* b, int parity, int apps, int step_off) {
+  switch (b->form) {
+    case Form::F32:
+      return launch_fused1_batch<StoreF32>(b->d_doms, b->d_maps, b->d_tiles, b->n_tiles, parity, apps, b->cfg,
+                                           b->d_step, step_off, b->d_counters, b->d_err, b->stream);
+    case Form::F32C:
+      return launch_fused1_batch<StoreF32C>(b->d_doms, b->d_maps, b->d_tiles, b->n_tiles, parity, apps, b->cfg,
+                                            b->d_step, step_off, b->d_counters, b->d_err, b->stream);
+    case Form::F16:
+      return launch_fused1_batch<StoreF16>(b->d_doms, b->d_maps, b->d_tiles, b->n_tiles, parity, apps, b->cfg,
+                                           b->d_step, step_off, b->d_counters, b->d_err, b->stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_b_all(fdtd_batch* b, int parity) {
+  const int n = (int)b->doms.size();
+  switch (b->form) {
+    case Form::F32: return launch_b_f32_batch<StoreF32>(b->d_doms, b->d_bstart, n, b->n_bblocks, parity, b->stream);
+    case Form::F32C: return launch_b_f32_batch<StoreF32C>(b->d_doms, b->d_bstart, n, b->n_bblocks, parity, b->stream);
+    case Form::F16: return launch_b_f32_batch<StoreF16>(b->d_doms, b->d_bstart, n, b->n_bblocks, parity, b->stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// The launches of `n` steps from copy `parity`.
+cudaError_t enqueue_steps(fdtd_batch* b, int64_t n, int parity) {
+  cudaError_t e = launch_b_all(b, parity);
+  for (int64_t s = 0; s < n && e == cudaSuccess; ++s)
+    e = launch_fused_all(b, parity ^ (int)(s & 1), s + 1 < n ? 2 : 1, (int)s);
+  if (e == cudaSuccess) {
+    advance_step<<<1, 1, 0, b->stream>>>(b->d_step, n);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+int check_batch(fdtd_batch* b) {
+  if (!b) return bfail(FDTD_ERR_INVALID_ARGUMENT, "null batch");
+  return FDTD_OK;
+}
+
+int check_domain(fdtd_batch* b, int d) {
+  if (int rc = check_batch(b)) return rc;
+  if (d < 0 || d >= (int)b->doms.size()) return bfail(FDTD_ERR_INVALID_ARGUMENT, "domain index out of range");
+  return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdtd_batch_create(const fdtd_params* params, int n, double dt, int precision, fdtd_batch** out) {
+  if (!params || !out) return bfail(FDTD_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (n <= 0) return bfail(FDTD_ERR_INVALID_ARGUMENT, "a batch needs at least one domain");
+  if (precision != FDTD_PRECISION_FP32 && precision != FDTD_PRECISION_FP32_COMP &&
+      precision != FDTD_PRECISION_FP16_SCALED)
+    return bfail(FDTD_ERR_UNSUPPORTED, "the batched form runs FP32, FP32_COMP or FP16_SCALED");
+  fdtd_batch* b = new fdtd_batch();
+  b->precision = precision;
+  b->form = (Form)precision;
+  cudaGetDevice(&b->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete b;
+    return bcuda(e, "batch stream");
+  }
+  b->stream = b->own_stream;
+  int rc = FDTD_OK;
+  for (int d = 0; d < n && rc == FDTD_OK; ++d) {
+    fdtd_handle* h = nullptr;
+    rc = fdtd_create(&params[d], dt, precision, &h);
+    if (rc == FDTD_OK) {
+      b->doms.push_back(h);
+      rc = fdtd_set_stream(h, b->stream);
+    }
+  }
+  if (rc == FDTD_OK) {
+    e = cudaMalloc(&b->d_counters, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(b->d_counters, 0, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_step, sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(b->d_err, 0, sizeof(int));
+    if (e != cudaSuccess) rc = bcuda(e, "batch set-up");
+  }
+  if (rc != FDTD_OK) {
+    std::string msg = fdtd_last_error();
+    fdtd_batch_destroy(b);
+    return bfail(rc, msg);
+  }
+  *out = b;
+  return FDTD_OK;
+}
+
+int fdtd_batch_destroy(fdtd_batch* b) {
+  if (!b) return FDTD_OK;
+  DeviceGuard dg(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  free_tables(b);
+  for (fdtd_handle* h : b->doms) fdtd_destroy(h);
+  cudaFree(b->d_counters);
+  cudaFree(b->d_step);
+  cudaFree(b->d_err);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  delete b;
+  return FDTD_OK;
+}
+
+int fdtd_batch_size(fdtd_batch* b, int* n) {
+  if (int rc = check_batch(b)) return rc;
+  if (!n) return bfail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  *n = (int)b->doms.size();
+  return FDTD_OK;
+}
+
+int fdtd_batch_domain_params(fdtd_batch* b, int d, fdtd_params* params) {
+  if (int rc = check_domain(b, d)) return rc;
+  if (!params) return bfail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  *params = b->doms[d]->p;
+  return FDTD_OK;
+}
+
+int fdtd_batch_copy_field_to_host(fdtd_batch* b, int d, int comp, double* host, size_t n) {
+  if (int rc = check_domain(b, d)) return rc;
+  if (comp < FDTD_EX || comp > FDTD_BZ)
+    return bfail(FDTD_ERR_LOGIC, "ERROR: Invalid field component");
+  DeviceGuard dg(b->device);
+  return fdtd_copy_field_to_host(b->doms[d], comp, host, n);
+}
+
+int fdtd_batch_copy_field_from_host(fdtd_batch* b, int d, int comp, const double* host, size_t n) {
+  if (int rc = check_domain(b, d)) return rc;
+  if (comp < FDTD_EX || comp > FDTD_BZ)
+    return bfail(FDTD_ERR_LOGIC, "ERROR: Invalid field component");
+  DeviceGuard dg(b->device);
+  return fdtd_copy_field_from_host(b->doms[d], comp, host, n);
+}
+
+int fdtd_batch_field_sums(fdtd_batch* b, int d, double out[FDTD_DIAG_COUNT]) {
+  if (int rc = check_domain(b, d)) return rc;
+  DeviceGuard dg(b->device);
+  return fdtd_field_sums(b->doms[d], out);
+}
+
+int fdtd_batch_set_fp16_exponents(fdtd_batch* b, int d, const int exponents[6]) {
+  if (int rc = check_domain(b, d)) return rc;
+  const int rc = fdtd_set_fp16_exponents(b->doms[d], exponents);
+  if (rc == FDTD_OK) b->dirty = true;
+  return rc;
+}
+
+int fdtd_batch_add_source(fdtd_batch* b, int d, const fdtd_source* src, int* index) {
+  if (int rc = check_domain(b, d)) return rc;
+  DeviceGuard dg(b->device);
+  const int rc = fdtd_add_source(b->doms[d], src, index);
+  if (rc == FDTD_OK) b->dirty = true;
+  return rc;
+}
+
+int fdtd_batch_set_config(fdtd_batch* b, int tile_y, int kchunk, int use_graphs) {
+  if (int rc = check_batch(b)) return rc;
+  if (tile_y != 0 && tile_y != 6 && tile_y != 14 && tile_y != 30)
+    return bfail(FDTD_ERR_INVALID_ARGUMENT, "tile_y must be 0 (default), 6, 14 or 30");
+  if (kchunk < 0) return bfail(FDTD_ERR_INVALID_ARGUMENT, "kchunk must be >= 0");
+  b->cfg.tile_y = tile_y ? tile_y : 14;
+  b->cfg.kchunk = kchunk ? kchunk : 24;
+  b->cfg.cells_per_thread = 1;
+  b->use_graphs = use_graphs != 0;
+  b->dirty = true;
+  return FDTD_OK;
+}
+
+int fdtd_batch_step(fdtd_batch* b, int64_t n) {
+  if (int rc = check_batch(b)) return rc;
+  if (n < 0) return bfail(FDTD_ERR_INVALID_ARGUMENT, "negative step count");
+  if (n == 0) return FDTD_OK;
+  if (n > 0x7fffffff) return bfail(FDTD_ERR_INVALID_ARGUMENT, "step count too large for one call");
+  DeviceGuard dg(b->device);
+  if (b->dirty)
+    if (int rc = build_tables(b)) return rc;
+  if (b->use_graphs) {
+    const auto key = std::make_pair(n, b->parity);
+    auto it = b->graphs.find(key);
+    if (it == b->graphs.end()) {
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      FDTD_BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed), "graph capture");
+      cudaError_t e = enqueue_steps(b, n, b->parity);
+      cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+      if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return bcuda(e, "batch step capture");
+      }
+      if (e2 != cudaSuccess) return bcuda(e2, "graph capture");
+      e = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return bcuda(e, "graph instantiation");
+      it = b->graphs.emplace(key, ge).first;
+    }
+    FDTD_BCUDA(cudaGraphLaunch(it->second, b->stream), "batch step graph launch");
+  } else {
+    FDTD_BCUDA(enqueue_steps(b, n, b->parity), "batch step launch");
+  }
+  if (n & 1) {
+    b->parity ^= 1;
+    for (fdtd_handle* h : b->doms) swap_copies(h);
+  }
+  b->step += n;
+  for (fdtd_handle* h : b->doms) h->host_step = b->step;
+  return FDTD_OK;
+}
+
+int fdtd_batch_synchronize(fdtd_batch* b) {
+  if (int rc = check_batch(b)) return rc;
+  DeviceGuard dg(b->device);
+  FDTD_BCUDA(cudaStreamSynchronize(b->stream), "batch synchronize");
+  int err = 0;
+  FDTD_BCUDA(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost), "batch status");
+  if (err) {
+    cudaMemset(b->d_err, 0, sizeof(int));
+    return bfail(FDTD_ERR_TIMEOUT, "a bounded device wait of the batched step gave up");
+  }
+  return FDTD_OK;
+}
+
+int fdtd_batch_set_stream(fdtd_batch* b, void* stream) {
+  if (int rc = check_batch(b)) return rc;
+  DeviceGuard dg(b->device);
+  FDTD_BCUDA(cudaStreamSynchronize(b->stream), "batch stream switch");
+  b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+  for (fdtd_handle* h : b->doms)
+    if (int rc = fdtd_set_stream(h, b->stream)) return rc;
+  drop_graphs(b);
+  return FDTD_OK;
+}
+
+int fdtd_batch_get_step(fdtd_batch* b, int64_t* step) {
+  if (int rc = check_batch(b)) return rc;
+  if (!step) return bfail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  *step = b->step;
+  return FDTD_OK;
+}
+
+int fdtd_batch_tiles(fdtd_batch* b, int64_t* tiles) {
+  if (int rc = check_batch(b)) return rc;
+  if (!tiles) return bfail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  DeviceGuard dg(b->device);
+  if (b->dirty)
+    if (int rc = build_tables(b)) return rc;
+  *tiles = b->n_tiles;
+  return FDTD_OK;
+}
+
+}  // extern "C"

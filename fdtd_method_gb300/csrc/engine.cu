@@ -10,8 +10,7 @@
 #include <vector>
 
 #include "../../include/fdtd_gb300.h"
-#include "engine_internal.h"
-#include "tma.cuh"
+#include "handle.h"
 
 using namespace fdtd;
 
@@ -41,11 +40,6 @@ constexpr double kPi = 3.14159265358;
 constexpr int64_t kStagingElems = int64_t(1) << 24;  // 16 Mi doubles = 128 MiB
 constexpr int kMaxDiagBlocks = 152 * 8;
 
-struct HostSource {
-  fdtd_source s;  // table pointers are not kept
-  std::vector<double> gx, gy, gz, amp;
-};
-
 Coef split_coef(double c) {
   const float h = (float)c;
   return Coef{h, (float)(c - (double)h)};
@@ -57,101 +51,6 @@ namespace fdtd {
 // Lets other translation units of the library report through fdtd_last_error().
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace fdtd
-
-struct fdtd_handle {
-  fdtd_params p{};
-  double dt = 0;
-  int precision = 0;
-  Form form = Form::F64;
-  Grid g{};
-  int device = 0;
-  // {cEx, cEy, cEz, cBx, cBy, cBz, cJ}, src/FDTD_kokkos/FDTD_kokkos.cpp:45-55
-  double coef[7] = {0, 0, 0, 0, 0, 0, 0};
-  CoefSet cs{};
-  cudaStream_t own_stream = nullptr;
-  cudaStream_t stream = nullptr;
-
-  // Storage.  FP64: field[0..8] are double arrays (E, B, J).  Other forms:
-  // field[0..5] hold the E/B words of the form, lo[0..5] the compensation
-  // words (FP32_COMP), jf[0..2] FP32 current arrays (allocated on first use).
-  void* field[9] = {nullptr};
-  LoT* lo[6] = {nullptr};
-  // Second copy of E/B (and lo) that the fused sweep writes into; swapped
-  // with field/lo after every fused step.
-  void* alt_field[6] = {nullptr};
-  LoT* alt_lo[6] = {nullptr};
-  float* jf[3] = {nullptr};
-  bool dense_j = false;  // the E update reads the dense J arrays
-  int fp16_exp[6] = {0, 0, 0, 0, 0, 0};
-
-  // Sources.
-  std::vector<HostSource> sources;
-  DevSource* d_src = nullptr;
-  double* d_tables = nullptr;
-  float* d_tables_f = nullptr;  // FP32 hi tables, then FP32 lo tables
-  int64_t tables_lo_off = 0;
-  int64_t host_step = 0;  // completed update_fields steps
-
-  // Step pipeline of the FP32-arithmetic forms (FP64 always uses the split
-  // sweeps, whose FP64 instruction count is the smallest).
-  int pipeline = FDTD_PIPELINE_AUTO;
-  FusedConfig fused_cfg;
-  PLayout L{};  // padded layout of the FP32-arithmetic forms
-  // TMA maps of the current and the second copy (rebuilt when the tile
-  // shape changes; swapped with the copies).
-  TmaMaps maps_cur;
-  TmaMaps maps_alt;
-  // Store maps (grid cells only) of both copies, for the one-cell-per-thread
-  // fused kernel.
-  TmaMaps smaps_cur;
-  TmaMaps smaps_alt;
-  int maps_tile_y = 0;
-  int* d_err = nullptr;  // device status word (bounded waits that gave up)
-
-  // Scratch.
-  double* d_staging = nullptr;
-  double* d_partials = nullptr;
-  double* d_diag_out = nullptr;
-
-  std::vector<void*> allocations;
-
-  // Kernel timing: event pairs recorded around launches while enabled.
-  struct TimedLaunch {
-    cudaEvent_t start, stop;
-    int kind;
-  };
-  bool timing = false;
-  std::vector<TimedLaunch> timed;
-  std::vector<cudaEvent_t> event_pool;
-
-  StateView make_view(void* const* f, LoT* const* l) const {
-    StateView v{};
-    v.form = form;
-    v.g = g;
-    v.L = L;
-    for (int c = 0; c < 6; ++c) v.f64[c] = (form == Form::F64) ? (double*)f[c] : nullptr;
-    for (int c = 0; c < 6; ++c) {
-      v.s32.v[c] = (float*)f[c];
-      v.s32c.hi[c] = (float*)f[c];
-      v.s32c.lo[c] = l[c];
-      v.s16.v[c] = (__half*)f[c];
-      v.s16.scale[c] = std::ldexp(1.0f, fp16_exp[c]);
-      v.s16.inv_scale[c] = std::ldexp(1.0f, -fp16_exp[c]);
-    }
-    return v;
-  }
-  StateView view() const { return make_view(field, lo); }
-  StateView view_alt() const { return make_view(alt_field, alt_lo); }
-  SourceSet source_set() const {
-    SourceSet ss{};
-    ss.count = (int)sources.size();
-    ss.src = d_src;
-    ss.tables = d_tables;
-    ss.tables_f = d_tables_f;
-    ss.lo_off = tables_lo_off;
-    return ss;
-  }
-};
 
 namespace {
 
@@ -184,8 +83,11 @@ size_t elem_bytes(Form f) {
 }
 
 int ensure_staging(fdtd_handle* h) {
+  // Transfers move at most kStagingElems values per chunk, and never more
+  // than the grid holds (small grids, as in a batch, get small buffers).
   if (!h->d_staging)
-    FDTD_CUDA(dev_alloc(h, (void**)&h->d_staging, sizeof(double) * kStagingElems), "staging buffer");
+    FDTD_CUDA(dev_alloc(h, (void**)&h->d_staging, sizeof(double) * std::min<int64_t>(kStagingElems, h->g.cells)),
+              "staging buffer");
   return FDTD_OK;
 }
 
@@ -235,17 +137,6 @@ int upload_sources(fdtd_handle* h) {
   FDTD_CUDA(cudaStreamSynchronize(h->stream), "source upload");
   return FDTD_OK;
 }
-
-struct DeviceGuard {
-  int prev = 0;
-  bool ok = false;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess) ok = true;
-  }
-  ~DeviceGuard() {
-    if (ok) cudaSetDevice(prev);
-  }
-};
 
 cudaEvent_t take_event(fdtd_handle* h) {
   if (!h->event_pool.empty()) {
@@ -326,6 +217,50 @@ int run_e(fdtd_handle* h, int64_t step) {
   return FDTD_OK;
 }
 
+// E step `step` followed by `apps` B half steps, in one sweep from the
+// current copy into the second one, which then becomes current.
+int run_fused(fdtd_handle* h, int64_t step, int apps) {
+  if (int rc = ensure_alt(h)) return rc;
+  LaunchTimer lt(h, FDTD_KERNEL_FUSED);
+  SourceSet ss = h->source_set();
+  StateView v = h->view();
+  StateView w = h->view_alt();
+  const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
+  const bool dj = h->dense_j && h->jf[0];
+  const FusedConfig& cf = h->fused_cfg;
+  StepMaps sm;
+  sm.ld = h->maps_cur;
+  sm.st = h->smaps_alt;
+  const void* m = cf.cells_per_thread == 2 ? static_cast<const void*>(&h->maps_cur) : static_cast<const void*>(&sm);
+  cudaError_t e = cudaSuccess;
+#define FDTD_FUSED_LAUNCH(FN)                                                                                  \
+  switch (h->form) {                                                                                         \
+    case Form::F32: e = FN(h->L, v.s32, w.s32, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;    \
+    case Form::F32C: e = FN(h->L, v.s32c, w.s32c, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break; \
+    case Form::F16: e = FN(h->L, v.s16, w.s16, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;    \
+    default: e = cudaErrorInvalidValue; break;                                                               \
+  }
+  if (cf.cells_per_thread == 2) {
+    FDTD_FUSED_LAUNCH(launch_fused_f32)
+  } else {
+    FDTD_FUSED_LAUNCH(launch_fused1_f32)
+  }
+#undef FDTD_FUSED_LAUNCH
+  lt.done();
+  if (e != cudaSuccess) return cuda_fail(e, "fused step launch");
+  swap_copies(h);
+  return FDTD_OK;
+}
+
+int check_handle(fdtd_handle* h) {
+  if (!h) return fail(FDTD_ERR_INVALID_ARGUMENT, "null handle");
+  return FDTD_OK;
+}
+
+}  // namespace
+
+namespace fdtd {
+
 // Second copy of the E/B storage for the fused sweep (allocated on first
 // use) and the TMA maps of both copies for the current tile shape.
 int ensure_alt(fdtd_handle* h) {
@@ -361,52 +296,16 @@ int ensure_alt(fdtd_handle* h) {
   return FDTD_OK;
 }
 
-// E step `step` followed by `apps` B half steps, in one sweep from the
-// current copy into the second one, which then becomes current.
-int run_fused(fdtd_handle* h, int64_t step, int apps) {
-  if (int rc = ensure_alt(h)) return rc;
-  LaunchTimer lt(h, FDTD_KERNEL_FUSED);
-  SourceSet ss = h->source_set();
-  StateView v = h->view();
-  StateView w = h->view_alt();
-  const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
-  const bool dj = h->dense_j && h->jf[0];
-  const FusedConfig& cf = h->fused_cfg;
-  StepMaps sm;
-  sm.ld = h->maps_cur;
-  sm.st = h->smaps_alt;
-  const void* m = cf.cells_per_thread == 2 ? static_cast<const void*>(&h->maps_cur) : static_cast<const void*>(&sm);
-  cudaError_t e = cudaSuccess;
-#define FDTD_FUSED_LAUNCH(FN)                                                                                  \
-  switch (h->form) {                                                                                         \
-    case Form::F32: e = FN(h->L, v.s32, w.s32, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;    \
-    case Form::F32C: e = FN(h->L, v.s32c, w.s32c, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break; \
-    case Form::F16: e = FN(h->L, v.s16, w.s16, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;    \
-    default: e = cudaErrorInvalidValue; break;                                                               \
-  }
-  if (cf.cells_per_thread == 2) {
-    FDTD_FUSED_LAUNCH(launch_fused_f32)
-  } else {
-    FDTD_FUSED_LAUNCH(launch_fused1_f32)
-  }
-#undef FDTD_FUSED_LAUNCH
-  lt.done();
-  if (e != cudaSuccess) return cuda_fail(e, "fused step launch");
+void swap_copies(fdtd_handle* h) {
   for (int c = 0; c < 6; ++c) {
     std::swap(h->field[c], h->alt_field[c]);
     std::swap(h->lo[c], h->alt_lo[c]);
   }
   std::swap(h->maps_cur, h->maps_alt);
   std::swap(h->smaps_cur, h->smaps_alt);
-  return FDTD_OK;
 }
 
-int check_handle(fdtd_handle* h) {
-  if (!h) return fail(FDTD_ERR_INVALID_ARGUMENT, "null handle");
-  return FDTD_OK;
-}
-
-}  // namespace
+}  // namespace fdtd
 
 extern "C" {
 

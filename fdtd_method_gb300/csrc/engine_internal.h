@@ -65,6 +65,36 @@ template <class S>
 int fused1_box_width();
 int fused1_lo_box_width();
 
+// Batched form: one record per domain in device memory (its layout, its two
+// state copies, coefficients and sources).
+struct StepMaps;
+template <class S>
+struct BatchDomain {
+  PLayout L;
+  S s[2];
+  CoefSet cs;
+  SourceSet ss;
+};
+
+// kernels_fused1.cu: one fused sweep over every tile of every domain, as one
+// persistent launch.  `doms` is a BatchDomain<S>[n], `maps` has two StepMaps
+// per domain (index 2 d + parity: loads of copy parity, stores into the
+// other), `tiles` the (domain, bx, by, bz) table; the step index is
+// *step_base + step_off; counters (2 ints, zero before the first launch) are
+// left at zero.
+template <class S>
+cudaError_t launch_fused1_batch(const void* doms, const StepMaps* maps, const int4* tiles, int n_tiles, int parity,
+                                int applications, const FusedConfig& cfg, const int64_t* step_base, int step_off,
+                                int* counters, int* err, cudaStream_t stream);
+
+// kernels_f32.cu: the leading B half step of every domain in place on copy
+// `parity`, as one launch of 32 x 8 blocks marching kBatchBChunk planes;
+// block_start[d] is the first block of domain d (n_dom + 1 entries).
+constexpr int kBatchBChunk = 16;
+template <class S>
+cudaError_t launch_b_f32_batch(const void* doms, const int64_t* block_start, int n_dom, int64_t n_blocks,
+                               int parity, cudaStream_t stream);
+
 // tma_maps.cu: tensor maps of the six hi arrays (and six lo arrays of the
 // compensated form) for a fused tile of `tile_y` interior rows.
 enum class HiType { F32, F16 };

@@ -1,0 +1,141 @@
+// Internal: the state behind an fdtd_handle, shared by the C-ABI layer
+// (engine.cu) and the batched form (batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/fdtd_gb300.h"
+#include "engine_internal.h"
+#include "tma.cuh"
+
+namespace fdtd {
+
+struct HostSource {
+  fdtd_source s;  // table pointers are not kept
+  std::vector<double> gx, gy, gz, amp;
+};
+
+// Reports through fdtd_last_error() (defined in engine.cu).
+void set_last_error(const std::string& msg);
+
+struct DeviceGuard {
+  int prev = 0;
+  bool ok = false;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess) ok = true;
+  }
+  ~DeviceGuard() {
+    if (ok) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace fdtd
+
+using namespace fdtd;
+
+struct fdtd_handle {
+  fdtd_params p{};
+  double dt = 0;
+  int precision = 0;
+  Form form = Form::F64;
+  Grid g{};
+  int device = 0;
+  // {cEx, cEy, cEz, cBx, cBy, cBz, cJ}, src/FDTD_kokkos/FDTD_kokkos.cpp:45-55
+  double coef[7] = {0, 0, 0, 0, 0, 0, 0};
+  CoefSet cs{};
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+
+  // Storage.  FP64: field[0..8] are double arrays (E, B, J).  Other forms:
+  // field[0..5] hold the E/B words of the form, lo[0..5] the compensation
+  // words (FP32_COMP), jf[0..2] FP32 current arrays (allocated on first use).
+  void* field[9] = {nullptr};
+  LoT* lo[6] = {nullptr};
+  // Second copy of E/B (and lo) that the fused sweep writes into; swapped
+  // with field/lo after every fused step.
+  void* alt_field[6] = {nullptr};
+  LoT* alt_lo[6] = {nullptr};
+  float* jf[3] = {nullptr};
+  bool dense_j = false;  // the E update reads the dense J arrays
+  int fp16_exp[6] = {0, 0, 0, 0, 0, 0};
+
+  // Sources.
+  std::vector<HostSource> sources;
+  DevSource* d_src = nullptr;
+  double* d_tables = nullptr;
+  float* d_tables_f = nullptr;  // FP32 hi tables, then FP32 lo tables
+  int64_t tables_lo_off = 0;
+  int64_t host_step = 0;  // completed update_fields steps
+
+  // Step pipeline of the FP32-arithmetic forms (FP64 always uses the split
+  // sweeps, whose FP64 instruction count is the smallest).
+  int pipeline = FDTD_PIPELINE_AUTO;
+  FusedConfig fused_cfg;
+  PLayout L{};  // padded layout of the FP32-arithmetic forms
+  // TMA maps of the current and the second copy (rebuilt when the tile
+  // shape changes; swapped with the copies).
+  TmaMaps maps_cur;
+  TmaMaps maps_alt;
+  // Store maps (grid cells only) of both copies, for the one-cell-per-thread
+  // fused kernel.
+  TmaMaps smaps_cur;
+  TmaMaps smaps_alt;
+  int maps_tile_y = 0;
+  int* d_err = nullptr;  // device status word (bounded waits that gave up)
+
+  // Scratch.
+  double* d_staging = nullptr;
+  double* d_partials = nullptr;
+  double* d_diag_out = nullptr;
+
+  std::vector<void*> allocations;
+
+  // Kernel timing: event pairs recorded around launches while enabled.
+  struct TimedLaunch {
+    cudaEvent_t start, stop;
+    int kind;
+  };
+  bool timing = false;
+  std::vector<TimedLaunch> timed;
+  std::vector<cudaEvent_t> event_pool;
+
+  StateView make_view(void* const* f, LoT* const* l) const {
+    StateView v{};
+    v.form = form;
+    v.g = g;
+    v.L = L;
+    for (int c = 0; c < 6; ++c) v.f64[c] = (form == Form::F64) ? (double*)f[c] : nullptr;
+    for (int c = 0; c < 6; ++c) {
+      v.s32.v[c] = (float*)f[c];
+      v.s32c.hi[c] = (float*)f[c];
+      v.s32c.lo[c] = l[c];
+      v.s16.v[c] = (__half*)f[c];
+      v.s16.scale[c] = std::ldexp(1.0f, fp16_exp[c]);
+      v.s16.inv_scale[c] = std::ldexp(1.0f, -fp16_exp[c]);
+    }
+    return v;
+  }
+  StateView view() const { return make_view(field, lo); }
+  StateView view_alt() const { return make_view(alt_field, alt_lo); }
+  SourceSet source_set() const {
+    SourceSet ss{};
+    ss.count = (int)sources.size();
+    ss.src = d_src;
+    ss.tables = d_tables;
+    ss.tables_f = d_tables_f;
+    ss.lo_off = tables_lo_off;
+    return ss;
+  }
+};
+
+namespace fdtd {
+// Allocates the second copy of the E/B storage (first use) and builds the
+// TMA maps of both copies for the handle's tile shape.
+int ensure_alt(fdtd_handle* h);
+// Swaps the current and the second copy (after a fused sweep).
+void swap_copies(fdtd_handle* h);
+}  // namespace fdtd

@@ -14,11 +14,10 @@
 
 namespace fdtd {
 
+// B update of column (i, j), planes k0 .. k0+kchunk-1.
 template <class S, class A, int kApplications>
-__global__ void __launch_bounds__(256) b_sweep(PLayout L, S st, CoefSet cs, int kchunk) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k0 = blockIdx.z * kchunk;
+__device__ __forceinline__ void b_column(const PLayout& L, const S& st, const CoefSet& cs, int i, int j, int k0,
+                                         int kchunk) {
   if (i >= L.Ni || j >= L.Nj || k0 >= L.Nk) return;
   const int k1 = min(k0 + kchunk, L.Nk);
   const Coef cx = cs.cb[0], cy = cs.cb[1], cz = cs.cb[2];
@@ -46,6 +45,32 @@ __global__ void __launch_bounds__(256) b_sweep(PLayout L, S st, CoefSet cs, int 
     ex = ex_kn;
     ey = ey_kn;
   }
+}
+
+template <class S, class A, int kApplications>
+__global__ void __launch_bounds__(256) b_sweep(PLayout L, S st, CoefSet cs, int kchunk) {
+  b_column<S, A, kApplications>(L, st, cs, blockIdx.x * blockDim.x + threadIdx.x,
+                                blockIdx.y * blockDim.y + threadIdx.y, blockIdx.z * kchunk, kchunk);
+}
+
+// The leading B half step of every domain of a batch: block b belongs to the
+// domain d with block_start[d] <= b < block_start[d+1].
+template <class S, class A>
+__global__ void __launch_bounds__(256) b_sweep_batch(const BatchDomain<S>* __restrict__ doms,
+                                                     const int64_t* __restrict__ block_start, int n_dom, int parity) {
+  const int64_t b = blockIdx.x;
+  int lo = 0, hi = n_dom;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (block_start[mid] <= b) lo = mid;
+    else hi = mid;
+  }
+  const BatchDomain<S>& d = doms[lo];
+  const int64_t local = b - block_start[lo];
+  const int nbx = (d.L.Ni + 31) / 32, nby = (d.L.Nj + 7) / 8;
+  const int bx = (int)(local % nbx), by = (int)((local / nbx) % nby), bz = (int)(local / ((int64_t)nbx * nby));
+  b_column<S, A, 1>(d.L, d.s[parity], d.cs, bx * 32 + threadIdx.x, by * 8 + threadIdx.y, bz * kBatchBChunk,
+                    kBatchBChunk);
 }
 
 template <class S, class A, bool kDenseJ, bool kSources>
@@ -76,20 +101,18 @@ __global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __r
     Pair ty = A::curl(cz, bx, bx_kp, cx, bz, st.load(5, col_ip + base));
     Pair tz = A::curl(cx, by, st.load(4, col_ip + base), cy, bx, st.load(3, col_jp + base));
     T jv[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
-    bool has_j = false;
+    unsigned has = 0;  // J components that carry current here
     if (kDenseJ) {
       const int64_t d = dcol + (int64_t)k * dplane;
       jv[0] = A::cur_dense(Jx[d]);
       jv[1] = A::cur_dense(Jy[d]);
       jv[2] = A::cur_dense(Jz[d]);
-      has_j = true;
+      has = 7u;
     }
-    if (kSources) has_j |= source_sum<A>(ss, step, i, j, k, L, jv);
-    if (has_j) {
-      tx = A::add(tx, A::cur_term(cs.cj, jv[0]));
-      ty = A::add(ty, A::cur_term(cs.cj, jv[1]));
-      tz = A::add(tz, A::cur_term(cs.cj, jv[2]));
-    }
+    if (kSources) has |= source_sum<A>(ss, step, i, j, k, L, jv);
+    if (has & 1u) tx = A::add(tx, A::cur_term(cs.cj, jv[0]));
+    if (has & 2u) ty = A::add(ty, A::cur_term(cs.cj, jv[1]));
+    if (has & 4u) tz = A::add(tz, A::cur_term(cs.cj, jv[2]));
     store_with_ghosts(st, L, 0, i, j, k, A::acc(st.load(0, col + base), tx));
     store_with_ghosts(st, L, 1, i, j, k, A::acc(st.load(1, col + base), ty));
     store_with_ghosts(st, L, 2, i, j, k, A::acc(st.load(2, col + base), tz));
@@ -136,8 +159,20 @@ cudaError_t launch_e_f32(const PLayout& L, const S& st, const float* const J[3],
   return cudaGetLastError();
 }
 
+template <class S>
+cudaError_t launch_b_f32_batch(const void* doms, const int64_t* block_start, int n_dom, int64_t n_blocks,
+                               int parity, cudaStream_t stream) {
+  using A = typename ArithOf<S>::type;
+  if (n_blocks <= 0) return cudaSuccess;
+  if (n_blocks > 0x7fffffff) return cudaErrorInvalidValue;
+  b_sweep_batch<S, A><<<(unsigned)n_blocks, dim3(32, 8), 0, stream>>>(static_cast<const BatchDomain<S>*>(doms),
+                                                                     block_start, n_dom, parity);
+  return cudaGetLastError();
+}
+
 #define FDTD_INSTANTIATE(S)                                                                            \
   template cudaError_t launch_b_f32<S>(const PLayout&, const S&, const CoefSet&, int, cudaStream_t); \
+  template cudaError_t launch_b_f32_batch<S>(const void*, const int64_t*, int, int64_t, int, cudaStream_t); \
   template cudaError_t launch_e_f32<S>(const PLayout&, const S&, const float* const[3], bool,         \
                                        const CoefSet&, const SourceSet&, int64_t, cudaStream_t);
 FDTD_INSTANTIATE(StoreF32)

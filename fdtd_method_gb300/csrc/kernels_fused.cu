@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(32 * (RY + 2))
       if (kDenseJ || kSrc != 0) {
         T j0[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
         T j1[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
-        bool h0 = false, h1 = false;
+        unsigned h0 = 0, h1 = 0;
         if (kDenseJ) {
           const int64_t plane = (int64_t)kk * L.Ni * L.Nj, row = (int64_t)yl * L.Ni;
           const int64_t d0 = xl0 + row + plane, d1 = xl1 + row + plane;
@@ -235,13 +235,13 @@ __global__ void __launch_bounds__(32 * (RY + 2))
             j0[0] = A::cur_dense(Jx[d0]);
             j0[1] = A::cur_dense(Jy[d0]);
             j0[2] = A::cur_dense(Jz[d0]);
-            h0 = true;
+            h0 = 7u;
           }
           if (e1) {
             j1[0] = A::cur_dense(Jx[d1]);
             j1[1] = A::cur_dense(Jy[d1]);
             j1[2] = A::cur_dense(Jz[d1]);
-            h1 = true;
+            h1 = 7u;
           }
         }
         if (kSrc == 1) {
@@ -258,11 +258,11 @@ __global__ void __launch_bounds__(32 * (RY + 2))
           for (int c = 0; c < 3; ++c) {
             const Pair t0 = A::cur_term(cs.cj, j0[c]), t1 = A::cur_term(cs.cj, j1[c]);
             const P2 s = A2::add(*q[c], make_p2(t0, t1));
-            if (h0) {
+            if (h0 >> c & 1u) {
               q[c]->hi.x = s.hi.x;
               q[c]->lo.x = s.lo.x;
             }
-            if (h1) {
+            if (h1 >> c & 1u) {
               q[c]->hi.y = s.hi.y;
               q[c]->lo.y = s.lo.y;
             }

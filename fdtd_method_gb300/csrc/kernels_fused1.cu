@@ -53,6 +53,11 @@ template <> struct Box1<StoreF16> { static constexpr int kW = 48, kOff = 8, kLoW
 
 constexpr int round128(int b) { return (b + 127) / 128 * 128; }
 
+// CTAs per SM the register budget is sized for (30-row tiles: one
+// 1024-thread CTA; otherwise two).
+template <int RY>
+constexpr int kMinCtas1 = RY == 30 ? 1 : 2;
+
 // Shared-memory plan (byte offsets).
 template <class S, int RY>
 struct Plan1 {
@@ -95,21 +100,30 @@ __device__ __forceinline__ bool window_meets(int o, int n, int N, int a, int m) 
   return s < n || s + m > N;
 }
 
-template <class S, class A, int RY, int kApps, bool kDenseJ>
-__global__ void __launch_bounds__(32 * (RY + 2))
-    fused1(PLayout L, S st, S out, const __grid_constant__ StepMaps maps, CoefSet cs, int kchunk,
-           const float* __restrict__ Jx, const float* __restrict__ Jy, const float* __restrict__ Jz,
-           SourceSet ss, int64_t step, int* err) {
+// One tile: columns bx*32 .., rows by*RY .., planes bz*kchunk .. of one
+// domain, with the CTA's shared memory `smem` (barriers initialised).  `ring`
+// counts the ring fills the CTA has consumed so far (it carries the slot and
+// phase from tile to tile); on return the leader has waited for the tile's
+// stores to read their staging, and the caller synchronises before the next
+// tile writes staging again.
+//
+// fused1_tile lists the sources that can reach the tile, then runs the plane
+// loop, fused1_planes, compiled with (kSrc) or without source evaluation.
+template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSrc>
+__device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
+                                              const CoefSet& cs, int bx, int by, int bz, int kchunk,
+                                              const float* __restrict__ Jx, const float* __restrict__ Jy,
+                                              const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
+                                              int* err, unsigned char* smem, uint32_t& ring, int nsrc) {
   using P = Plan1<S, RY>;
   using HiT = typename S::HiT;
   using T = typename A::Cur;
   constexpr int NS = kStages1;
-  extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + P::kBar);
   int* list = reinterpret_cast<int*>(smem + P::kList);
 
   const int lane = threadIdx.x, w = threadIdx.y;
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * RY;
+  const int x0 = bx * 32, y0 = by * RY;
   const int nx = min(32, L.Ni - x0), ny = min(RY, L.Nj - y0);
   const bool hcol = (w == RY + 1);
   // box row (lanes of the halo-column warp past the tile's rows are clamped
@@ -121,9 +135,11 @@ __global__ void __launch_bounds__(32 * (RY + 2))
   // logical coordinates (x = Ni and y = Nj are the ghost copies of 0)
   const int xu = x0 + cx, yu = y0 + r - 1;
   const int xl = xu >= L.Ni ? xu - L.Ni : xu, yl = yu >= L.Nj ? yu - L.Nj : yu;
-  const int k0 = blockIdx.z * kchunk;
+  const int k0 = bz * kchunk;
   const int k1 = min(k0 + kchunk, L.Nk);
   const bool leader = (w == 0 && lane == 0);
+  const int slot0 = (int)(ring % NS);
+  const uint32_t phase0 = (ring / NS) & 1u;
   const bool tile_edge = x0 == 0 || x0 + nx == L.Ni || y0 == 0 || y0 + ny == L.Nj;
   // The copy engine clips a store along x in 16-byte units, not elements: a
   // tile narrower than 32 columns would overwrite the ghost column past the
@@ -142,7 +158,7 @@ __global__ void __launch_bounds__(32 * (RY + 2))
   const int lo_own = r * P::LW + cx + kLoOff1;
 
   auto issue = [&](int t) {
-    const int slot = (t - k0) % NS;
+    const int slot = (slot0 + t - k0) % NS;
     const int kk = (t == L.Nk) ? 0 : t;
     unsigned char* base = smem + P::kRing + slot * P::kStage;
     mbar_arrive_expect_tx(&bar[slot], P::kTx);
@@ -152,32 +168,27 @@ __global__ void __launch_bounds__(32 * (RY + 2))
         tma_load_3d(base + 6 * P::kHiBox + c * P::kLoBox, &maps.ld.lo[c], x0 + kPadX - kLoOff1, y0, kk, &bar[slot]);
   };
 
-  // Sources that can touch this tile's cells (its E' halo included), in
-  // registration order; the exact per-cell test comes later.
-  if (w == 0) {
-    int n = 0;
-    for (int b = 0; b < ss.count; b += 32) {
-      const int q = b + lane;
-      bool hit = false;
-      if (q < ss.count) {
-        const DevSource& d = ss.src[q];
-        hit = step < d.n_amp && window_meets(d.i0, d.ni, L.Ni, x0, nx + 1) &&
-              window_meets(d.j0, d.nj, L.Nj, y0, ny + 1);
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, hit);
-      if (hit) list[n + __popc(m & ((1u << lane) - 1u))] = q;
-      n += __popc(m);
-    }
-    if (lane == 0) list[kMaxSources] = n;
-  }
-  if (leader) {
-    for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
-    mbar_init_fence();
-  }
-  __syncthreads();
-  const int nsrc = list[kMaxSources];
   if (leader)
     for (int t = k0; t <= k1 && t < k0 + NS; ++t) issue(t);
+
+  // Per-column factor (amp gx) gy of the first kFastSources listed sources
+  // (only the z factor changes from plane to plane).
+  T sxy[kFastSources];
+  unsigned smask = 0;
+#pragma unroll
+  for (int q = 0; q < kFastSources; ++q) {
+    sxy[q] = A::cur_zero();
+    if (kSrc && q < nsrc) {
+      const DevSource& d = ss.src[list[q]];
+      const int di = box_offset(xl, d.i0, d.ni, L.Ni);
+      const int dj = box_offset(yl, d.j0, d.nj, L.Nj);
+      if (active && di >= 0 && dj >= 0) {
+        sxy[q] = A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + step), A::cur_table(ss, d.gx_off + di)),
+                            A::cur_table(ss, d.gy_off + dj));
+        smask |= 1u << q;
+      }
+    }
+  }
 
   Pair pbx{0.f, 0.f}, pby{0.f, 0.f}, pbz{0.f, 0.f};
   Pair pex{0.f, 0.f}, pey{0.f, 0.f}, pez{0.f, 0.f};
@@ -187,8 +198,8 @@ __global__ void __launch_bounds__(32 * (RY + 2))
     pby = st.load(4, b0);
   }
 
-  int slot = 0;
-  uint32_t phase = 0;
+  int slot = slot0;
+  uint32_t phase = phase0;
   for (int t = k0; t <= k1; ++t) {
     const int cur = t & 1;
     const int kk = (t == L.Nk) ? 0 : t;
@@ -208,17 +219,30 @@ __global__ void __launch_bounds__(32 * (RY + 2))
     Pair qx = A::curl(cs.ce[1], bz, V(5, -1, 0), cs.ce[2], by, pby);
     Pair qy = A::curl(cs.ce[2], bx, pbx, cs.ce[0], bz, V(5, 0, -1));
     Pair qz = A::curl(cs.ce[0], by, V(4, 0, -1), cs.ce[1], bx, V(3, -1, 0));
-    if (kDenseJ || nsrc > 0) {
+    if (kDenseJ || kSrc) {
+      // Current, accumulated per J component in registration order; only the
+      // components that received current get the current term.
       T jv[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
-      bool has_j = false;
+      unsigned has = 0;
       if (kDenseJ && active) {
         const int64_t d = xl + (int64_t)yl * L.Ni + (int64_t)kk * L.Ni * L.Nj;
         jv[0] = A::cur_dense(Jx[d]);
         jv[1] = A::cur_dense(Jy[d]);
         jv[2] = A::cur_dense(Jz[d]);
-        has_j = true;
+        has = 7u;
       }
-      for (int i = 0; i < nsrc; ++i) {
+#pragma unroll
+      for (int q = 0; q < kFastSources; ++q) {
+        if (kSrc && q < nsrc) {
+          const DevSource& d = ss.src[list[q]];
+          const int dk = box_offset(kk, d.k0, d.nk, L.Nk);  // the same for the whole tile
+          if (dk >= 0 && (smask >> q & 1u)) {
+            add_current<A>(jv, d.comp_mask, A::cur_mul(sxy[q], A::cur_table(ss, d.gz_off + dk)));
+            has |= (unsigned)d.comp_mask;
+          }
+        }
+      }
+      for (int i = kFastSources; kSrc && i < nsrc; ++i) {
         const DevSource& d = ss.src[list[i]];
         const int dk = box_offset(kk, d.k0, d.nk, L.Nk);
         if (dk < 0) continue;
@@ -230,14 +254,12 @@ __global__ void __launch_bounds__(32 * (RY + 2))
                                                           A::cur_table(ss, d.gx_off + di)),
                                                A::cur_table(ss, d.gy_off + dj)),
                                     A::cur_table(ss, d.gz_off + dk)));
-          has_j = true;
+          has |= (unsigned)d.comp_mask;
         }
       }
-      if (has_j) {
-        qx = A::add(qx, A::cur_term(cs.cj, jv[0]));
-        qy = A::add(qy, A::cur_term(cs.cj, jv[1]));
-        qz = A::add(qz, A::cur_term(cs.cj, jv[2]));
-      }
+      if (has & 1u) qx = A::add(qx, A::cur_term(cs.cj, jv[0]));
+      if (has & 2u) qy = A::add(qy, A::cur_term(cs.cj, jv[1]));
+      if (has & 4u) qz = A::add(qz, A::cur_term(cs.cj, jv[2]));
     }
     const Pair ax = A::acc(V(0, 0, 0), qx), ay = A::acc(V(1, 0, 0), qy), az = A::acc(V(2, 0, 0), qz);
     // E' in its stored words; the B update uses the value they hold.
@@ -348,7 +370,126 @@ __global__ void __launch_bounds__(32 * (RY + 2))
       phase ^= 1u;
     }
   }
-  if (leader) bulk_wait_all();
+  ring += (uint32_t)(k1 - k0 + 1);
+  if (leader) bulk_wait_read_all();
+}
+
+//
+// kSplit: compile the plane loop twice and run the source-free copy on tiles
+// that no source reaches (fewer live registers there).  The batched kernel
+// uses one copy: its tiles alternate between the two cases, and two hot copies
+// of the loop ran about 30 % slower there.
+template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSplit>
+__device__ __forceinline__ void fused1_tile(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
+                                            const CoefSet& cs, int bx, int by, int bz, int kchunk,
+                                            const float* __restrict__ Jx, const float* __restrict__ Jy,
+                                            const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
+                                            int* err, unsigned char* smem, uint32_t& ring) {
+  using P = Plan1<S, RY>;
+  int* list = reinterpret_cast<int*>(smem + P::kList);
+  // Sources that can touch this tile's cells (its E' halo included), in
+  // registration order; the exact per-cell test comes in the plane loop.
+  if (threadIdx.y == 0) {
+    const int lane = threadIdx.x;
+    const int x0 = bx * 32, y0 = by * RY;
+    const int nx = min(32, L.Ni - x0), ny = min(RY, L.Nj - y0);
+    int n = 0;
+    for (int b = 0; b < ss.count; b += 32) {
+      const int q = b + lane;
+      bool hit = false;
+      if (q < ss.count) {
+        const DevSource& d = ss.src[q];
+        hit = step < d.n_amp && window_meets(d.i0, d.ni, L.Ni, x0, nx + 1) &&
+              window_meets(d.j0, d.nj, L.Nj, y0, ny + 1);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (hit) list[n + __popc(m & ((1u << lane) - 1u))] = q;
+      n += __popc(m);
+    }
+    if (lane == 0) list[kMaxSources] = n;
+  }
+  __syncthreads();
+  const int nsrc = list[kMaxSources];
+  if (!kSplit || nsrc > 0)
+    fused1_planes<S, A, RY, kApps, kDenseJ, true>(L, st, out, maps, cs, bx, by, bz, kchunk, Jx, Jy, Jz, ss, step, err,
+                                                  smem, ring, nsrc);
+  else
+    fused1_planes<S, A, RY, kApps, kDenseJ, false>(L, st, out, maps, cs, bx, by, bz, kchunk, Jx, Jy, Jz, ss, step,
+                                                   err, smem, ring, 0);
+}
+
+template <int NS>
+__device__ __forceinline__ void init_ring(uint64_t* bar) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+}
+
+template <class S, class A, int RY, int kApps, bool kDenseJ>
+__global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
+    fused1(PLayout L, S st, S out, const __grid_constant__ StepMaps maps, CoefSet cs, int kchunk,
+           const float* __restrict__ Jx, const float* __restrict__ Jy, const float* __restrict__ Jz,
+           SourceSet ss, int64_t step, int* err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
+  uint32_t ring = 0;
+  fused1_tile<S, A, RY, kApps, kDenseJ, true>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z, kchunk, Jx, Jy,
+                                        Jz, ss, step, err, smem, ring);
+  if (threadIdx.x == 0 && threadIdx.y == 0) bulk_wait_all();
+}
+
+// Batched form: a persistent kernel; every CTA takes tiles (domain, bx, by,
+// bz) from the tile table in order, through an atomic counter, until none
+// are left.  `parity` selects which of each domain's two copies is read.  The
+// last CTA to finish resets the counters for the next launch.
+template <class S, class A, int RY, int kApps>
+__global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
+    fused1_batch(const BatchDomain<S>* __restrict__ doms, const StepMaps* __restrict__ maps,
+                 const int4* __restrict__ tiles, int n_tiles, int parity, int kchunk,
+                 const int64_t* __restrict__ step_base, int step_off, int* counters, int* err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ BatchDomain<S> dom;
+  __shared__ int4 tile;
+  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
+  const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const int64_t step = *step_base + step_off;
+  uint32_t ring = 0;
+  for (;;) {
+    if (leader) {
+      const int it = atomicAdd(&counters[0], 1);
+      tile = it < n_tiles ? tiles[it] : make_int4(-1, 0, 0, 0);
+    }
+    __syncthreads();
+    const int4 w = tile;
+    if (w.x < 0) break;
+    // the tile's domain record, copied word by word into shared memory
+    constexpr int kWords = (int)(sizeof(BatchDomain<S>) / 4);
+    const int* src = reinterpret_cast<const int*>(doms + w.x);
+    int* dst = reinterpret_cast<int*>(&dom);
+    for (int q = tid; q < kWords; q += blockDim.x * blockDim.y) dst[q] = src[q];
+    if (threadIdx.y == 1 && threadIdx.x < 24) {
+      // warm the descriptor cache for this tile's loads and stores
+      const StepMaps& m = maps[2 * w.x + parity];
+      const int q = threadIdx.x;
+      const CUtensorMap* tm = q < 6 ? &m.ld.hi[q] : q < 12 ? &m.ld.lo[q - 6] : q < 18 ? &m.st.hi[q - 12] : &m.st.lo[q - 18];
+      if (Plan1<S, RY>::kLo || (q < 6 || (q >= 12 && q < 18))) prefetch_tensormap(tm);
+    }
+    __syncthreads();
+    fused1_tile<S, A, RY, kApps, false, false>(dom.L, dom.s[parity], dom.s[parity ^ 1], maps[2 * w.x + parity], dom.cs, w.y,
+                                        w.z, w.w, kchunk, nullptr, nullptr, nullptr, dom.ss, step, err, smem, ring);
+    __syncthreads();
+  }
+  if (leader) {
+    bulk_wait_all();
+    __threadfence();
+    if (atomicAdd(&counters[1], 1) == (int)(gridDim.x * gridDim.y * gridDim.z) - 1) {
+      counters[0] = 0;
+      counters[1] = 0;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -396,6 +537,44 @@ cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const
   return launch1_ry<S, 14>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
 }
 
+template <class S, int RY, int APPS>
+static cudaError_t launch1_batch_one(const BatchDomain<S>* doms, const StepMaps* maps, const int4* tiles,
+                                     int n_tiles, int parity, int kchunk, const int64_t* step_base, int step_off,
+                                     int* counters, int* err, cudaStream_t stream) {
+  using A = typename ArithOf1<S>::type;
+  auto kern = fused1_batch<S, A, RY, APPS>;
+  const int bytes = Plan1<S, RY>::kTotal;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * (RY + 2), bytes)) != cudaSuccess)
+    return e;
+  const int grid = sms * (per_sm > 0 ? per_sm : 1);
+  kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(doms, maps, tiles, n_tiles, parity, kchunk, step_base, step_off,
+                                                  counters, err);
+  return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t launch_fused1_batch(const void* doms, const StepMaps* maps, const int4* tiles, int n_tiles, int parity,
+                                int applications, const FusedConfig& cfg, const int64_t* step_base, int step_off,
+                                int* counters, int* err, cudaStream_t stream) {
+  const BatchDomain<S>* d = static_cast<const BatchDomain<S>*>(doms);
+  const int kc = cfg.kchunk;
+#define FDTD_B(RY)                                                                                                  \
+  return applications == 2                                                                                       \
+             ? launch1_batch_one<S, RY, 2>(d, maps, tiles, n_tiles, parity, kc, step_base, step_off, counters, err, \
+                                           stream)                                                               \
+             : launch1_batch_one<S, RY, 1>(d, maps, tiles, n_tiles, parity, kc, step_base, step_off, counters, err, \
+                                           stream)
+  if (cfg.tile_y == 6) FDTD_B(6);
+  if (cfg.tile_y == 30) FDTD_B(30);
+  FDTD_B(14);
+#undef FDTD_B
+}
+
 template <class S>
 int fused1_box_width() { return Box1<S>::kW; }
 int fused1_lo_box_width() { return Box1<StoreF32C>::kLoW; }
@@ -404,6 +583,8 @@ int fused1_lo_box_width() { return Box1<StoreF32C>::kLoW; }
   template cudaError_t launch_fused1_f32<S>(const PLayout&, const S&, const S&, const void*,            \
                                             const float* const[3], bool, const CoefSet&, const SourceSet&, \
                                             int64_t, int, const FusedConfig&, int*, cudaStream_t);       \
+  template cudaError_t launch_fused1_batch<S>(const void*, const StepMaps*, const int4*, int, int, int,          \
+                                              const FusedConfig&, const int64_t*, int, int*, int*, cudaStream_t); \
   template int fused1_box_width<S>();
 FDTD_INSTANTIATE(StoreF32)
 FDTD_INSTANTIATE(StoreF32C)

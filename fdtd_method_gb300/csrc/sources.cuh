@@ -19,11 +19,13 @@ __device__ __forceinline__ void add_current(typename A::Cur jv[3], int mask, typ
   if (mask & 4) jv[2] = A::cur_add(jv[2], v);
 }
 
-// Every source at logical cell (i, j, k), time step s.
+// Every source at logical cell (i, j, k), time step s.  Returns the mask of
+// the J components that received current (bit c: component c); only those
+// get the current term.
 template <class A>
-__device__ __forceinline__ bool source_sum(const SourceSet& ss, int64_t s, int i, int j, int k,
-                                           const PLayout& L, typename A::Cur jv[3]) {
-  bool any = false;
+__device__ __forceinline__ unsigned source_sum(const SourceSet& ss, int64_t s, int i, int j, int k,
+                                               const PLayout& L, typename A::Cur jv[3]) {
+  unsigned any = 0;
   for (int q = 0; q < ss.count; ++q) {
     const DevSource& d = ss.src[q];
     if (s >= d.n_amp) continue;
@@ -38,7 +40,7 @@ __device__ __forceinline__ bool source_sum(const SourceSet& ss, int64_t s, int i
                               A::cur_table(ss, d.gy_off + dj)),
                    A::cur_table(ss, d.gz_off + dk));
     add_current<A>(jv, d.comp_mask, v);
-    any = true;
+    any |= (unsigned)d.comp_mask;
   }
   return any;
 }
@@ -66,10 +68,11 @@ struct ColumnSources {
       }
     }
   }
-  // Adds the contributions at plane k; true if any source covers the cell.
-  __device__ __forceinline__ bool eval(const SourceSet& ss, int k, const PLayout& L,
-                                       typename A::Cur jv[3]) const {
-    bool any = false;
+  // Adds the contributions at plane k; returns the mask of J components that
+  // received current.
+  __device__ __forceinline__ unsigned eval(const SourceSet& ss, int k, const PLayout& L,
+                                           typename A::Cur jv[3]) const {
+    unsigned any = 0;
 #pragma unroll
     for (int q = 0; q < kFastSources; ++q) {
       if (mask & (1u << q)) {
@@ -77,7 +80,7 @@ struct ColumnSources {
         const int dk = box_offset(k, d.k0, d.nk, L.Nk);
         if (dk >= 0) {
           add_current<A>(jv, d.comp_mask, A::cur_mul(xy[q], A::cur_table(ss, d.gz_off + dk)));
-          any = true;
+          any |= (unsigned)d.comp_mask;
         }
       }
     }

@@ -330,3 +330,115 @@ class FDTD:
         return {"coef_E": (cdt / p.dx, cdt / p.dy, cdt / p.dz),
                 "coef_B": (cdt / (2.0 * p.dx), cdt / (2.0 * p.dy), cdt / (2.0 * p.dz)),
                 "current_coef": -4.0 * Const.PI * dt}
+
+
+class FDTDBatch:
+    """Many independent periodic domains advanced together on one GPU (the
+    batched form; the reference advances one grid per object).  Every domain
+    has its own Parameters and sources and the same dt and precision (FP32,
+    FP32_COMP or FP16_SCALED).  ``step(n)`` advances all domains by n steps:
+    one persistent kernel launch per fused sweep works through the tile table
+    of every domain, and the step group runs as one CUDA graph.  Each domain's
+    results equal those of a single FDTD of the same form run alone."""
+
+    def __init__(self, parameters, dt, precision=Precision.FP32_COMP):
+        self._b = None
+        lib = _lib.load()
+        self.parameters = list(parameters)
+        self.dt = float(dt)
+        self.precision = Precision(precision)
+        arr = (_lib.Params * len(self.parameters))(*[p.to_c() for p in self.parameters])
+        b = ctypes.c_void_p()
+        _lib.check(lib.fdtd_batch_create(arr, len(self.parameters), self.dt, int(self.precision), ctypes.byref(b)))
+        self._b = b
+        self._lib = lib
+
+    def close(self):
+        if self._b is not None:
+            self._lib.fdtd_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self.parameters)
+
+    def _handle(self):
+        if self._b is None:
+            raise FDTDError(_lib.FDTD_ERR_INVALID_ARGUMENT, "batch is closed")
+        return self._b
+
+    def _params(self, domain):
+        if not 0 <= int(domain) < len(self.parameters):
+            raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "domain index out of range")
+        return self.parameters[int(domain)]
+
+    def add_source(self, domain, src):
+        self._params(domain)
+        c, keep = src.to_c()
+        idx = ctypes.c_int()
+        _lib.check(self._lib.fdtd_batch_add_source(self._handle(), int(domain), ctypes.byref(c), ctypes.byref(idx)))
+        return idx.value
+
+    def copy_to_host(self, domain, comp, out=None):
+        n = self._params(domain).cells
+        if out is None:
+            out = np.empty(n, dtype=np.float64)
+        if out.dtype != np.float64 or out.size != n or not out.flags.c_contiguous:
+            raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "output must be a contiguous float64 array of Ni*Nj*Nk")
+        _lib.check(self._lib.fdtd_batch_copy_field_to_host(self._handle(), int(domain), int(comp), out.ctypes.data, n))
+        return out
+
+    def copy_from_host(self, domain, comp, values):
+        n = self._params(domain).cells
+        a = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        if a.size != n:
+            raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "expected %d values, got %d" % (n, a.size))
+        _lib.check(self._lib.fdtd_batch_copy_field_from_host(self._handle(), int(domain), int(comp), a.ctypes.data, n))
+
+    def field_sums(self, domain):
+        out = (ctypes.c_double * _lib.DIAG_COUNT)()
+        _lib.check(self._lib.fdtd_batch_field_sums(self._handle(), int(domain), out))
+        return np.array(out[:], dtype=np.float64)
+
+    def energy(self, domain):
+        s = self.field_sums(domain)
+        p = self._params(domain)
+        return float(s[:6].sum() * p.dx * p.dy * p.dz / (8.0 * Const.PI))
+
+    def set_fp16_exponents(self, domain, exps):
+        arr = (ctypes.c_int * 6)(*[int(e) for e in exps])
+        _lib.check(self._lib.fdtd_batch_set_fp16_exponents(self._handle(), int(domain), arr))
+
+    def set_config(self, tile_y=0, kchunk=0, graphs=True):
+        _lib.check(self._lib.fdtd_batch_set_config(self._handle(), int(tile_y), int(kchunk), 1 if graphs else 0))
+
+    def step(self, n):
+        _lib.check(self._lib.fdtd_batch_step(self._handle(), int(n)))
+
+    def synchronize(self):
+        _lib.check(self._lib.fdtd_batch_synchronize(self._handle()))
+
+    def set_stream(self, stream_handle):
+        _lib.check(self._lib.fdtd_batch_set_stream(self._handle(), ctypes.c_void_p(int(stream_handle or 0))))
+
+    @property
+    def step_index(self):
+        v = ctypes.c_int64()
+        _lib.check(self._lib.fdtd_batch_get_step(self._handle(), ctypes.byref(v)))
+        return v.value
+
+    def tiles(self):
+        v = ctypes.c_int64()
+        _lib.check(self._lib.fdtd_batch_tiles(self._handle(), ctypes.byref(v)))
+        return v.value

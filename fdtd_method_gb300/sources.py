@@ -157,3 +157,28 @@ def random_pulses(params, count, seed=0, n_steps=1000, sigma=8.0, comps=("z", "x
         comp = comps[rng.integer(0, len(comps) - 1)]
         out.append(gaussian_pulse(params, c, sigma, A, T, 3.0 * T, T, n_steps, phase=phase, comp=comp))
     return out
+
+
+def batch_workload(count=256, seed=0, n_steps=500, lo=32, hi=160, sigma=4.0):
+    """The batched-form workload: `count` periodic domains with per-axis edge
+    lengths uniform in [lo, hi]; each starts from a plane wave along a random
+    axis with mode number 1..4 and carries one Gaussian-pulse source
+    (A ~ U[0.5, 2], T ~ U[20, 60] steps, tau = T, t0 = 3 tau, random cell,
+    random phase, Jz or Jx).  Returns a list of (params, {component: initial
+    field}, source)."""
+    rng = SplitMix64(seed)
+    out = []
+    for _ in range(count):
+        p = normalised_parameters(rng.integer(lo, hi), rng.integer(lo, hi), rng.integer(lo, hi))
+        axis = rng.integer(0, 2)
+        mode = rng.integer(1, 4)
+        init = plane_wave_fields(p, axis=axis, mode=mode)
+        A = rng.uniform(0.5, 2.0)
+        T = rng.uniform(20.0, 60.0)
+        phase = rng.uniform(0.0, 2.0 * math.pi)
+        c = (rng.integer(0, p.Ni - 1), rng.integer(0, p.Nj - 1), rng.integer(0, p.Nk - 1))
+        comp = ("z", "x")[rng.integer(0, 1)]
+        src = gaussian_pulse(p, c, sigma, A, T, 3.0 * T, T, n_steps, phase=phase, comp=comp)
+        src.meta.update({"axis": axis, "mode": mode})
+        out.append((p, init, src))
+    return out

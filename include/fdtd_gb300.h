@@ -195,6 +195,43 @@ enum fdtd_pipeline { FDTD_PIPELINE_AUTO = 0, FDTD_PIPELINE_SPLIT = 1, FDTD_PIPEL
 int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int cells_per_thread);
 int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t launches[FDTD_KERNEL_KINDS]);
 
+/* ------------------------------------------------------------------------
+ * Batched form (new; the reference advances one grid per object).  A batch
+ * holds n independent periodic domains of any sizes on one GPU, stored in an
+ * FP32-arithmetic form (FP32, FP32_COMP or FP16_SCALED), all with the same
+ * dt.  fdtd_batch_step(b, n) advances every domain by n update_fields steps:
+ * one launch does the leading B half step of every domain, then each fused
+ * sweep of all domains is one persistent kernel launch that works through a
+ * per-domain tile table; the whole step group runs as one CUDA graph
+ * (captured on first use for each step count, then replayed).  Each domain's
+ * results are bit-identical to a single-domain handle of the same form run
+ * alone.  Domains take analytic sources only (no dense J arrays).
+ * Not thread-safe per batch. */
+typedef struct fdtd_batch fdtd_batch;
+
+/* params[0..n-1] describe the domains (as fdtd_create; same validation). */
+int fdtd_batch_create(const fdtd_params* params, int n, double dt, int precision, fdtd_batch** out);
+int fdtd_batch_destroy(fdtd_batch* b);
+int fdtd_batch_size(fdtd_batch* b, int* n);
+int fdtd_batch_domain_params(fdtd_batch* b, int domain, fdtd_params* params);
+/* Domain-wise versions of fdtd_add_source, fdtd_copy_field_to_host/from_host
+ * (E and B components only), fdtd_field_sums and fdtd_set_fp16_exponents. */
+int fdtd_batch_add_source(fdtd_batch* b, int domain, const fdtd_source* src, int* index);
+int fdtd_batch_copy_field_to_host(fdtd_batch* b, int domain, int comp, double* host, size_t n);
+int fdtd_batch_copy_field_from_host(fdtd_batch* b, int domain, int comp, const double* host, size_t n);
+int fdtd_batch_field_sums(fdtd_batch* b, int domain, double out[FDTD_DIAG_COUNT]);
+int fdtd_batch_set_fp16_exponents(fdtd_batch* b, int domain, const int exponents[6]);
+/* Tile shape of the fused sweep (tile_y 6, 14 or 30; kchunk planes per tile;
+ * 0 = defaults 14 and 24) and whether step groups run as CUDA graphs. */
+int fdtd_batch_set_config(fdtd_batch* b, int tile_y, int kchunk, int use_graphs);
+/* n steps of every domain; asynchronous on the batch's stream. */
+int fdtd_batch_step(fdtd_batch* b, int64_t n);
+int fdtd_batch_get_step(fdtd_batch* b, int64_t* step);
+/* Number of fused-sweep tiles of the batch at its current tile shape. */
+int fdtd_batch_tiles(fdtd_batch* b, int64_t* tiles);
+int fdtd_batch_set_stream(fdtd_batch* b, void* stream);
+int fdtd_batch_synchronize(fdtd_batch* b);
+
 /* No counterpart in the reference.  The ten field sums of fdtd_field_sums,
  * for callers that cannot allocate device memory (an application whose pool
  * allocator owns every device allocation, a monitor that must not call

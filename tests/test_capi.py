@@ -67,3 +67,14 @@ def test_null_handle_calls_fail_cleanly(lib):
     assert lib.fdtd_update_fields(None) == _lib.FDTD_ERR_INVALID_ARGUMENT
     assert lib.fdtd_destroy(None) == 0
     assert Precision.FP32_COMP == 2
+
+
+def test_batch_arguments_checked_before_gpu_work(lib):
+    p = Parameters(4, 4, 4, 0, 1, 0, 1, 0, 1, 0.25, 0.25, 0.25)
+    arr = (_lib.Params * 1)(p.to_c())
+    b = ctypes.c_void_p()
+    assert lib.fdtd_batch_create(arr, 0, 1e-12, 2, ctypes.byref(b)) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_batch_create(arr, 1, 1e-12, 0, ctypes.byref(b)) == _lib.FDTD_ERR_UNSUPPORTED
+    assert b"FP32" in lib.fdtd_last_error()
+    assert lib.fdtd_batch_step(None, 1) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_batch_destroy(None) == 0
