@@ -66,6 +66,7 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=0, help="timed FP64 steps (default max(20, K/5))")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form leg")
     ap.add_argument("--batch-only", action="store_true", help="run only the batched-form leg and print it")
     ap.add_argument("--batch-domains", type=int, default=256)
@@ -281,6 +282,7 @@ def run_batched(args, stream, world):
             b.copy_from_host(q, int(c), v)
         b.add_source(q, src)
     cells = sum(w[0].cells for w in wl)
+    tuned = None if args.no_autotune else b.autotune(sweeps=5)
     b.step(G)  # captures the group's graph and warms up
     b.synchronize()
     torch.cuda.synchronize()
@@ -304,7 +306,7 @@ def run_batched(args, stream, world):
     edges = [w[0].Ni for w in wl] + [w[0].Nj for w in wl] + [w[0].Nk for w in wl]
     return {"value": world * cells * steps / (ms / 1e3) / 1e9, "unit": UNIT, "domains": len(wl), "cells": cells,
             "edge_min": min(edges), "edge_max": max(edges), "tiles_per_sweep": tiles, "steps": steps,
-            "group_steps": G, "ms_per_step": ms / steps, "launches_per_group": G + 2,
+            "group_steps": G, "ms_per_step": ms / steps, "launches_per_group": G + 2, "autotune": tuned,
             "step_roofline": {"algorithmic_bytes_per_cell_step": 12 * bpv, "achieved": gbs, "peak": hbm,
                               "frac": gbs / hbm, "peak_note": note},
             "workload": "%d periodic domains, edges uniform in 32..160 cells, plane wave (random axis, mode 1-4) "
@@ -337,6 +339,9 @@ def run_ours(args):
     sim.set_pipeline(args.pipeline, args.tile_y, args.kchunk, args.cells_per_thread)
     sim.set_stream(stream.cuda_stream)
     sim.add_source(src)
+    tuned = None
+    if not args.no_autotune and args.pipeline != "split" and not (args.tile_y or args.kchunk or args.cells_per_thread):
+        tuned = sim.autotune(sweeps=10, reuse=False)  # before the timed region; the state is only read
     sim.step(W)
     sim.synchronize()
     sim.kernel_times()
@@ -394,6 +399,8 @@ def run_ours(args):
         host = [torch.zeros(cells, dtype=torch.float64).pin_memory().numpy() for _ in range(6)]
         s = FDTD(p, COURANT_DT, PREC[args.precision])
         s.set_pipeline(args.pipeline, args.tile_y, args.kchunk, args.cells_per_thread)
+        if tuned:
+            s.autotune(reuse=True)  # the shape chosen above (cached)
         s.add_source(src)
         for c in range(6):  # warm-up job (not timed)
             s.copy_from_host(c, host[c])
@@ -459,7 +466,8 @@ def run_ours(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
                 "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic (seeded Gaussian-pulse source, zero initial fields)",
-                "config": config_dict(args, p, src), "clocks": clk, "e2e": e2e, "gpu_launches": launches,
+                "config": dict(config_dict(args, p, src), autotune=tuned), "clocks": clk, "e2e": e2e,
+                "gpu_launches": launches,
                 "roofline": roofline, "step_roofline": step_roof, "cpu_baseline": cpu,
                 "fp64": {"value": v64, "unit": UNIT, "steps": K64, "ms_per_step": ms64 / K64,
                          "chosen_vs_fp64": value / v64,

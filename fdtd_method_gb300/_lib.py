@@ -60,6 +60,11 @@ class Source(ctypes.Structure):
                 ("n_amp", ctypes.c_int64)]
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("tile_y", ctypes.c_int), ("kchunk", ctypes.c_int), ("cells_per_thread", ctypes.c_int),
+                ("ms_per_sweep", ctypes.c_double), ("candidates", ctypes.c_int), ("cached", ctypes.c_int)]
+
+
 _H = ctypes.c_void_p
 _D = ctypes.POINTER(ctypes.c_double)
 
@@ -87,6 +92,8 @@ SIGNATURES = {
     "fdtd_set_kernel_timing": [_H, ctypes.c_int],
     "fdtd_kernel_times": [_H, _D, ctypes.POINTER(ctypes.c_int64)],
     "fdtd_set_pipeline": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+    "fdtd_autotune": [_H, ctypes.c_int, ctypes.c_int, ctypes.POINTER(TuneResult)],
+    "fdtd_batch_autotune": [_H, ctypes.c_int, ctypes.POINTER(TuneResult)],
     "fdtd_field_sums_noalloc": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p],
     # batched form
     "fdtd_batch_create": [ctypes.POINTER(Params), ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(_H)],

@@ -381,6 +381,62 @@ int fdtd_batch_step(fdtd_batch* b, int64_t n) {
   return FDTD_OK;
 }
 
+int fdtd_batch_autotune(fdtd_batch* b, int sweeps, fdtd_tune_result* out) {
+  if (int rc = check_batch(b)) return rc;
+  if (sweeps <= 0) sweeps = 5;
+  DeviceGuard dg(b->device);
+  // The timed sweeps read copy `parity` and write the other copy: the state
+  // is left as it was.  Tables are rebuilt per candidate (copy 0 = current).
+  static const int rows[] = {6, 14, 30};
+  static const int chunks[] = {16, 24, 32, 48};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FDTD_BCUDA(cudaEventCreate(&e0), "autotune events");
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return bfail(FDTD_ERR_CUDA, "autotune events");
+  }
+  fdtd_tune_result best{};
+  best.ms_per_sweep = 1e30;
+  best.cells_per_thread = 1;
+  const bool graphs = b->use_graphs;
+  int rc = FDTD_OK;
+  for (int ty : rows) {
+    for (int kc : chunks) {
+      b->cfg.tile_y = ty;
+      b->cfg.kchunk = kc;
+      b->cfg.cells_per_thread = 1;
+      if ((rc = build_tables(b)) != FDTD_OK) break;
+      cudaError_t e = launch_fused_all(b, 0, 2, 0);  // warm-up
+      if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+      for (int q = 0; q < sweeps && e == cudaSuccess; ++q) e = launch_fused_all(b, 0, 2, 0);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) {
+        rc = bcuda(e, "batch autotune sweep");
+        break;
+      }
+      best.candidates += 1;
+      if (ms / sweeps < best.ms_per_sweep) {
+        best.ms_per_sweep = ms / sweeps;
+        best.tile_y = ty;
+        best.kchunk = kc;
+      }
+    }
+    if (rc != FDTD_OK) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != FDTD_OK) return rc;
+  b->cfg.tile_y = best.tile_y;
+  b->cfg.kchunk = best.kchunk;
+  b->use_graphs = graphs;
+  b->dirty = true;
+  if (out) *out = best;
+  return FDTD_OK;
+}
+
 int fdtd_batch_synchronize(fdtd_batch* b) {
   if (int rc = check_batch(b)) return rc;
   DeviceGuard dg(b->device);

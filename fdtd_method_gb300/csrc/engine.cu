@@ -4,6 +4,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -219,9 +222,9 @@ int run_e(fdtd_handle* h, int64_t step) {
 
 // E step `step` followed by `apps` B half steps, in one sweep from the
 // current copy into the second one, which then becomes current.
-int run_fused(fdtd_handle* h, int64_t step, int apps) {
-  if (int rc = ensure_alt(h)) return rc;
-  LaunchTimer lt(h, FDTD_KERNEL_FUSED);
+// One fused sweep from the current copy into the second one, without the
+// swap (the autotuner repeats it to time a tile shape: the state is only read).
+cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps) {
   SourceSet ss = h->source_set();
   StateView v = h->view();
   StateView w = h->view_alt();
@@ -246,11 +249,33 @@ int run_fused(fdtd_handle* h, int64_t step, int apps) {
     FDTD_FUSED_LAUNCH(launch_fused1_f32)
   }
 #undef FDTD_FUSED_LAUNCH
+  return e;
+}
+
+int run_fused(fdtd_handle* h, int64_t step, int apps) {
+  if (int rc = ensure_alt(h)) return rc;
+  LaunchTimer lt(h, FDTD_KERNEL_FUSED);
+  cudaError_t e = launch_fused_sweep(h, step, apps);
   lt.done();
   if (e != cudaSuccess) return cuda_fail(e, "fused step launch");
   swap_copies(h);
   return FDTD_OK;
 }
+
+// Tile shapes the autotuner tries (one cell per thread: 6, 14 or 30 rows;
+// two cells per thread: 6 or 14), each with every chunk length.
+constexpr int kTuneRows1[] = {6, 14, 30};
+constexpr int kTuneRows2[] = {6, 14};
+constexpr int kTuneChunks[] = {16, 24, 32, 48};
+
+struct TuneKey {
+  int form, Ni, Nj, Nk;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(form, Ni, Nj, Nk) < std::tie(o.form, o.Ni, o.Nj, o.Nk);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, fdtd_tune_result> g_tune_cache;
 
 int check_handle(fdtd_handle* h) {
   if (!h) return fail(FDTD_ERR_INVALID_ARGUMENT, "null handle");
@@ -638,6 +663,77 @@ int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int 
   h->fused_cfg.tile_y = tile_y ? tile_y : 14;
   h->fused_cfg.kchunk = kchunk ? kchunk : 24;
   h->fused_cfg.cells_per_thread = cells_per_thread ? cells_per_thread : 1;
+  return FDTD_OK;
+}
+
+int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out) {
+  if (int rc = check_handle(h)) return rc;
+  if (h->form == Form::F64) return fail(FDTD_ERR_UNSUPPORTED, "the FP64 form has one pipeline; nothing to tune");
+  if (sweeps <= 0) sweeps = 10;
+  DeviceGuard dg(h->device);
+  const TuneKey key{(int)h->form, h->g.Ni, h->g.Nj, h->g.Nk};
+  fdtd_tune_result best{};
+  bool cached = false;
+  if (reuse) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      best = it->second;
+      cached = true;
+    }
+  }
+  if (!cached) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    FDTD_CUDA(cudaEventCreate(&e0), "autotune events");
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+      cudaEventDestroy(e0);
+      return fail(FDTD_ERR_CUDA, "autotune events");
+    }
+    best.ms_per_sweep = 1e30;
+    int rc = FDTD_OK;
+    for (int cpt = 1; cpt <= 2 && rc == FDTD_OK; ++cpt) {
+      const int* rows = cpt == 1 ? kTuneRows1 : kTuneRows2;
+      const int nrows = cpt == 1 ? 3 : 2;
+      for (int a = 0; a < nrows && rc == FDTD_OK; ++a)
+        for (int kc : kTuneChunks) {
+          h->fused_cfg.tile_y = rows[a];
+          h->fused_cfg.kchunk = kc;
+          h->fused_cfg.cells_per_thread = cpt;
+          if ((rc = ensure_alt(h)) != FDTD_OK) break;
+          cudaError_t e = launch_fused_sweep(h, h->host_step, 2);  // warm-up
+          if (e == cudaSuccess) e = cudaEventRecord(e0, h->stream);
+          for (int q = 0; q < sweeps && e == cudaSuccess; ++q) e = launch_fused_sweep(h, h->host_step, 2);
+          if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+          if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+          float ms = 0.f;
+          if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+          if (e != cudaSuccess) {
+            rc = cuda_fail(e, "autotune sweep");
+            break;
+          }
+          best.candidates += 1;
+          if (ms / sweeps < best.ms_per_sweep) {
+            best.ms_per_sweep = ms / sweeps;
+            best.tile_y = rows[a];
+            best.kchunk = kc;
+            best.cells_per_thread = cpt;
+          }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != FDTD_OK) return rc;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = best;
+  }
+  h->fused_cfg.tile_y = best.tile_y;
+  h->fused_cfg.kchunk = best.kchunk;
+  h->fused_cfg.cells_per_thread = best.cells_per_thread;
+  if (int rc = ensure_alt(h)) return rc;
+  if (out) {
+    *out = best;
+    out->cached = cached ? 1 : 0;
+  }
   return FDTD_OK;
 }
 

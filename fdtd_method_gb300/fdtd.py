@@ -309,6 +309,15 @@ class FDTD:
         _lib.check(self._lib.fdtd_set_pipeline(self._handle(), self.PIPELINES[pipeline], int(tile_y), int(kchunk),
                                                int(cells_per_thread)))
 
+    def autotune(self, sweeps=10, reuse=True):
+        """Times every candidate launch shape of the fused sweep on this grid
+        (the state is only read) and keeps the fastest.  Returns the choice
+        as a dict; results are cached per (precision, grid) in the process."""
+        r = _lib.TuneResult()
+        _lib.check(self._lib.fdtd_autotune(self._handle(), int(sweeps), 1 if reuse else 0, ctypes.byref(r)))
+        return {"tile_y": r.tile_y, "kchunk": r.kchunk, "cells_per_thread": r.cells_per_thread,
+                "ms_per_sweep": r.ms_per_sweep, "candidates": r.candidates, "cached": bool(r.cached)}
+
     def set_kernel_timing(self, enabled):
         """Bracket every step-pipeline kernel launch with CUDA events."""
         _lib.check(self._lib.fdtd_set_kernel_timing(self._handle(), 1 if enabled else 0))
@@ -425,6 +434,14 @@ class FDTDBatch:
 
     def step(self, n):
         _lib.check(self._lib.fdtd_batch_step(self._handle(), int(n)))
+
+    def autotune(self, sweeps=5):
+        """Times the persistent fused sweep for every candidate tile shape
+        (the state is only read) and keeps the fastest."""
+        r = _lib.TuneResult()
+        _lib.check(self._lib.fdtd_batch_autotune(self._handle(), int(sweeps), ctypes.byref(r)))
+        return {"tile_y": r.tile_y, "kchunk": r.kchunk, "ms_per_sweep": r.ms_per_sweep,
+                "candidates": r.candidates}
 
     def synchronize(self):
         _lib.check(self._lib.fdtd_batch_synchronize(self._handle()))

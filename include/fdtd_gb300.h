@@ -195,6 +195,23 @@ enum fdtd_pipeline { FDTD_PIPELINE_AUTO = 0, FDTD_PIPELINE_SPLIT = 1, FDTD_PIPEL
 int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int cells_per_thread);
 int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t launches[FDTD_KERNEL_KINDS]);
 
+/* Autotuner (new).  Times `sweeps` fused sweeps (0 = 10) for every candidate
+ * launch shape of the FP32-arithmetic forms (cells_per_thread 1 with tile_y
+ * 6, 14 and 30; cells_per_thread 2 with tile_y 6 and 14; each with kchunk 16,
+ * 24, 32 and 48) on the handle's own grid, and keeps the fastest
+ * (fdtd_set_pipeline's shape arguments).  The timed sweeps read the current
+ * state and write the handle's second copy, so the simulation state does not
+ * change.  Results are cached per (precision, Ni, Nj, Nk) in the process;
+ * reuse != 0 takes a cached result without timing.  Synchronous.  The FP64
+ * form gives FDTD_ERR_UNSUPPORTED. */
+typedef struct fdtd_tune_result {
+    int tile_y, kchunk, cells_per_thread;
+    double ms_per_sweep;  /* of the chosen shape */
+    int candidates;       /* shapes timed */
+    int cached;           /* 1 if taken from the cache */
+} fdtd_tune_result;
+int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out);
+
 /* ------------------------------------------------------------------------
  * Batched form (new; the reference advances one grid per object).  A batch
  * holds n independent periodic domains of any sizes on one GPU, stored in an
@@ -230,6 +247,10 @@ int fdtd_batch_get_step(fdtd_batch* b, int64_t* step);
 /* Number of fused-sweep tiles of the batch at its current tile shape. */
 int fdtd_batch_tiles(fdtd_batch* b, int64_t* tiles);
 int fdtd_batch_set_stream(fdtd_batch* b, void* stream);
+/* Autotuner of the batch: times `sweeps` (0 = 5) persistent fused sweeps of
+ * every domain for tile_y 6, 14 and 30 with kchunk 16, 24, 32 and 48, and
+ * keeps the fastest; the state does not change.  Synchronous. */
+int fdtd_batch_autotune(fdtd_batch* b, int sweeps, fdtd_tune_result* out);
 int fdtd_batch_synchronize(fdtd_batch* b);
 
 /* No counterpart in the reference.  The ten field sums of fdtd_field_sums,
