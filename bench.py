@@ -261,6 +261,18 @@ def timed_steps(sim, stream, steps, world):
 
 
 PREC = {"fp32_comp": 2, "fp32": 1, "fp16_scaled": 3}
+# power-of-two storage scale of every component in the FP16 form (fields of
+# this workload peak near 1e1; 2^6 keeps them clear of the subnormal range)
+FP16_EXPONENTS = [6] * 6
+
+
+def make_sim(p, precision_name):
+    from fdtd_method_gb300 import FDTD
+    from fdtd_method_gb300.sources import COURANT_DT
+    s = FDTD(p, COURANT_DT, PREC[precision_name])
+    if precision_name == "fp16_scaled":
+        s.set_fp16_exponents(FP16_EXPONENTS)
+    return s
 BYTES_PER_VALUE = {"fp32_comp": 6, "fp32": 4, "fp16_scaled": 2, "fp64": 8}
 
 
@@ -278,6 +290,8 @@ def run_batched(args, stream, world):
     b = FDTDBatch([w[0] for w in wl], COURANT_DT, PREC[args.precision])
     b.set_stream(stream.cuda_stream)
     for q, (p, init, src) in enumerate(wl):
+        if args.precision == "fp16_scaled":
+            b.set_fp16_exponents(q, FP16_EXPONENTS)
         for c, v in init.items():
             b.copy_from_host(q, int(c), v)
         b.add_source(q, src)
@@ -335,7 +349,7 @@ def run_ours(args):
     out = {}
 
     # --- chosen form, device-timed ---------------------------------------
-    sim = FDTD(p, COURANT_DT, PREC[args.precision])
+    sim = make_sim(p, args.precision)
     sim.set_pipeline(args.pipeline, args.tile_y, args.kchunk, args.cells_per_thread)
     sim.set_stream(stream.cuda_stream)
     sim.add_source(src)
@@ -397,7 +411,7 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         host = [torch.zeros(cells, dtype=torch.float64).pin_memory().numpy() for _ in range(6)]
-        s = FDTD(p, COURANT_DT, PREC[args.precision])
+        s = make_sim(p, args.precision)
         s.set_pipeline(args.pipeline, args.tile_y, args.kchunk, args.cells_per_thread)
         if tuned:
             s.autotune(reuse=True)  # the shape chosen above (cached)
@@ -429,7 +443,7 @@ def run_ours(args):
     acc = None
     if not args.no_accuracy and rank == 0:
         a = FDTD(p, COURANT_DT, Precision.FP64)
-        b = FDTD(p, COURANT_DT, PREC[args.precision])
+        b = make_sim(p, args.precision)
         b.set_pipeline(args.pipeline, args.tile_y, args.kchunk, args.cells_per_thread)
         for x in (a, b):
             x.add_source(src)

@@ -81,6 +81,7 @@ SIGNATURES = {
     "fdtd_copy_field_to_host": [_H, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t],
     "fdtd_copy_field_from_host": [_H, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t],
     "fdtd_add_source": [_H, ctypes.POINTER(Source), ctypes.POINTER(ctypes.c_int)],
+    "fdtd_export_field": [_H, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p],
     "fdtd_clear_sources": [_H],
     "fdtd_get_step": [_H, ctypes.POINTER(ctypes.c_int64)],
     "fdtd_set_step": [_H, ctypes.c_int64],

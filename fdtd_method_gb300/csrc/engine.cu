@@ -565,6 +565,16 @@ int fdtd_copy_field_to_host(fdtd_handle* h, int comp, double* host, size_t n) {
   return FDTD_OK;
 }
 
+int fdtd_export_field(fdtd_handle* h, int comp, int64_t offset, int64_t count, double* device_dst) {
+  if (int rc = check_handle(h)) return rc;
+  if (comp < FDTD_EX || comp > FDTD_BZ) return fail(FDTD_ERR_LOGIC, "ERROR: Invalid field component");
+  if (!device_dst || offset < 0 || count < 0 || offset + count > h->g.cells)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "export range outside the grid");
+  DeviceGuard dg(h->device);
+  FDTD_CUDA(launch_export(h->view(), comp, device_dst, offset, count, h->stream), "export field");
+  return FDTD_OK;
+}
+
 int fdtd_copy_field_from_host(fdtd_handle* h, int comp, const double* host, size_t n) {
   if (int rc = check_handle(h)) return rc;
   if (comp < FDTD_EX || comp > FDTD_JZ) return fail(FDTD_ERR_LOGIC, "ERROR: Invalid field component");

@@ -253,6 +253,13 @@ class FDTD:
             raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "expected %d values, got %d" % (n, a.size))
         _lib.check(self._lib.fdtd_copy_field_from_host(self._handle(), int(comp), a.ctypes.data, n))
 
+    def export_field(self, comp, offset, count, device_ptr):
+        """FP64 values of E/B component `comp` at flat cells offset ..
+        offset+count-1 into device memory at `device_ptr` (asynchronous on the
+        solver's stream; synchronize() before reading them elsewhere)."""
+        _lib.check(self._lib.fdtd_export_field(self._handle(), int(comp), int(offset), int(count),
+                                               ctypes.c_void_p(int(device_ptr))))
+
     def add_source(self, src):
         c, keep = src.to_c()
         idx = ctypes.c_int()

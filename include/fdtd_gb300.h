@@ -142,6 +142,12 @@ int fdtd_get_field(fdtd_handle* h, int comp, double** device_ptr);
 int fdtd_copy_field_to_host(fdtd_handle* h, int comp, double* host, size_t n);
 int fdtd_copy_field_from_host(fdtd_handle* h, int comp, const double* host, size_t n);
 
+/* New: FP64 values of the E/B component `comp` at the flat cells
+ * offset .. offset+count-1 (any storage form), written into device memory at
+ * device_dst.  Asynchronous on the handle's stream (device-side diagnostics
+ * and comparisons; no host copy). */
+int fdtd_export_field(fdtd_handle* h, int comp, int64_t offset, int64_t count, double* device_dst);
+
 /* Registers a separable current source (see fdtd_source); returns its index
  * through *index if non-null.  Sources replace the reference sample driver's
  * per-step SetCurrent kernel (perf-tests/kokkos_sample/kokkos_sample.cpp:88-129). */
