@@ -310,8 +310,8 @@ int ensure_alt(fdtd_handle* h) {
     const int lbw = two ? fused_lo_box_width() : fused1_lo_box_width();
     LoT* const* lo_cur = h->form == Form::F32C ? h->lo : nullptr;
     LoT* const* lo_alt = h->form == Form::F32C ? h->alt_lo : nullptr;
-    if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, lbw, h->fused_cfg.tile_y) != cudaSuccess ||
-        build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, h->fused_cfg.tile_y) != cudaSuccess)
+    if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, lbw, h->fused_cfg.tile_y, !two) != cudaSuccess ||
+        build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, h->fused_cfg.tile_y, !two) != cudaSuccess)
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
     if (!two && (build_tma_store_maps(&h->smaps_cur, h->L, ht, h->field, lo_cur, h->fused_cfg.tile_y) != cudaSuccess ||
                  build_tma_store_maps(&h->smaps_alt, h->L, ht, h->alt_field, lo_alt, h->fused_cfg.tile_y) != cudaSuccess))

@@ -102,8 +102,10 @@ enum class HiType { F32, F16 };
 // margins excluded), box 32 x tile_y.
 cudaError_t build_tma_store_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], LoT* const lo[6],
                                  int tile_y);
+// trimmed (the one-cell-per-thread kernel): boxes of components other than
+// Bx and Bz are one row shorter (they start at the tile's first row).
 cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6],
-                           LoT* const lo[6], int box_w, int lo_box_w, int tile_y);
+                           LoT* const lo[6], int box_w, int lo_box_w, int tile_y, bool trimmed);
 
 // misc.cu — conversions, diagnostics, small helpers.
 enum class Form { F64 = 0, F32 = 1, F32C = 2, F16 = 3 };

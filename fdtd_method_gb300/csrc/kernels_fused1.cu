@@ -38,6 +38,8 @@
 #include "sources.cuh"
 #include "tma.cuh"
 
+#include <type_traits>
+
 namespace fdtd {
 
 template <class S> struct ArithOf1 { using type = ArithPlain; };
@@ -53,10 +55,64 @@ template <> struct Box1<StoreF16> { static constexpr int kW = 48, kOff = 8, kLoW
 
 constexpr int round128(int b) { return (b + 127) / 128 * 128; }
 
+// A field component as a compile-time constant, and a loop over the six.
+template <int c>
+using Comp = std::integral_constant<int, c>;
+template <class F>
+__device__ __forceinline__ void for_each_comp(F&& f) {
+  f(Comp<0>{});
+  f(Comp<1>{});
+  f(Comp<2>{});
+  f(Comp<3>{});
+  f(Comp<4>{});
+  f(Comp<5>{});
+}
+
 // CTAs per SM the register budget is sized for (30-row tiles: one
 // 1024-thread CTA; otherwise two).
 template <int RY>
 constexpr int kMinCtas1 = RY == 30 ? 1 : 2;
+
+// Ring-stage layout of the per-component tile boxes (see Plan1): byte offset
+// of each hi and lo box, box rows, first box row and x shift per component.
+// Computed once at compile time into a table, so that every shared-memory
+// offset in the kernel folds to an immediate.
+struct BoxTable {
+  int hi[7], lo[7];    // byte offsets ([6]: end of the hi / lo boxes)
+  int rows[6], row0[6], xoff[6], lxoff[6];
+  unsigned tx;         // bytes the six (twelve) copies write
+  int stage;           // stage size, 128-byte multiple
+};
+
+constexpr BoxTable box_table(int RY, int W, int LW, int HS, int LS, bool lo, int off, int lo_off) {
+  BoxTable b{};
+  int at = 0;
+  unsigned tx = 0;
+  for (int c = 0; c < 6; ++c) {
+    const bool below = (c == 3 || c == 5), left = (c == 4 || c == 5);
+    b.rows[c] = below ? RY + 2 : RY + 1;
+    b.row0[c] = below ? 0 : 1;
+    b.xoff[c] = left ? off : 0;
+    b.lxoff[c] = left ? lo_off : 0;
+  }
+  for (int c = 0; c < 6; ++c) {
+    b.hi[c] = at;
+    at = (at + b.rows[c] * W * HS + 127) / 128 * 128;
+    tx += (unsigned)(b.rows[c] * W * HS);
+  }
+  b.hi[6] = at;
+  for (int c = 0; c < 6; ++c) {
+    b.lo[c] = at;
+    if (lo) {
+      at = (at + b.rows[c] * LW * LS + 127) / 128 * 128;
+      tx += (unsigned)(b.rows[c] * LW * LS);
+    }
+  }
+  b.lo[6] = at;
+  b.tx = tx;
+  b.stage = at;
+  return b;
+}
 
 // Shared-memory plan (byte offsets).
 template <class S, int RY>
@@ -66,11 +122,23 @@ struct Plan1 {
   static constexpr int ROWS = RY + 2;
   static constexpr int W = Box1<S>::kW, LW = Box1<S>::kLoW, OFF = Box1<S>::kOff;
   static constexpr int HS = (int)sizeof(HiT), LS = (int)sizeof(LoT);
-  // ring stage: 6 hi boxes, then 6 lo boxes
-  static constexpr int kHiBox = ROWS * W * HS;
-  static constexpr int kLoBox = ROWS * LW * LS;
-  static constexpr uint32_t kTx = 6 * kHiBox + 6 * kLoBox;
-  static constexpr int kStage = round128(6 * kHiBox + 6 * kLoBox);
+  // Ring stage: 6 hi boxes, then 6 lo boxes.  Each component's box holds
+  // only the halos its stencil reads: the column left of the tile for By and
+  // Bz (E update, i-1), the row below for Bx and Bz (E update, j-1); every
+  // box holds the column right of the tile and the row above, where the
+  // halo warps compute E'.  Box row 0 is y0-1 for Bx, Bz and y0 otherwise
+  // (box row of thread row r: r - row0).  Every box starts on a 128-byte
+  // boundary, as tensor copies require.
+  // Per-component scalars of the table (device code may use scalar
+  // constants, not the table object).
+  static constexpr BoxTable box() { return box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1); }
+  template <int c> static constexpr int kHiAt = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).hi[c];
+  template <int c> static constexpr int kLoAt = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).lo[c];
+  template <int c> static constexpr int kRow0 = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).row0[c];
+  template <int c> static constexpr int kXOff = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).xoff[c];
+  template <int c> static constexpr int kLXOff = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).lxoff[c];
+  static constexpr uint32_t kTx = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).tx;
+  static constexpr int kStage = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).stage;
   // E' exchange / staging buffer: per component RY+2 rows of 32 (rows 0..RY-1
   // the tile, row RY the halo row, row RY+1 the halo column by row), hi words
   // then lo words.
@@ -88,6 +156,10 @@ struct Plan1 {
   static constexpr int kBar = kBst + 2 * kBBytes;
   static constexpr int kList = kBar + kStages1 * 8;
   static constexpr int kTotal = kList + 4 * (kMaxSources + 1);
+  static_assert(box().hi[1] % 128 == 0 && box().hi[5] % 128 == 0 && box().lo[0] % 128 == 0 &&
+                    box().lo[5] % 128 == 0,
+                "ring boxes must start on 128-byte boundaries");
+  static_assert(kStage % 128 == 0 && kTx <= (uint32_t)kStage, "ring stage layout");
   static_assert((kXComp * HS) % 128 == 0 && (kXComp * LS) % 128 == 0, "staging boxes must stay 128-byte aligned");
   static_assert((kBComp * HS) % 128 == 0 && (kBComp * LS) % 128 == 0, "staging boxes must stay 128-byte aligned");
 };
@@ -154,18 +226,23 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
   const int xo_up = (r == ny) ? RY * 32 + cx : r * 32 + cx;
   const int xo_right = (cx + 1 == nx) ? (RY + 1) * 32 + (r - 1) : (r - 1) * 32 + cx + 1;
   const int bo_own = (r - 1) * 32 + cx;
-  const int hi_own = r * P::W + cx + P::OFF;     // ring box offsets (elements)
-  const int lo_own = r * P::LW + cx + kLoOff1;
+  const int hi_own = r * P::W + cx;  // ring box element offsets, before each component's shifts
+  const int lo_own = r * P::LW + cx;
 
   auto issue = [&](int t) {
     const int slot = (slot0 + t - k0) % NS;
     const int kk = (t == L.Nk) ? 0 : t;
     unsigned char* base = smem + P::kRing + slot * P::kStage;
     mbar_arrive_expect_tx(&bar[slot], P::kTx);
-    for (int c = 0; c < 6; ++c) tma_load_3d(base + c * P::kHiBox, &maps.ld.hi[c], x0 + kPadX - P::OFF, y0, kk, &bar[slot]);
-    if (P::kLo)
-      for (int c = 0; c < 6; ++c)
-        tma_load_3d(base + 6 * P::kHiBox + c * P::kLoBox, &maps.ld.lo[c], x0 + kPadX - kLoOff1, y0, kk, &bar[slot]);
+    // (y coordinates are padded rows: logical row y0-1 is padded row y0)
+    for_each_comp([&](auto cc) {
+      constexpr int c = decltype(cc)::value;
+      tma_load_3d(base + P::template kHiAt<c>, &maps.ld.hi[c], x0 + kPadX - P::template kXOff<c>,
+                  y0 + P::template kRow0<c>, kk, &bar[slot]);
+      if (P::kLo)
+        tma_load_3d(base + P::template kLoAt<c>, &maps.ld.lo[c], x0 + kPadX - P::template kLXOff<c>,
+                    y0 + P::template kRow0<c>, kk, &bar[slot]);
+    });
   };
 
   if (leader)
@@ -206,19 +283,22 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
     mbar_wait_bounded(&bar[slot], phase, err);
     const unsigned char* stage = smem + P::kRing + slot * P::kStage;
     const HiT* H = reinterpret_cast<const HiT*>(stage) + hi_own;
-    const LoT* Q = reinterpret_cast<const LoT*>(stage + 6 * P::kHiBox) + lo_own;
+    const LoT* Q = reinterpret_cast<const LoT*>(stage) + lo_own;
     // component c at box offset (dr rows, dc columns) from this thread's cell
-    auto V = [&](int c, int dr, int dc) -> Pair {
-      const HiT h = H[c * P::ROWS * P::W + dr * P::W + dc];
-      const LoT q = P::kLo ? Q[c * P::ROWS * P::LW + dr * P::LW + dc] : LoT(0);
+    auto V = [&](auto cc, int dr, int dc) -> Pair {
+      constexpr int c = decltype(cc)::value;
+      const HiT h = H[P::template kHiAt<c> / P::HS + (dr - P::template kRow0<c>) * P::W + P::template kXOff<c> + dc];
+      const LoT q = P::kLo ? Q[P::template kLoAt<c> / P::LS + (dr - P::template kRow0<c>) * P::LW +
+                               P::template kLXOff<c> + dc]
+                           : LoT(0);
       return st.decode(c, h, q);
     };
 
     // 1. E'(t)
-    const Pair bx = V(3, 0, 0), by = V(4, 0, 0), bz = V(5, 0, 0);
-    Pair qx = A::curl(cs.ce[1], bz, V(5, -1, 0), cs.ce[2], by, pby);
-    Pair qy = A::curl(cs.ce[2], bx, pbx, cs.ce[0], bz, V(5, 0, -1));
-    Pair qz = A::curl(cs.ce[0], by, V(4, 0, -1), cs.ce[1], bx, V(3, -1, 0));
+    const Pair bx = V(Comp<3>{}, 0, 0), by = V(Comp<4>{}, 0, 0), bz = V(Comp<5>{}, 0, 0);
+    Pair qx = A::curl(cs.ce[1], bz, V(Comp<5>{}, -1, 0), cs.ce[2], by, pby);
+    Pair qy = A::curl(cs.ce[2], bx, pbx, cs.ce[0], bz, V(Comp<5>{}, 0, -1));
+    Pair qz = A::curl(cs.ce[0], by, V(Comp<4>{}, 0, -1), cs.ce[1], bx, V(Comp<3>{}, -1, 0));
     if (kDenseJ || kSrc) {
       // Current, accumulated per J component in registration order; only the
       // components that received current get the current term.
@@ -261,7 +341,7 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
       if (has & 2u) qy = A::add(qy, A::cur_term(cs.cj, jv[1]));
       if (has & 4u) qz = A::add(qz, A::cur_term(cs.cj, jv[2]));
     }
-    const Pair ax = A::acc(V(0, 0, 0), qx), ay = A::acc(V(1, 0, 0), qy), az = A::acc(V(2, 0, 0), qz);
+    const Pair ax = A::acc(V(Comp<0>{}, 0, 0), qx), ay = A::acc(V(Comp<1>{}, 0, 0), qy), az = A::acc(V(Comp<2>{}, 0, 0), qz);
     // E' in its stored words; the B update uses the value they hold.
     const HiT ehx = st.enc_hi(0, ax), ehy = st.enc_hi(1, ay), ehz = st.enc_hi(2, az);
     const LoT elx = st.enc_lo(ax), ely = st.enc_lo(ay), elz = st.enc_lo(az);
@@ -436,7 +516,7 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
   init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
   uint32_t ring = 0;
   fused1_tile<S, A, RY, kApps, kDenseJ, true>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z, kchunk, Jx, Jy,
-                                        Jz, ss, step, err, smem, ring);
+                                              Jz, ss, step, err, smem, ring);
   if (threadIdx.x == 0 && threadIdx.y == 0) bulk_wait_all();
 }
 
@@ -478,8 +558,9 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
       if (Plan1<S, RY>::kLo || (q < 6 || (q >= 12 && q < 18))) prefetch_tensormap(tm);
     }
     __syncthreads();
-    fused1_tile<S, A, RY, kApps, false, false>(dom.L, dom.s[parity], dom.s[parity ^ 1], maps[2 * w.x + parity], dom.cs, w.y,
-                                        w.z, w.w, kchunk, nullptr, nullptr, nullptr, dom.ss, step, err, smem, ring);
+    fused1_tile<S, A, RY, kApps, false, false>(dom.L, dom.s[parity], dom.s[parity ^ 1], maps[2 * w.x + parity], dom.cs,
+                                               w.y, w.z, w.w, kchunk, nullptr, nullptr, nullptr, dom.ss, step, err, smem,
+                                               ring);
     __syncthreads();
   }
   if (leader) {

@@ -80,14 +80,16 @@ cudaError_t build_tma_store_maps(void* maps, const PLayout& L, HiType ht, void* 
 }
 
 cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], LoT* const lo[6],
-                           int box_w, int lo_box_w, int tile_y) {
+                           int box_w, int lo_box_w, int tile_y, bool trimmed) {
   TmaMaps* m = static_cast<TmaMaps*>(maps);
   std::memset(m, 0, sizeof(TmaMaps));
   const CUtensorMapDataType dt = ht == HiType::F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
   const size_t es = ht == HiType::F32 ? 4 : 2;
   for (int c = 0; c < 6; ++c) {
-    if (!encode(&m->hi[c], dt, es, hi[c], L, box_w, tile_y)) return cudaErrorInvalidValue;
-    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, sizeof(LoT), lo[c], L, lo_box_w, tile_y))
+    // trimmed: only Bx and Bz (components 3, 5) carry the row below the tile
+    const int ty = (trimmed && c != 3 && c != 5) ? tile_y - 1 : tile_y;
+    if (!encode(&m->hi[c], dt, es, hi[c], L, box_w, ty)) return cudaErrorInvalidValue;
+    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, sizeof(LoT), lo[c], L, lo_box_w, ty))
       return cudaErrorInvalidValue;
   }
   return cudaSuccess;
