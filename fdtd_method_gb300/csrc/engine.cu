@@ -277,6 +277,19 @@ struct TuneKey {
 std::mutex g_tune_mu;
 std::map<TuneKey, fdtd_tune_result> g_tune_cache;
 
+// Device address of a page-locked host buffer (nullptr for other memory).
+// The conversion kernels read and write such buffers directly, over the
+// host link, with no staging copy.
+double* device_alias(const double* host) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return static_cast<double*>(at.devicePointer);
+}
+
 int check_handle(fdtd_handle* h) {
   if (!h) return fail(FDTD_ERR_INVALID_ARGUMENT, "null handle");
   return FDTD_OK;
@@ -541,8 +554,16 @@ int fdtd_copy_field_to_host(fdtd_handle* h, int comp, double* host, size_t n) {
     std::memset(host, 0, sizeof(double) * n);
     return FDTD_OK;
   }
-  if (int rc = ensure_staging(h)) return rc;
   StateView v = h->view();
+  if (comp < FDTD_JX) {
+    if (double* dev = device_alias(host)) {
+      // pinned host memory the device addresses: convert in one pass
+      FDTD_CUDA(launch_export(v, comp, dev, 0, (int64_t)n, h->stream), "copy field to host");
+      FDTD_CUDA(cudaStreamSynchronize(h->stream), "copy field to host");
+      return FDTD_OK;
+    }
+  }
+  if (int rc = ensure_staging(h)) return rc;
   for (int64_t off = 0; off < (int64_t)n; off += kStagingElems) {
     const int64_t m = std::min<int64_t>(kStagingElems, (int64_t)n - off);
     cudaError_t e;
@@ -586,6 +607,14 @@ int fdtd_copy_field_from_host(fdtd_handle* h, int comp, const double* host, size
     FDTD_CUDA(cudaStreamSynchronize(h->stream), "copy field from host");
     if (comp >= FDTD_JX) h->dense_j = true;
     return FDTD_OK;
+  }
+  if (comp < FDTD_JX) {
+    if (double* dev = device_alias(host)) {
+      // pinned host memory the device addresses: convert in one pass
+      FDTD_CUDA(launch_import(h->view(), comp, dev, 0, (int64_t)n, h->stream), "copy field from host");
+      FDTD_CUDA(cudaStreamSynchronize(h->stream), "copy field from host");
+      return FDTD_OK;
+    }
   }
   if (int rc = ensure_staging(h)) return rc;
   if (comp >= FDTD_JX) {

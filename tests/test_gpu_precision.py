@@ -62,6 +62,31 @@ def fp64_pulse():
     return p, src, fields(s), s.energy()
 
 
+@pytest.mark.parametrize("prec", [Precision.FP32, Precision.FP32_COMP, Precision.FP16_SCALED])
+def test_pinned_host_buffers_match_pageable(prec):
+    """Page-locked host buffers are converted in place by the device (no
+    staging copy); the values must equal the staged path's, both ways."""
+    torch = pytest.importorskip("torch")
+    p = normalised_parameters(45, 21, 13)
+    rng = np.random.default_rng(11)
+    vals = [rng.standard_normal(p.cells) for _ in range(6)]
+    a = FDTD(p, COURANT_DT, prec)
+    b = FDTD(p, COURANT_DT, prec)
+    for s_ in (a, b):
+        if prec == Precision.FP16_SCALED:
+            s_.set_fp16_exponents([6] * 6)
+    pinned = [torch.from_numpy(v).pin_memory() for v in vals]
+    for c in range(6):
+        a.copy_from_host(c, vals[c])
+        b.copy_from_host(c, pinned[c].numpy())
+    a.step(3)
+    b.step(3)
+    for c in range(6):
+        out = torch.zeros(p.cells, dtype=torch.float64).pin_memory()
+        b.copy_to_host(c, out.numpy())
+        np.testing.assert_array_equal(out.numpy(), a.get_field(c).numpy())
+
+
 @pytest.mark.parametrize("prec,bar", [(Precision.FP32, 1e-5), (Precision.FP32_COMP, 1e-5),
                                       (Precision.FP16_SCALED, 5e-2)])
 def test_pulse_rel_l2_vs_fp64(fp64_pulse, prec, bar):
