@@ -18,6 +18,8 @@
  *   parameter validation      src/FDTD_kokkos/FDTD_kokkos.cpp:7-12
  *   update_fields = B/2,E,B/2 src/FDTD_kokkos/FDTD_kokkos.cpp:91-104
  *   current box source        perf-tests/kokkos_sample/kokkos_sample.cpp:88-129
+ *   PML (split-field layer)   src/FDTD_kokkos/FDTD_PML_kokkos.cpp:22-189,
+ *                             include/FDTD_kokkos/kokkos_functors.h:154-415
  *
  * Arithmetic is written in the reference's evaluation order and must be built
  * with -ffp-contract=off so that no multiply-add is fused (the reference's
@@ -97,18 +99,22 @@ static inline long wrap(long i, long N) {
     return (N - 1) * minus_one + i * !(minus_one || at_n);
 }
 
-/* include/FDTD_kokkos/kokkos_functors.h:128-151 over the whole grid. */
-void oracle_update_B(long Ni, long Nj, long Nk,
-                     const double* Ex, const double* Ey, const double* Ez,
-                     double* Bx, double* By, double* Bz,
-                     double cx, double cy, double cz) {
+/* A box of cells [i0,i1) x [j0,j1) x [k0,k1): the ranges the reference's
+ * functors take (kokkos_functors.h:45-63 and :109-127). */
+typedef struct { long i0, i1, j0, j1, k0, k1; } oracle_box;
+
+/* include/FDTD_kokkos/kokkos_functors.h:128-151 over a box. */
+void oracle_update_B_box(long Ni, long Nj, long Nk, oracle_box b,
+                         const double* Ex, const double* Ey, const double* Ez,
+                         double* Bx, double* By, double* Bz,
+                         double cx, double cy, double cz) {
     const long plane = Ni * Nj;
 #pragma omp parallel for schedule(static)
-    for (long k = 0; k < Nk; ++k) {
+    for (long k = b.k0; k < b.k1; ++k) {
         const long kn = wrap(k + 1, Nk);
-        for (long j = 0; j < Nj; ++j) {
+        for (long j = b.j0; j < b.j1; ++j) {
             const long jn = wrap(j + 1, Nj);
-            for (long i = 0; i < Ni; ++i) {
+            for (long i = b.i0; i < b.i1; ++i) {
                 const long in = wrap(i + 1, Ni);
                 const long idx = i + j * Ni + k * plane;
                 const long i_n = in + j * Ni + k * plane;
@@ -122,20 +128,29 @@ void oracle_update_B(long Ni, long Nj, long Nk,
     }
 }
 
-/* include/FDTD_kokkos/kokkos_functors.h:64-90 over the whole grid.  A null
- * J pointer set means J == 0 (the term cJ*0 = -0 leaves every sum unchanged). */
-void oracle_update_E(long Ni, long Nj, long Nk,
-                     const double* Bx, const double* By, const double* Bz,
-                     const double* Jx, const double* Jy, const double* Jz,
-                     double* Ex, double* Ey, double* Ez,
-                     double cJ, double cx, double cy, double cz) {
+/* The same over the whole grid. */
+void oracle_update_B(long Ni, long Nj, long Nk,
+                     const double* Ex, const double* Ey, const double* Ez,
+                     double* Bx, double* By, double* Bz,
+                     double cx, double cy, double cz) {
+    const oracle_box all = {0, Ni, 0, Nj, 0, Nk};
+    oracle_update_B_box(Ni, Nj, Nk, all, Ex, Ey, Ez, Bx, By, Bz, cx, cy, cz);
+}
+
+/* include/FDTD_kokkos/kokkos_functors.h:64-90 over a box.  A null J pointer
+ * set means J == 0 (the term cJ*0 = -0 leaves every sum unchanged). */
+void oracle_update_E_box(long Ni, long Nj, long Nk, oracle_box b,
+                         const double* Bx, const double* By, const double* Bz,
+                         const double* Jx, const double* Jy, const double* Jz,
+                         double* Ex, double* Ey, double* Ez,
+                         double cJ, double cx, double cy, double cz) {
     const long plane = Ni * Nj;
 #pragma omp parallel for schedule(static)
-    for (long k = 0; k < Nk; ++k) {
+    for (long k = b.k0; k < b.k1; ++k) {
         const long kp = wrap(k - 1, Nk);
-        for (long j = 0; j < Nj; ++j) {
+        for (long j = b.j0; j < b.j1; ++j) {
             const long jp = wrap(j - 1, Nj);
-            for (long i = 0; i < Ni; ++i) {
+            for (long i = b.i0; i < b.i1; ++i) {
                 const long ip = wrap(i - 1, Ni);
                 const long idx = i + j * Ni + k * plane;
                 const long i_p = ip + j * Ni + k * plane;
@@ -150,6 +165,16 @@ void oracle_update_E(long Ni, long Nj, long Nk,
             }
         }
     }
+}
+
+/* The same over the whole grid. */
+void oracle_update_E(long Ni, long Nj, long Nk,
+                     const double* Bx, const double* By, const double* Bz,
+                     const double* Jx, const double* Jy, const double* Jz,
+                     double* Ex, double* Ey, double* Ez,
+                     double cJ, double cx, double cy, double cz) {
+    const oracle_box all = {0, Ni, 0, Nj, 0, Nk};
+    oracle_update_E_box(Ni, Nj, Nk, all, Bx, By, Bz, Jx, Jy, Jz, Ex, Ey, Ez, cJ, cx, cy, cz);
 }
 
 /* Adds every active source's contribution for time step `step` into the three
@@ -235,6 +260,182 @@ void oracle_run_driver(long Ni, long Nj, long Nk, double* f[9], const double coe
         oracle_update_E(Ni, Nj, Nk, f[3], f[4], f[5], J[0], J[1], J[2], f[0], f[1], f[2],
                         coef[6], coef[0], coef[1], coef[2]);
         oracle_update_B(Ni, Nj, Nk, f[0], f[1], f[2], f[3], f[4], f[5], coef[3], coef[4], coef[5]);
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * PML: the reference's split-field absorbing layer (class FDTD_PML).
+ *
+ * Layer thickness per axis: (int)(N * pml_percent) cells at both ends
+ * (FDTD_PML_kokkos.cpp:71-73).  The conductivity of an axis depends only on
+ * the distance d (in cells) into the layer: sigma = SGm * (d / pml)^4 with
+ * SGm = -(4 + 1)/2 * ln(R) / (pml * dx) and R = 1e-12
+ * (FDTD_PML_kokkos.cpp:108-116, :132-136, kokkos_functors.h:182-189); the
+ * distance is pml - i in the lower layer and i + 1 + pml - N in the upper one
+ * (FDTD_PML_kokkos.cpp:109-127), and sigma is zero outside the layer (the
+ * reference leaves those cells unset: its first touch is commented out,
+ * FDTD_PML_kokkos.cpp:47-69; zero is what its arrays hold on a fresh
+ * allocation).  E and B use the same conductivity.
+ *
+ * The split fields Exy, Exz, Eyx, Eyz, Ezx, Ezy, Bxy, Bxz, Byx, Byz, Bzx, Bzy
+ * start at zero and live on the whole grid (as the reference's arrays). */
+#define ORACLE_PML_N 4.0
+#define ORACLE_PML_R 1e-12
+
+/* Layer thickness of each axis. */
+void oracle_pml_sizes(const oracle_params* p, double pml_percent, int pml[3]) {
+    pml[0] = (int)((double)p->Ni * pml_percent);
+    pml[1] = (int)((double)p->Nj * pml_percent);
+    pml[2] = (int)((double)p->Nk * pml_percent);
+}
+
+/* Conductivity profile of one axis of n cells with a layer of `pml` cells and
+ * spacing d: sig[0..n-1] (zero outside the two layers). */
+static void pml_sigma_axis(long n, int pml, double d, double* sig) {
+    for (long i = 0; i < n; ++i) sig[i] = 0.0;
+    if (pml <= 0) return;
+    const double sgm = -(ORACLE_PML_N + 1.0) / 2.0 * log(ORACLE_PML_R) / ((double)pml * d);
+    for (long i = 0; i < pml; ++i)
+        sig[i] = sgm * pow((double)(pml - i) / (double)pml, ORACLE_PML_N);
+    for (long i = n - pml; i < n; ++i)
+        sig[i] = sgm * pow((double)(i + 1 + pml - n) / (double)pml, ORACLE_PML_N);
+}
+
+void oracle_pml_sigma(const oracle_params* p, double pml_percent, double* sx, double* sy, double* sz) {
+    int pml[3];
+    oracle_pml_sizes(p, pml_percent, pml);
+    pml_sigma_axis(p->Ni, pml[0], p->dx, sx);
+    pml_sigma_axis(p->Nj, pml[1], p->dy, sy);
+    pml_sigma_axis(p->Nk, pml[2], p->dz, sz);
+}
+
+/* kokkos_functors.h:211-213 (decay over one step) and the curl coefficient
+ * of :279-292 / :375-388. */
+static inline double pml_decay(double sigma, double dt) { return exp(-sigma * dt * ORACLE_C); }
+static inline double pml_coef2(double sigma, double dt, double d) {
+    if (sigma != 0.0) return (1.0 - pml_decay(sigma, dt)) / (sigma * d);
+    return ORACLE_C * dt / d;
+}
+
+/* kokkos_functors.h:261-309: split-field E update over a box. */
+static void pml_update_E(long Ni, long Nj, long Nk, oracle_box b, double* f[9], double* s[12],
+                         const double* sig[3], double dt, double dx, double dy, double dz) {
+    const long plane = Ni * Nj;
+    double *Ex = f[0], *Ey = f[1], *Ez = f[2];
+    const double *Bx = f[3], *By = f[4], *Bz = f[5];
+    double *Exy = s[0], *Exz = s[1], *Eyx = s[2], *Eyz = s[3], *Ezx = s[4], *Ezy = s[5];
+#pragma omp parallel for schedule(static)
+    for (long k = b.k0; k < b.k1; ++k) {
+        const long kp = wrap(k - 1, Nk);
+        for (long j = b.j0; j < b.j1; ++j) {
+            const long jp = wrap(j - 1, Nj);
+            for (long i = b.i0; i < b.i1; ++i) {
+                const long ip = wrap(i - 1, Ni);
+                const long idx = i + j * Ni + k * plane;
+                const long i_p = ip + j * Ni + k * plane;
+                const long j_p = i + jp * Ni + k * plane;
+                const long k_p = i + j * Ni + kp * plane;
+                const double c2x = pml_coef2(sig[0][i], dt, dx);
+                const double c2y = pml_coef2(sig[1][j], dt, dy);
+                const double c2z = pml_coef2(sig[2][k], dt, dz);
+                const double ax = pml_decay(sig[0][i], dt), ay = pml_decay(sig[1][j], dt),
+                             az = pml_decay(sig[2][k], dt);
+                Eyx[idx] = Eyx[idx] * ax - c2x * (Bz[idx] - Bz[i_p]);
+                Ezx[idx] = Ezx[idx] * ax + c2x * (By[idx] - By[i_p]);
+                Exy[idx] = Exy[idx] * ay + c2y * (Bz[idx] - Bz[j_p]);
+                Ezy[idx] = Ezy[idx] * ay - c2y * (Bx[idx] - Bx[j_p]);
+                Exz[idx] = Exz[idx] * az - c2z * (By[idx] - By[k_p]);
+                Eyz[idx] = Eyz[idx] * az + c2z * (Bx[idx] - Bx[k_p]);
+                Ex[idx] = Exz[idx] + Exy[idx];
+                Ey[idx] = Eyx[idx] + Eyz[idx];
+                Ez[idx] = Ezy[idx] + Ezx[idx];
+            }
+        }
+    }
+}
+
+/* kokkos_functors.h:357-405: split-field B update over a box. */
+static void pml_update_B(long Ni, long Nj, long Nk, oracle_box b, double* f[9], double* s[12],
+                         const double* sig[3], double dt, double dx, double dy, double dz) {
+    const long plane = Ni * Nj;
+    const double *Ex = f[0], *Ey = f[1], *Ez = f[2];
+    double *Bx = f[3], *By = f[4], *Bz = f[5];
+    double *Bxy = s[6], *Bxz = s[7], *Byx = s[8], *Byz = s[9], *Bzx = s[10], *Bzy = s[11];
+#pragma omp parallel for schedule(static)
+    for (long k = b.k0; k < b.k1; ++k) {
+        const long kn = wrap(k + 1, Nk);
+        for (long j = b.j0; j < b.j1; ++j) {
+            const long jn = wrap(j + 1, Nj);
+            for (long i = b.i0; i < b.i1; ++i) {
+                const long in = wrap(i + 1, Ni);
+                const long idx = i + j * Ni + k * plane;
+                const long i_n = in + j * Ni + k * plane;
+                const long j_n = i + jn * Ni + k * plane;
+                const long k_n = i + j * Ni + kn * plane;
+                const double c2x = pml_coef2(sig[0][i], dt, dx);
+                const double c2y = pml_coef2(sig[1][j], dt, dy);
+                const double c2z = pml_coef2(sig[2][k], dt, dz);
+                const double ax = pml_decay(sig[0][i], dt), ay = pml_decay(sig[1][j], dt),
+                             az = pml_decay(sig[2][k], dt);
+                Byx[idx] = Byx[idx] * ax + c2x * (Ez[i_n] - Ez[idx]);
+                Bzx[idx] = Bzx[idx] * ax - c2x * (Ey[i_n] - Ey[idx]);
+                Bxy[idx] = Bxy[idx] * ay - c2y * (Ez[j_n] - Ez[idx]);
+                Bzy[idx] = Bzy[idx] * ay + c2y * (Ex[j_n] - Ex[idx]);
+                Bxz[idx] = Bxz[idx] * az + c2z * (Ey[k_n] - Ey[idx]);
+                Byz[idx] = Byz[idx] * az - c2z * (Ex[k_n] - Ex[idx]);
+                Bx[idx] = Bxy[idx] + Bxz[idx];
+                By[idx] = Byz[idx] + Byx[idx];
+                Bz[idx] = Bzx[idx] + Bzy[idx];
+            }
+        }
+    }
+}
+
+/* The six layer slabs of FDTD_PML::update_fields (FDTD_PML_kokkos.cpp:170-186):
+ * they tile everything outside the main box exactly once. */
+void oracle_pml_slabs(long Ni, long Nj, long Nk, const int pml[3], oracle_box out[6]) {
+    const long pi = pml[0], pj = pml[1], pk = pml[2];
+    const oracle_box s[6] = {
+        {0, Ni - pi, 0, Nj, 0, pk},             /* part_from_start i, all j, lower k */
+        {pi, Ni - pi, 0, pj, pk, Nk - pk},      /* main i, lower j, main k           */
+        {0, pi, 0, Nj, pk, Nk},                 /* lower i, all j, part_from_end k   */
+        {pi, Ni, 0, Nj, Nk - pk, Nk},           /* part_from_end i, all j, upper k   */
+        {pi, Ni - pi, Nj - pj, Nj, pk, Nk - pk},/* main i, upper j, main k           */
+        {Ni - pi, Ni, 0, Nj, 0, Nk - pk}};      /* upper i, all j, part_from_start k */
+    for (int q = 0; q < 6; ++q) out[q] = s[q];
+}
+
+/* FDTD_PML::update_fields (FDTD_PML_kokkos.cpp:162-189) repeated `steps` times:
+ * B/2 on the main box; the split-field B update on the six slabs (a whole
+ * step: its coefficient is c dt/d); E on the main box (with current); the
+ * split-field E update on the slabs; B/2 on the main box.  f as in oracle_run
+ * (f[6..8] may be null); split = the twelve split fields; sig = the three
+ * conductivity profiles (oracle_pml_sigma).  Sources as in oracle_run. */
+void oracle_pml_run(long Ni, long Nj, long Nk, double* f[9], const double coef[7], const int pml[3],
+                    const double* sig[3], double dt, double dx, double dy, double dz, double* split[12],
+                    const oracle_source* src, int nsrc, long step0, int steps, double* jwork[3]) {
+    const long n = Ni * Nj * Nk;
+    const oracle_box main_box = {pml[0], Ni - pml[0], pml[1], Nj - pml[1], pml[2], Nk - pml[2]};
+    oracle_box slab[6];
+    oracle_pml_slabs(Ni, Nj, Nk, pml, slab);
+    for (int s = 0; s < steps; ++s) {
+        const double* J[3] = {f[6], f[7], f[8]};
+        if (nsrc > 0) {
+            for (int c = 0; c < 3; ++c) {
+                if (f[6 + c]) memcpy(jwork[c], f[6 + c], sizeof(double) * n);
+                else memset(jwork[c], 0, sizeof(double) * n);
+            }
+            oracle_add_sources(Ni, Nj, Nk, jwork, src, nsrc, step0 + s);
+            J[0] = jwork[0];
+            J[1] = jwork[1];
+            J[2] = jwork[2];
+        }
+        oracle_update_B_box(Ni, Nj, Nk, main_box, f[0], f[1], f[2], f[3], f[4], f[5], coef[3], coef[4], coef[5]);
+        for (int q = 0; q < 6; ++q) pml_update_B(Ni, Nj, Nk, slab[q], f, split, sig, dt, dx, dy, dz);
+        oracle_update_E_box(Ni, Nj, Nk, main_box, f[3], f[4], f[5], J[0], J[1], J[2], f[0], f[1], f[2],
+                            coef[6], coef[0], coef[1], coef[2]);
+        for (int q = 0; q < 6; ++q) pml_update_E(Ni, Nj, Nk, slab[q], f, split, sig, dt, dx, dy, dz);
+        oracle_update_B_box(Ni, Nj, Nk, main_box, f[0], f[1], f[2], f[3], f[4], f[5], coef[3], coef[4], coef[5]);
     }
 }
 

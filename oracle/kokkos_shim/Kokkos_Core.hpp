@@ -59,9 +59,16 @@ class View<T*, Props...> {
  public:
   using value_type = T;
   View() = default;
+  // Every allocation is zero-filled, WithoutInitializing included.  The
+  // reference's PML class allocates its conductivity and split-field arrays
+  // without initialisation and reads them in cells it never sets
+  // (src/FDTD_kokkos/FDTD_PML_kokkos.cpp:47-69, first touch commented out);
+  // a zero fill gives those reads the values a fresh allocation holds, so the
+  // reference's results are defined and repeatable.
   View(const ViewAllocProp& prop, std::size_t n) : label_(prop.label), n_(n) {
     data_ = std::shared_ptr<T[]>(new T[n ? n : 1]);
-    if (prop.initialize) std::memset(data_.get(), 0, sizeof(T) * (n ? n : 1));
+    (void)prop.initialize;
+    std::memset(data_.get(), 0, sizeof(T) * (n ? n : 1));
   }
   View(const std::string& label, std::size_t n) : View(ViewAllocProp{label, true}, n) {}
   T& operator()(long i) const { return data_[i]; }

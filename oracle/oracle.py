@@ -1,7 +1,7 @@
 """ctypes access to the oracle (test infrastructure only).
 
 ``Oracle`` runs the C restatement in fdtd_oracle.c (each function there cites
-the reference file:line it restates).  ``RefKokkos`` drives the reference's own
+the reference file:line it restates); ``OraclePML`` its PML subclass.  ``RefKokkos`` drives the reference's own
 FDTD_kokkos::FDTD compiled from its sources in oracle/_ref (present only where
 the reference checkout was available to build it).
 """
@@ -59,6 +59,16 @@ def oracle_lib():
         lib.oracle_run_driver.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.POINTER(_D), _D,
                                           ctypes.POINTER(OracleSource), ctypes.c_int, ctypes.c_long, ctypes.c_int]
         lib.oracle_run_driver.restype = None
+        lib.oracle_pml_sizes.argtypes = [ctypes.POINTER(OracleParams), ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
+        lib.oracle_pml_sizes.restype = None
+        lib.oracle_pml_sigma.argtypes = [ctypes.POINTER(OracleParams), ctypes.c_double, _D, _D, _D]
+        lib.oracle_pml_sigma.restype = None
+        lib.oracle_pml_run.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.POINTER(_D), _D,
+                                       ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_D), ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(_D),
+                                       ctypes.POINTER(OracleSource), ctypes.c_int, ctypes.c_long, ctypes.c_int,
+                                       ctypes.POINTER(_D)]
+        lib.oracle_pml_run.restype = None
         lib.oracle_field_sums.argtypes = [ctypes.c_long, ctypes.POINTER(_D), _D]
         lib.oracle_field_sums.restype = None
         lib.oracle_threads.restype = ctypes.c_int
@@ -155,6 +165,45 @@ class Oracle:
         return field_sums(self.f[:6])
 
 
+def _cparams(params):
+    return OracleParams(params.Ni, params.Nj, params.Nk, params.ax, params.bx, params.ay, params.by,
+                        params.az, params.bz, params.dx, params.dy, params.dz)
+
+
+class OraclePML(Oracle):
+    """The reference's FDTD_PML (split-field absorbing layer of
+    (int)(N * pml_percent) cells at both ends of every axis), restated in C
+    (oracle_pml_run in fdtd_oracle.c)."""
+
+    def __init__(self, params, dt, pml_percent, with_current=True):
+        super().__init__(params, dt, with_current)
+        self.pml_percent = float(pml_percent)
+        cp = _cparams(params)
+        sizes = (ctypes.c_int * 3)()
+        oracle_lib().oracle_pml_sizes(ctypes.byref(cp), self.pml_percent, sizes)
+        self.pml = list(sizes)
+        self.sigma = [np.zeros(params.Ni), np.zeros(params.Nj), np.zeros(params.Nk)]
+        oracle_lib().oracle_pml_sigma(ctypes.byref(cp), self.pml_percent, *[_ptr(a) for a in self.sigma])
+        self.split = [np.zeros_like(self.f[0]) for _ in range(12)]
+
+    def step(self, n=1):
+        p = self.params
+        ptrs = (_D * 9)(*[(_ptr(a) if a is not None else _D()) for a in self.f])
+        csrc, keep = self._csources()
+        if self.sources and self._jwork is None:
+            self._jwork = [np.zeros_like(self.f[0]) for _ in range(3)]
+        jw = (_D * 3)(*([_ptr(a) for a in self._jwork] if self._jwork else [_D(), _D(), _D()]))
+        sig = (_D * 3)(*[_ptr(a) for a in self.sigma])
+        spl = (_D * 12)(*[_ptr(a) for a in self.split])
+        pml = (ctypes.c_int * 3)(*self.pml)
+        oracle_lib().oracle_pml_run(p.Ni, p.Nj, p.Nk, ptrs, _ptr(self.coef), pml, sig, self.dt, p.dx, p.dy, p.dz,
+                                    spl, csrc, len(self.sources), self.step_index, int(n), jw)
+        self.step_index += int(n)
+
+    def step_driver(self, n=1):
+        raise NotImplementedError("the PML oracle steps through step()")
+
+
 # ---------------------------------------------------------------------------
 # The reference itself (oracle/_ref), where it was built.
 
@@ -171,6 +220,9 @@ def ref_lib():
         lib.ref_kokkos_create.argtypes = [ctypes.POINTER(ctypes.c_int), _D, ctypes.c_double]
         lib.ref_kokkos_create.restype = ctypes.c_void_p
         lib.ref_kokkos_destroy.argtypes = [ctypes.c_void_p]
+        lib.ref_kokkos_pml_create.argtypes = [ctypes.POINTER(ctypes.c_int), _D, ctypes.c_double, ctypes.c_double]
+        lib.ref_kokkos_pml_create.restype = ctypes.c_void_p
+        lib.ref_kokkos_pml_destroy.argtypes = [ctypes.c_void_p]
         lib.ref_kokkos_update_fields.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.ref_kokkos_zeroed_currents.argtypes = [ctypes.c_void_p]
         lib.ref_kokkos_field.argtypes = [ctypes.c_void_p, ctypes.c_int, _D, ctypes.c_long, ctypes.c_int]
@@ -192,21 +244,28 @@ class RefKokkos:
     """FDTD_kokkos::FDTD from the reference's own sources (oracle/_ref).
     kind="kokkos" (the north-star path) or "openmp" (its OpenMP twin)."""
 
-    def __init__(self, params, dt, kind="kokkos"):
+    def __init__(self, params, dt, kind="kokkos", pml_percent=None):
         lib = ref_lib()
         self.kind = kind
+        self.pml = pml_percent is not None
         n = (ctypes.c_int * 3)(params.Ni, params.Nj, params.Nk)
         b = (ctypes.c_double * 9)(params.ax, params.bx, params.ay, params.by, params.az, params.bz,
                                   params.dx, params.dy, params.dz)
-        create = lib.ref_kokkos_create if kind == "kokkos" else lib.ref_omp_create
-        self.h = create(n, b, float(dt))
+        if self.pml:
+            self.h = lib.ref_kokkos_pml_create(n, b, float(dt), float(pml_percent))
+        else:
+            create = lib.ref_kokkos_create if kind == "kokkos" else lib.ref_omp_create
+            self.h = create(n, b, float(dt))
         if not self.h:
             raise ValueError(lib.ref_last_error().decode())
         self.n = params.Ni * params.Nj * params.Nk
 
     def close(self):
         if self.h:
-            (ref_lib().ref_kokkos_destroy if self.kind == "kokkos" else ref_lib().ref_omp_destroy)(self.h)
+            if self.pml:
+                ref_lib().ref_kokkos_pml_destroy(self.h)
+            else:
+                (ref_lib().ref_kokkos_destroy if self.kind == "kokkos" else ref_lib().ref_omp_destroy)(self.h)
             self.h = None
 
     def __del__(self):

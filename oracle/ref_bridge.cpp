@@ -6,12 +6,14 @@
 //
 // Wrapped reference interfaces:
 //   FDTD_kokkos::FDTD           include/FDTD_kokkos/FDTD_kokkos.h:7-36
+//   FDTD_kokkos::FDTD_PML       include/FDTD_kokkos/FDTD_PML_kokkos.h:10-33
 //   FDTD_openmp::FDTD           include/FDTD/FDTD.h:9-41      (REF_WITH_OPENMP_TWIN)
 //   run_test_kokkos             unit-tests/test_FDTD_method_kokkos.cpp:18-69
 #include <cstring>
 #include <exception>
 #include <string>
 
+#include "FDTD_PML_kokkos.h"
 #include "FDTD_kokkos.h"
 #ifdef REF_WITH_OPENMP_TWIN
 #include "FDTD.h"
@@ -46,6 +48,21 @@ void* ref_kokkos_create(const int* n, const double* b, double dt) {
   }
 }
 void ref_kokkos_destroy(void* h) { delete static_cast<FDTD_kokkos::FDTD*>(h); }
+
+// The PML subclass, handed out as its FDTD base (update_fields is virtual,
+// get_field is the base's); destroyed through its own type.
+void* ref_kokkos_pml_create(const int* n, const double* b, double dt, double pml_percent) {
+  try {
+    FDTD_kokkos::FDTD* base = new FDTD_kokkos::FDTD_PML(make_params(n, b), dt, pml_percent);
+    return base;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
+void ref_kokkos_pml_destroy(void* h) {
+  delete static_cast<FDTD_kokkos::FDTD_PML*>(static_cast<FDTD_kokkos::FDTD*>(h));
+}
 
 void ref_kokkos_update_fields(void* h, int steps) {
   auto* f = static_cast<FDTD_kokkos::FDTD*>(h);

@@ -15,6 +15,16 @@ CASES = {
 }
 
 
+# PML cases (FDTD_PML(Parameters, dt, pml_percent)); same domain and inputs
+PML_CASES = {
+    "pml_random_20x16x12_p20": {"n": (20, 16, 12), "steps": 6, "seed": 21, "comps": range(9), "pml": 0.2},
+    "pml_noJ_15x12x10_p25": {"n": (15, 12, 10), "steps": 8, "seed": 22, "comps": range(6), "pml": 0.25},
+    "pml_zero_8x8x8_p0": {"n": (8, 8, 8), "steps": 5, "seed": 23, "comps": range(9), "pml": 0.0},
+    "pml_flat_24x6x9_p15": {"n": (24, 6, 9), "steps": 7, "seed": 24, "comps": range(9), "pml": 0.15},
+    "pml_odd_11x13x7_p30": {"n": (11, 13, 7), "steps": 4, "seed": 25, "comps": range(9), "pml": 0.3},
+}
+
+
 def case_params(spec):
     from fdtd_method_gb300.fdtd import Parameters
     Ni, Nj, Nk = spec["n"]

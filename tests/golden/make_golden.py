@@ -11,6 +11,8 @@ unmodified against the host Kokkos stand-in.  Outputs:
                              seeds by `case_inputs`, exactly, on any host)
   reference_sample.json      stdout slices of the reference's kokkos_sample
                              program (perf-tests/kokkos_sample/kokkos_sample.cpp)
+  reference_pml_cases.npz    final E and B of small runs of FDTD_kokkos::FDTD_PML
+                             (src/FDTD_kokkos/FDTD_PML_kokkos.cpp) on seeded inputs
 
     python tests/golden/make_golden.py
 """
@@ -25,7 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from golden_inputs import CASES, case_inputs, case_params  # noqa: E402
+from golden_inputs import CASES, PML_CASES, case_inputs, case_params  # noqa: E402
 from oracle import RefKokkos, run_reference_unit_tests  # noqa: E402
 from oracle.oracle import REF_DIR  # noqa: E402
 
@@ -47,6 +49,18 @@ def main():
             out["%s/%d" % (name, comp)] = ref.get(comp)
         ref.close()
     np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **out)
+
+    out = {}
+    for name, spec in PML_CASES.items():
+        params, dt = case_params(spec)
+        ref = RefKokkos(params, dt, pml_percent=spec["pml"])
+        for comp, values in case_inputs(spec).items():
+            ref.set(comp, values)
+        ref.update_fields(spec["steps"])
+        for comp in range(6):
+            out["%s/%d" % (name, comp)] = ref.get(comp)
+        ref.close()
+    np.savez_compressed(os.path.join(HERE, "reference_pml_cases.npz"), **out)
 
     sample = {}
     for n, it in ((16, 60), (32, 100), (20, 30)):

@@ -7,8 +7,8 @@ import os
 import numpy as np
 import pytest
 
-from golden_inputs import CASES, case_inputs, case_params
-from oracle import Oracle, RefKokkos, coefficients, field_sums, ref_available
+from golden_inputs import CASES, PML_CASES, case_inputs, case_params
+from oracle import Oracle, OraclePML, RefKokkos, coefficients, field_sums, ref_available
 from refcases import CONVERGENCE_CASES, run_convergence
 
 from fdtd_method_gb300 import sources
@@ -147,3 +147,55 @@ def test_reference_rejects_what_oracle_rejects():
     r = RefKokkos(Parameters(2, 2, 2, 0, 1, 0, 1, 0, 1, 0.5, 0.5, 0.5), 1e-12)
     with pytest.raises(RuntimeError, match="Invalid field component"):
         r.get(9)
+
+
+PML_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_pml_cases.npz")
+
+
+@pytest.mark.parametrize("name", sorted(PML_CASES))
+def test_oracle_pml_matches_reference_golden_cases(name):
+    """The PML restatement against the reference's own FDTD_PML
+    (src/FDTD_kokkos/FDTD_PML_kokkos.cpp) on recorded runs, bit for bit."""
+    spec = PML_CASES[name]
+    params, dt = case_params(spec)
+    o = OraclePML(params, dt, spec["pml"])
+    for comp, values in case_inputs(spec).items():
+        o.set(comp, values)
+    o.step(spec["steps"])
+    golden = np.load(PML_GOLDEN)
+    for comp in range(6):
+        np.testing.assert_array_equal(o.get(comp), golden["%s/%d" % (name, comp)], err_msg="component %d" % comp)
+
+
+def test_oracle_pml_layer_profile():
+    """Layer thickness (int)(N * pml_percent) per axis; conductivity zero in
+    the main box, largest at the outer faces, symmetric (FDTD_PML_kokkos.cpp:71-136)."""
+    p = Parameters(20, 16, 12, 0.0, 1.0, 0.0, 2.0, 0.0, 3.0, 0.05, 0.125, 0.25)
+    o = OraclePML(p, 1e-13, 0.2)
+    assert o.pml == [4, 3, 2]
+    sx = o.sigma[0]
+    assert np.all(sx[4:16] == 0.0) and np.all(sx[:4] > 0.0) and np.all(sx[16:] > 0.0)
+    np.testing.assert_array_equal(sx[:4], sx[16:][::-1])
+    assert np.all(np.diff(sx[:4]) < 0)
+    o0 = OraclePML(p, 1e-13, 0.0)
+    assert o0.pml == [0, 0, 0] and not any(s.any() for s in o0.sigma)
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference build (oracle/_ref) not present on this host")
+@pytest.mark.parametrize("shape,pct", [((18, 14, 10), 0.2), ((9, 9, 9), 0.34), ((16, 1, 6), 0.25)])
+def test_oracle_pml_bitwise_equal_to_reference_build(shape, pct):
+    Ni, Nj, Nk = shape
+    p = Parameters(Ni, Nj, Nk, 0.0, 1.0, 0.0, 2.0, 0.0, 3.0, 1.0 / Ni, 2.0 / Nj, 3.0 / Nk)
+    dt = 0.3 * min(p.dx, p.dy, p.dz) / 3e10
+    rng = np.random.default_rng(Ni + 31 * Nj)
+    o = OraclePML(p, dt, pct)
+    r = RefKokkos(p, dt, pml_percent=pct)
+    for c in range(9):
+        v = rng.standard_normal(p.Ni * p.Nj * p.Nk)
+        o.set(c, v)
+        r.set(c, v)
+    o.step(5)
+    r.update_fields(5)
+    for c in range(6):
+        np.testing.assert_array_equal(o.get(c), r.get(c))
+    r.close()
