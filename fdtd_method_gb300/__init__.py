@@ -7,11 +7,11 @@ Amazingkivas/FDTD_Method, behind the reference solver class's API.
     sim.update_fields()
     ey = sim.get_field(Component.EY).numpy()
 """
-from .fdtd import (FDTD, FDTDBatch, Axis, Component, Const, CurrentParameters, Field, FDTDError,  # noqa: F401
+from .fdtd import (FDTD, FDTD_PML, FDTDBatch, Axis, Component, Const, CurrentParameters, Field, FDTDError,  # noqa: F401
                    InvalidArgument, LogicError, OutOfMemory, Parameters, Precision,
                    SelectedFields, SeparableSource)
 from . import sources  # noqa: F401
 
-__all__ = ["FDTD", "FDTDBatch", "Axis", "Component", "Const", "CurrentParameters", "Field", "FDTDError",
+__all__ = ["FDTD", "FDTD_PML", "FDTDBatch", "Axis", "Component", "Const", "CurrentParameters", "Field", "FDTDError",
            "InvalidArgument", "LogicError", "OutOfMemory", "Parameters", "Precision",
            "SelectedFields", "SeparableSource", "sources"]

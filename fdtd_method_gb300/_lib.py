@@ -74,6 +74,8 @@ SIGNATURES = {
     "fdtd_abi_version": [],
     "fdtd_create": [ctypes.POINTER(Params), ctypes.c_double, ctypes.c_int, ctypes.POINTER(_H)],
     "fdtd_destroy": [_H],
+    "fdtd_create_pml": [ctypes.POINTER(Params), ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.POINTER(_H)],
+    "fdtd_get_pml": [_H, ctypes.POINTER(ctypes.c_int)],
     "fdtd_update_fields": [_H],
     "fdtd_step": [_H, ctypes.c_int64],
     "fdtd_zeroed_currents": [_H],

@@ -39,6 +39,10 @@ int cuda_fail(cudaError_t e, const char* what) {
 // Speed of light and pi as the reference defines them (include/Constants.h:6,11).
 constexpr double kC = 3e10;
 constexpr double kPi = 3.14159265358;
+// PML constants of the reference (include/Constants.h:7,10): reflection R and
+// the order N of the conductivity profile.
+constexpr double kPmlR = 1e-12;
+constexpr double kPmlOrder = 4.0;
 
 constexpr int64_t kStagingElems = int64_t(1) << 24;  // 16 Mi doubles = 128 MiB
 constexpr int kMaxDiagBlocks = 152 * 8;
@@ -180,7 +184,7 @@ int run_b(fdtd_handle* h, int apps) {
   if (h->form == Form::F64) {
     Fp64Fields F;
     for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c];
-    e = launch_b_fp64(h->g, F, &h->coef[3], apps, h->stream);
+    e = launch_b_fp64(h->g, h->main_box(), F, &h->coef[3], apps, h->stream);
   } else {
     StateView v = h->view();
     switch (h->form) {
@@ -203,7 +207,7 @@ int run_e(fdtd_handle* h, int64_t step) {
   if (h->form == Form::F64) {
     Fp64Fields F;
     for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c];
-    e = launch_e_fp64(h->g, F, &h->coef[0], h->coef[6], h->dense_j, ss, step, h->stream);
+    e = launch_e_fp64(h->g, h->main_box(), F, &h->coef[0], h->coef[6], h->dense_j, ss, step, h->stream);
   } else {
     StateView v = h->view();
     const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
@@ -288,6 +292,39 @@ double* device_alias(const double* host) {
   }
   if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
   return static_cast<double*>(at.devicePointer);
+}
+
+// The six layer slabs of FDTD_PML::update_fields (FDTD_PML_kokkos.cpp:170-186),
+// which tile everything outside the main box exactly once.
+void pml_slabs(const fdtd_handle* h, Box out[6]) {
+  const int Ni = h->g.Ni, Nj = h->g.Nj, Nk = h->g.Nk;
+  const int pi = h->pml_size[0], pj = h->pml_size[1], pk = h->pml_size[2];
+  out[0] = Box{0, Ni - pi, 0, Nj, 0, pk};
+  out[1] = Box{pi, Ni - pi, 0, pj, pk, Nk - pk};
+  out[2] = Box{0, pi, 0, Nj, pk, Nk};
+  out[3] = Box{pi, Ni, 0, Nj, Nk - pk, Nk};
+  out[4] = Box{pi, Ni - pi, Nj - pj, Nj, pk, Nk - pk};
+  out[5] = Box{Ni - pi, Ni, 0, Nj, 0, Nk - pk};
+}
+
+// Split-field update of the layer: B (e = false) or E (e = true).
+int run_pml(fdtd_handle* h, bool e) {
+  Fp64Fields F;
+  for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c];
+  PmlFields P;
+  for (int q = 0; q < 12; ++q) P.split[q] = h->split[q];
+  for (int a = 0; a < 3; ++a) {
+    P.decay[a] = h->pml_decay[a];
+    P.coef2[a] = h->pml_coef2[a];
+  }
+  Box slab[6];
+  pml_slabs(h, slab);
+  for (int q = 0; q < 6; ++q) {
+    const cudaError_t err = e ? launch_e_pml_fp64(h->g, slab[q], F, P, h->stream)
+                              : launch_b_pml_fp64(h->g, slab[q], F, P, h->stream);
+    if (err != cudaSuccess) return cuda_fail(err, "PML update launch");
+  }
+  return FDTD_OK;
 }
 
 int check_handle(fdtd_handle* h) {
@@ -439,6 +476,72 @@ int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle
   return FDTD_OK;
 }
 
+int fdtd_create_pml(const fdtd_params* params, double dt, double pml_percent, int precision, fdtd_handle** out) {
+  if (!params || !out) return fail(FDTD_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (!(pml_percent >= 0.0 && pml_percent < 0.5))
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "pml_percent must be in [0, 0.5)");
+  if (precision != FDTD_PRECISION_FP64)
+    return fail(FDTD_ERR_UNSUPPORTED, "the PML layer runs in the FP64 form");
+  fdtd_handle* h = nullptr;
+  if (int rc = fdtd_create(params, dt, precision, &h)) return rc;
+  h->pml = true;
+  // src/FDTD_kokkos/FDTD_PML_kokkos.cpp:71-73
+  const int n[3] = {params->Ni, params->Nj, params->Nk};
+  const double d[3] = {params->dx, params->dy, params->dz};
+  for (int a = 0; a < 3; ++a) h->pml_size[a] = static_cast<int>(static_cast<double>(n[a]) * pml_percent);
+  int rc = FDTD_OK;
+  for (int q = 0; q < 12 && rc == FDTD_OK; ++q) {
+    cudaError_t e = dev_alloc(h, (void**)&h->split[q], sizeof(double) * h->g.cells);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->split[q], 0, sizeof(double) * h->g.cells, h->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "PML split fields");
+  }
+  for (int a = 0; a < 3 && rc == FDTD_OK; ++a) {
+    // Conductivity along axis a (FDTD_PML_kokkos.cpp:108-136 with
+    // kokkos_functors.h:182-189), zero inside; then the per-step decay and the
+    // curl coefficient of the split-field updates (kokkos_functors.h:211-213,
+    // :279-292), all in FP64 on the host as the reference evaluates them.
+    const int pml = h->pml_size[a];
+    std::vector<double> sigma(n[a], 0.0), decay(n[a]), coef2(n[a]);
+    if (pml > 0) {
+      const double sgm = -(kPmlOrder + 1.0) / 2.0 * std::log(kPmlR) / (static_cast<double>(pml) * d[a]);
+      for (int i = 0; i < pml; ++i)
+        sigma[i] = sgm * std::pow(static_cast<double>(pml - i) / static_cast<double>(pml), kPmlOrder);
+      for (int i = n[a] - pml; i < n[a]; ++i)
+        sigma[i] = sgm * std::pow(static_cast<double>(i + 1 + pml - n[a]) / static_cast<double>(pml), kPmlOrder);
+    }
+    for (int i = 0; i < n[a]; ++i) {
+      decay[i] = std::exp(-sigma[i] * dt * kC);
+      coef2[i] = sigma[i] != 0.0 ? (1.0 - std::exp(-sigma[i] * dt * kC)) / (sigma[i] * d[a]) : kC * dt / d[a];
+    }
+    cudaError_t e = dev_alloc(h, (void**)&h->pml_decay[a], sizeof(double) * n[a]);
+    if (e == cudaSuccess) e = dev_alloc(h, (void**)&h->pml_coef2[a], sizeof(double) * n[a]);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(h->pml_decay[a], decay.data(), sizeof(double) * n[a], cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(h->pml_coef2[a], coef2.data(), sizeof(double) * n[a], cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = cuda_fail(e, "PML tables");
+  }
+  if (rc == FDTD_OK) {
+    const cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "PML set-up");
+  }
+  if (rc != FDTD_OK) {
+    const std::string msg = g_last_error;
+    fdtd_destroy(h);
+    return fail(rc, msg);
+  }
+  *out = h;
+  return FDTD_OK;
+}
+
+int fdtd_get_pml(fdtd_handle* h, int sizes[3]) {
+  if (int rc = check_handle(h)) return rc;
+  if (!sizes) return fail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  for (int a = 0; a < 3; ++a) sizes[a] = h->pml_size[a];
+  return FDTD_OK;
+}
+
 int fdtd_destroy(fdtd_handle* h) {
   if (!h) return FDTD_OK;
   // Source buffers are not in `allocations` (they are replaced on update).
@@ -498,7 +601,14 @@ int fdtd_step(fdtd_handle* h, int64_t n) {
   if (int rc = run_b(h, 1)) return rc;
   for (int64_t s = 0; s < n; ++s) {
     const int apps = s + 1 < n ? 2 : 1;
-    if (fused) {
+    if (h->pml) {
+      // FDTD_PML::update_fields (FDTD_PML_kokkos.cpp:162-189): B/2 inside,
+      // B on the six layer slabs, E inside, E on the slabs, B/2 inside.
+      if (int rc = run_pml(h, false)) return rc;
+      if (int rc = run_e(h, h->host_step + s)) return rc;
+      if (int rc = run_pml(h, true)) return rc;
+      if (int rc = run_b(h, apps)) return rc;
+    } else if (fused) {
       if (int rc = run_fused(h, h->host_step + s, apps)) return rc;
     } else {
       if (int rc = run_e(h, h->host_step + s)) return rc;

@@ -31,11 +31,33 @@ struct FusedConfig {
   int cells_per_thread = 1;  // 1: 32-wide tiles (kernels_fused1.cu); 2: 64-wide, packed float2
 };
 
-// kernels_fp64.cu
-cudaError_t launch_b_fp64(const Grid& g, const Fp64Fields& F, const double cb[3], int applications,
-                          cudaStream_t st);
-cudaError_t launch_e_fp64(const Grid& g, const Fp64Fields& F, const double ce[3], double cJ,
+// A box of cells [i0,i1) x [j0,j1) x [k0,k1) (the ranges the reference's
+// functors take, kokkos_functors.h:45-63 and :109-127).
+struct Box {
+  int i0, i1, j0, j1, k0, k1;
+  __host__ __device__ bool empty() const { return i1 <= i0 || j1 <= j0 || k1 <= k0; }
+  static Box whole(const Grid& g) { return Box{0, g.Ni, 0, g.Nj, 0, g.Nk}; }
+};
+
+// kernels_fp64.cu: the FP64 sweeps over a box.
+cudaError_t launch_b_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const double cb[3],
+                          int applications, cudaStream_t st);
+cudaError_t launch_e_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const double ce[3], double cJ,
                           bool dense_j, const SourceSet& ss, int64_t step, cudaStream_t st);
+
+// kernels_pml.cu: the split-field layer updates (FP64) over a box.  split =
+// Exy, Exz, Eyx, Eyz, Ezx, Ezy, Bxy, Bxz, Byx, Byz, Bzx, Bzy; decay[a][n] =
+// exp(-sigma_a(n) c dt) and coef2[a][n] the curl coefficient along axis a,
+// tables on the device.
+struct PmlFields {
+  double* split[12];
+  const double* decay[3];
+  const double* coef2[3];
+};
+cudaError_t launch_e_pml_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const PmlFields& P,
+                              cudaStream_t st);
+cudaError_t launch_b_pml_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const PmlFields& P,
+                              cudaStream_t st);
 
 // kernels_f32.cu (padded layout)
 template <class S>

@@ -73,6 +73,19 @@ struct fdtd_handle {
 
   // Step pipeline of the FP32-arithmetic forms (FP64 always uses the split
   // sweeps, whose FP64 instruction count is the smallest).
+  // PML (FDTD_PML, src/FDTD_kokkos/FDTD_PML_kokkos.cpp): layer thickness per
+  // axis, the twelve split fields Exy, Exz, Eyx, Eyz, Ezx, Ezy, Bxy, Bxz, Byx,
+  // Byz, Bzx, Bzy, and the per-axis decay / curl-coefficient tables.
+  bool pml = false;
+  int pml_size[3] = {0, 0, 0};
+  double* split[12] = {nullptr};
+  double* pml_decay[3] = {nullptr};
+  double* pml_coef2[3] = {nullptr};
+  // The box the ordinary updates cover: the whole grid, or inside the layer.
+  Box main_box() const {
+    return Box{pml_size[0], g.Ni - pml_size[0], pml_size[1], g.Nj - pml_size[1], pml_size[2], g.Nk - pml_size[2]};
+  }
+
   int pipeline = FDTD_PIPELINE_AUTO;
   FusedConfig fused_cfg;
   PLayout L{};  // padded layout of the FP32-arithmetic forms

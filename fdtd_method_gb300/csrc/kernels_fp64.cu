@@ -26,17 +26,17 @@ namespace fdtd {
 // therefore the same t — the two additions stay separate, so the result is
 // the reference's bit for bit).  kernels: kokkos_functors.h:128-151.
 template <int kApplications>
-__global__ void __launch_bounds__(256) b_update_fp64(Grid g, const double* __restrict__ Ex,
+__global__ void __launch_bounds__(256) b_update_fp64(Grid g, Box b, const double* __restrict__ Ex,
                                                      const double* __restrict__ Ey,
                                                      const double* __restrict__ Ez,
                                                      double* __restrict__ Bx, double* __restrict__ By,
                                                      double* __restrict__ Bz, double cx, double cy,
                                                      double cz, int kchunk) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k0 = blockIdx.z * kchunk;
-  if (i >= g.Ni || j >= g.Nj || k0 >= g.Nk) return;
-  const int k1 = min(k0 + kchunk, g.Nk);
+  const int i = b.i0 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = b.j0 + blockIdx.y * blockDim.y + threadIdx.y;
+  const int k0 = b.k0 + blockIdx.z * kchunk;
+  if (i >= b.i1 || j >= b.j1 || k0 >= b.k1) return;
+  const int k1 = min(k0 + kchunk, b.k1);
   const int64_t col = i + (int64_t)j * g.Ni;
   const int64_t col_in = wrap_next(i, g.Ni) + (int64_t)j * g.Ni;
   const int64_t col_jn = i + (int64_t)wrap_next(j, g.Nj) * g.Ni;
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256) b_update_fp64(Grid g, const double* __res
 // the cJ*J term: cJ < 0, so cJ*0 = -0 and x + (-0) = x for every x, which
 // leaves the result bit-identical.
 template <bool kDenseJ, bool kSources>
-__global__ void __launch_bounds__(256) e_update_fp64(Grid g, const double* __restrict__ Bx,
+__global__ void __launch_bounds__(256) e_update_fp64(Grid g, Box b, const double* __restrict__ Bx,
                                                      const double* __restrict__ By,
                                                      const double* __restrict__ Bz,
                                                      const double* __restrict__ Jx,
@@ -90,11 +90,11 @@ __global__ void __launch_bounds__(256) e_update_fp64(Grid g, const double* __res
                                                      double* __restrict__ Ez, double cJ, double cx,
                                                      double cy, double cz, int kchunk, SourceSet ss,
                                                      int64_t s) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k0 = blockIdx.z * kchunk;
-  if (i >= g.Ni || j >= g.Nj || k0 >= g.Nk) return;
-  const int k1 = min(k0 + kchunk, g.Nk);
+  const int i = b.i0 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = b.j0 + blockIdx.y * blockDim.y + threadIdx.y;
+  const int k0 = b.k0 + blockIdx.z * kchunk;
+  if (i >= b.i1 || j >= b.j1 || k0 >= b.k1) return;
+  const int k1 = min(k0 + kchunk, b.k1);
   const int64_t col = i + (int64_t)j * g.Ni;
   const int64_t col_ip = wrap_prev(i, g.Ni) + (int64_t)j * g.Ni;
   const int64_t col_jp = i + (int64_t)wrap_prev(j, g.Nj) * g.Ni;
@@ -144,30 +144,32 @@ __global__ void __launch_bounds__(256) e_update_fp64(Grid g, const double* __res
 // ---------------------------------------------------------------------------
 // Host-side launchers (called from engine.cu).
 
-static dim3 fp64_grid(const Grid& g, int kchunk) {
-  return dim3((g.Ni + 31) / 32, (g.Nj + 7) / 8, (g.Nk + kchunk - 1) / kchunk);
+static dim3 fp64_grid(const Box& b, int kchunk) {
+  return dim3((b.i1 - b.i0 + 31) / 32, (b.j1 - b.j0 + 7) / 8, (b.k1 - b.k0 + kchunk - 1) / kchunk);
 }
 
-cudaError_t launch_b_fp64(const Grid& g, const Fp64Fields& F, const double cb[3], int applications,
-                          cudaStream_t st) {
+cudaError_t launch_b_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const double cb[3],
+                          int applications, cudaStream_t st) {
+  if (box.empty()) return cudaSuccess;
   const int kchunk = 16;
-  dim3 block(32, 8), grid = fp64_grid(g, kchunk);
+  dim3 block(32, 8), grid = fp64_grid(box, kchunk);
   if (applications == 2)
-    b_update_fp64<2><<<grid, block, 0, st>>>(g, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5],
+    b_update_fp64<2><<<grid, block, 0, st>>>(g, box, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5],
                                              cb[0], cb[1], cb[2], kchunk);
   else
-    b_update_fp64<1><<<grid, block, 0, st>>>(g, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5],
+    b_update_fp64<1><<<grid, block, 0, st>>>(g, box, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5],
                                              cb[0], cb[1], cb[2], kchunk);
   return cudaGetLastError();
 }
 
-cudaError_t launch_e_fp64(const Grid& g, const Fp64Fields& F, const double ce[3], double cJ,
+cudaError_t launch_e_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const double ce[3], double cJ,
                           bool dense_j, const SourceSet& ss, int64_t step, cudaStream_t st) {
+  if (box.empty()) return cudaSuccess;
   const int kchunk = 16;
-  dim3 block(32, 8), grid = fp64_grid(g, kchunk);
+  dim3 block(32, 8), grid = fp64_grid(box, kchunk);
   const bool src = ss.count > 0;
 #define FDTD_E64(DJ, SRC)                                                                     \
-  e_update_fp64<DJ, SRC><<<grid, block, 0, st>>>(g, F.f[3], F.f[4], F.f[5], F.f[6], F.f[7],   \
+  e_update_fp64<DJ, SRC><<<grid, block, 0, st>>>(g, box, F.f[3], F.f[4], F.f[5], F.f[6], F.f[7], \
                                                  F.f[8], F.f[0], F.f[1], F.f[2], cJ, ce[0],   \
                                                  ce[1], ce[2], kchunk, ss, step)
   if (dense_j && src) FDTD_E64(true, true);

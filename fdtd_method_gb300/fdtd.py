@@ -348,6 +348,36 @@ class FDTD:
                 "current_coef": -4.0 * Const.PI * dt}
 
 
+class FDTD_PML(FDTD):
+    """Drop-in for FDTD_kokkos::FDTD_PML (include/FDTD_kokkos/FDTD_PML_kokkos.h:10-33,
+    src/FDTD_kokkos/FDTD_PML_kokkos.cpp): the solver with a split-field
+    absorbing layer of (int)(N * pml_percent) cells on every face.
+    update_fields follows FDTD_PML::update_fields (FP64, bit-identical to the
+    reference)."""
+
+    def __init__(self, parameters, dt, pml_percent):
+        self._h = None
+        lib = _lib.load()
+        self.parameters = parameters
+        self.dt = float(dt)
+        self.precision = Precision.FP64
+        self.pml_percent = float(pml_percent)
+        p = parameters.to_c()
+        h = ctypes.c_void_p()
+        _lib.check(lib.fdtd_create_pml(ctypes.byref(p), self.dt, self.pml_percent, int(Precision.FP64),
+                                       ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+        self._sources = []
+
+    @property
+    def pml_size(self):
+        """Layer thickness (cells) along x, y, z."""
+        out = (ctypes.c_int * 3)()
+        _lib.check(self._lib.fdtd_get_pml(self._handle(), out))
+        return list(out)
+
+
 class FDTDBatch:
     """Many independent periodic domains advanced together on one GPU (the
     batched form; the reference advances one grid per object).  Every domain

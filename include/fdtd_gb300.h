@@ -113,6 +113,21 @@ int fdtd_abi_version(void);
  * coefficients.  `precision` is an fdtd_precision. */
 int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle** out);
 
+/* Replaces FDTD_PML::FDTD_PML(Parameters, FP dt, FP pml_percent)
+ * (include/FDTD_kokkos/FDTD_PML_kokkos.h:10-33, src/FDTD_kokkos/FDTD_PML_kokkos.cpp:22-160):
+ * a grid whose outer (int)(N * pml_percent) cells on each face of every axis
+ * form a split-field absorbing layer (conductivity (d/pml)^4 profile,
+ * reflection 1e-12).  update_fields / fdtd_step then follow
+ * FDTD_PML::update_fields (:162-189): B/2 inside, the split-field B update on
+ * the layer, E inside (with current), the split-field E update on the layer,
+ * B/2 inside.  FP64 form only (other precisions give FDTD_ERR_UNSUPPORTED);
+ * pml_percent must be in [0, 0.5).  The split fields and conductivities start
+ * at zero (the reference leaves them unset).  All other entry points work as
+ * for fdtd_create's handles; fdtd_destroy releases it. */
+int fdtd_create_pml(const fdtd_params* params, double dt, double pml_percent, int precision, fdtd_handle** out);
+/* Layer thickness per axis in cells (all zero for a handle without PML). */
+int fdtd_get_pml(fdtd_handle* h, int sizes[3]);
+
 /* Releases the fields (the reference's Views are freed with the object). */
 int fdtd_destroy(fdtd_handle* h);
 

@@ -142,6 +142,22 @@ class FDTD {
   FDTD& operator=(const FDTD&) = delete;
   virtual ~FDTD() { fdtd_destroy(h_); }
 
+ protected:
+  // For subclasses that create their handle with another constructor.
+  FDTD(Parameters parameters, FP dt, fdtd_handle* h) : parameters_(parameters), dt_(dt), h_(h) {
+    const std::size_t n = static_cast<std::size_t>(parameters.Ni) * parameters.Nj * parameters.Nk;
+    for (int c = 0; c < 9; ++c) fields_[c] = Field(h_, static_cast<Component>(c), n);
+  }
+  static fdtd_handle* create_pml(const Parameters& parameters, FP dt, FP pml_percent) {
+    fdtd_params p{parameters.Ni, parameters.Nj, parameters.Nk, parameters.ax, parameters.bx, parameters.ay,
+                  parameters.by, parameters.az, parameters.bz, parameters.dx, parameters.dy, parameters.dz};
+    fdtd_handle* h = nullptr;
+    check(fdtd_create_pml(&p, dt, pml_percent, FDTD_PRECISION_FP64, &h));
+    return h;
+  }
+
+ public:
+
   Field& get_field(Component c) {
     const int i = static_cast<int>(c);
     if (i < 0 || i > 8) throw std::logic_error("ERROR: Invalid field component");
@@ -169,6 +185,16 @@ class FDTD {
   FP dt_;
   fdtd_handle* h_ = nullptr;
   Field fields_[9];
+};
+
+// Replaces FDTD_kokkos::FDTD_PML (include/FDTD_kokkos/FDTD_PML_kokkos.h:10-33):
+// the same solver with a split-field absorbing layer of (int)(N * pml_percent)
+// cells on every face; update_fields follows FDTD_PML::update_fields.
+class FDTD_PML : public FDTD {
+ public:
+  FDTD_PML(Parameters parameters, FP dt, FP pml_percent)
+      : FDTD(parameters, dt, create_pml(parameters, dt, pml_percent)) {}
+  void update_fields() override { check(fdtd_update_fields(handle())); }
 };
 
 }  // namespace FDTD_gb300

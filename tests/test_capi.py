@@ -78,3 +78,12 @@ def test_batch_arguments_checked_before_gpu_work(lib):
     assert b"FP32" in lib.fdtd_last_error()
     assert lib.fdtd_batch_step(None, 1) == _lib.FDTD_ERR_INVALID_ARGUMENT
     assert lib.fdtd_batch_destroy(None) == 0
+
+
+def test_pml_arguments_checked_before_gpu_work(lib):
+    p = Parameters(8, 8, 8, 0, 1, 0, 1, 0, 1, 0.125, 0.125, 0.125).to_c()
+    h = ctypes.c_void_p()
+    for bad in (-0.1, 0.5, 0.7, float("nan")):
+        assert lib.fdtd_create_pml(ctypes.byref(p), 1e-12, bad, 0, ctypes.byref(h)) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_create_pml(ctypes.byref(p), 1e-12, 0.2, 2, ctypes.byref(h)) == _lib.FDTD_ERR_UNSUPPORTED
+    assert b"FP64" in lib.fdtd_last_error()
