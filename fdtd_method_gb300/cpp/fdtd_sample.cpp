@@ -2,19 +2,23 @@
 // (perf-tests/kokkos_sample/kokkos_sample.cpp): a box current
 // sin(2 pi t/T) cos^2(2 pi x/Tx) cos^2(2 pi y/Ty) cos^2(2 pi z/Tz) in Jx, Jy, Jz
 // for period/dt steps, then a free run; prints the execution time and the same
-// 10 x 10 slice of Ex.  Usage: fdtd_sample [N iters]  (default 32 100).
+// 10 x 10 slice of Ex.  Usage: fdtd_sample [N iters [pml]]  (default 32 100).
+// With "pml" it also runs the same source on FDTD_PML(params, dt, 0.2) and
+// prints its execution time, as the reference's sample does under
+// __PML_TEST__ (perf-tests/sample/sample.cpp:93-123).
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <iomanip>
 #include <iostream>
+#include <string>
 #include <vector>
 
 #include "fdtd_gb300.hpp"
 
 using namespace FDTD_gb300;
 
-static void spherical_wave(int n, int it) {
+static void spherical_wave(int n, int it, bool with_pml) {
   CurrentParameters cur_param{8, 4, 0.2};
   const double T = cur_param.period;
   const double Tx = cur_param.period_x, Ty = cur_param.period_y, Tz = cur_param.period_z;
@@ -65,6 +69,37 @@ static void spherical_wave(int n, int it) {
   std::chrono::duration<double> elapsed = t1 - t0;
   std::cout << "Execution time: " << elapsed.count() << " s" << std::endl;
 
+  if (with_pml) {
+    FDTD_PML pml_method(params, cur_param.dt, 0.2);
+    if (!g[0].empty() && !g[1].empty() && !g[2].empty() && cur_time > 0) {
+      fdtd_source s{};
+      s.comp_mask = 7;
+      s.i0 = ((start[0] % n) + n) % n;
+      s.j0 = ((start[1] % n) + n) % n;
+      s.k0 = ((start[2] % n) + n) % n;
+      s.ni = static_cast<int>(g[0].size());
+      s.nj = static_cast<int>(g[1].size());
+      s.nk = static_cast<int>(g[2].size());
+      s.gx = g[0].data();
+      s.gy = g[1].data();
+      s.gz = g[2].data();
+      s.amp = amp.data();
+      s.n_amp = cur_time;
+      pml_method.add_source(s);
+    }
+    auto p0 = std::chrono::high_resolution_clock::now();
+    pml_method.step(it);
+    pml_method.fence();
+    auto p1 = std::chrono::high_resolution_clock::now();
+    std::chrono::duration<double> elapsed_pml = p1 - p0;
+    std::cout << "Execution time (PML): " << elapsed_pml.count() << " s" << std::endl;
+    double sums[FDTD_DIAG_COUNT];
+    pml_method.field_sums(sums);
+    double e2 = 0.0;
+    for (int c = 0; c < 6; ++c) e2 += sums[c];
+    std::cout << "PML field square sum: " << std::scientific << std::setprecision(6) << e2 << std::endl;
+  }
+
   auto& Ex_device = method.get_field(Component::EX);
   auto Ex_host = create_mirror_view(Ex_device);
   deep_copy(Ex_host, Ex_device);
@@ -82,9 +117,11 @@ static void spherical_wave(int n, int it) {
 int main(int argc, char* argv[]) {
   try {
     if (argc == 1) {
-      spherical_wave(32, 100);
+      spherical_wave(32, 100, false);
     } else if (argc == 3) {
-      spherical_wave(std::atoi(argv[1]), std::atoi(argv[2]));
+      spherical_wave(std::atoi(argv[1]), std::atoi(argv[2]), false);
+    } else if (argc == 4 && std::string(argv[3]) == "pml") {
+      spherical_wave(std::atoi(argv[1]), std::atoi(argv[2]), true);
     } else {
       std::cout << "ERROR: Incorrect number of parameters" << std::endl;
       return 1;

@@ -87,3 +87,28 @@ def test_pml_arguments_checked_before_gpu_work(lib):
         assert lib.fdtd_create_pml(ctypes.byref(p), 1e-12, bad, 0, ctypes.byref(h)) == _lib.FDTD_ERR_INVALID_ARGUMENT
     assert lib.fdtd_create_pml(ctypes.byref(p), 1e-12, 0.2, 2, ctypes.byref(h)) == _lib.FDTD_ERR_UNSUPPORTED
     assert b"FP64" in lib.fdtd_last_error()
+
+
+def test_slice_csv_matches_the_plotting_script_format(tmp_path):
+    """OutFiles_<n>/<iteration>.csv as python_script_legend/visualization.py
+    reads it: ';' separator, decimal comma, a header row."""
+    import numpy as np
+
+    from fdtd_method_gb300 import slices
+    from fdtd_method_gb300.fdtd import Component
+
+    p = Parameters(5, 4, 3, 0, 1, 0, 1, 0, 1, 0.2, 0.25, 0.33)
+    values = np.arange(p.cells, dtype=np.float64) * -0.125
+
+    class Stub:  # stands in for a solver: only get_field(c).numpy() is used
+        parameters = p
+
+        def get_field(self, c):
+            return type("F", (), {"numpy": lambda self_: values})()
+
+    path = slices.write_slice_csv(Stub(), Component.EY, 17, root=str(tmp_path))
+    assert path.endswith(os.path.join("OutFiles_2", "17.csv"))
+    lines = open(path).read().splitlines()
+    assert lines[0].split(";") == ["0", "1", "2", "3", "4"]
+    table = np.array([[float(x.replace(",", ".")) for x in ln.split(";")] for ln in lines[1:]])
+    np.testing.assert_array_equal(table, values.reshape(3, 4, 5)[1])

@@ -45,3 +45,27 @@ def test_cpp_sample_rejects_wrong_argument_count():
     r = subprocess.run([os.path.join(BIN, "fdtd_sample"), "16"], capture_output=True, text=True)
     assert r.returncode == 1
     assert "Incorrect number of parameters" in r.stdout
+
+
+def test_cpp_sample_pml_run_uses_the_pml_class():
+    """The sample's PML option (the reference sample's __PML_TEST__ block)
+    drives FDTD_gb300::FDTD_PML; the periodic slice is unchanged and the
+    layer's field sum matches the Python PML class on the same job."""
+    golden = json.load(open(os.path.join(GOLDEN, "reference_sample.json")))
+    r = subprocess.run([os.path.join(BIN, "fdtd_sample"), "16", "60", "pml"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "Execution time (PML)" in r.stdout
+    rows = [ln for ln in r.stdout.splitlines() if ln.strip() and "Execution" not in ln and "PML" not in ln]
+    assert [x.split() for x in rows] == [x.split() for x in golden["16_60"]]
+    value = float([ln for ln in r.stdout.splitlines() if ln.startswith("PML field square sum")][0].split()[-1])
+
+    from fdtd_method_gb300 import FDTD_PML, sources
+    from fdtd_method_gb300.fdtd import CurrentParameters, Parameters
+    d = 3e10
+    p = Parameters(16, 16, 16, -8 * d, 8 * d, -8 * d, 8 * d, -8 * d, 8 * d, d, d, d)
+    cp = CurrentParameters(8, 4, 0.2)
+    src, _ = sources.sample_box_source(p, cp, iterations=60)
+    s = FDTD_PML(p, cp.dt, 0.2)
+    s.add_source(src)
+    s.step(60)
+    assert value == pytest.approx(float(s.field_sums()[:6].sum()), rel=1e-6)
