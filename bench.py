@@ -235,13 +235,22 @@ def barrier(world):
 
 
 def max_over_ranks(world, x):
+    """The largest x over all ranks (the slowest replica's time)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(world, cells, steps, ms):
+    """Whole-job Gcell-steps/s of `world` replicas that each advanced `cells`
+    cells by `steps` steps, the slowest taking `ms` milliseconds (weak
+    scaling: the work per GPU is fixed)."""
+    return world * cells * steps / (ms / 1e3) / 1e9
 
 
 def timed_steps(sim, stream, steps, world):
@@ -367,7 +376,7 @@ def run_ours(args):
     kt = sim.kernel_times()
     sim.set_kernel_timing(False)
     ms = max_over_ranks(world, ms)
-    value = world * cells * K / (ms / 1e3) / 1e9
+    value = replica_value(world, cells, K, ms)
     launches = int(sum(n for _, n in kt.values()))
 
     bpv = BYTES_PER_VALUE[args.precision]
