@@ -29,8 +29,9 @@
 //      B(t-1) carried in registers);
 //   2. on interior cells (t > k0), computes B'(t-1) = B(t-1) + apps (c/2) curl E'
 //      (E'(t-1) at i+1, j+1 from the exchange plane, E'(t) in registers);
-//   3. writes both to staging, and the CTA synchronises once; thread 0 then
-//      stores the staged boxes and refills the freed ring slot.
+//   3. writes both to staging, and the CTA synchronises once; lane 0 of the
+//      halo-column warp then stores the staged boxes and refills the freed
+//      ring slot.
 // The sweep reads the state from `st` and writes the new state to `out`:
 // neighbouring tiles read what a tile writes, so an in-place update would race.
 #include "arith.cuh"
@@ -175,7 +176,7 @@ __device__ __forceinline__ bool window_meets(int o, int n, int N, int a, int m) 
 // One tile: columns bx*32 .., rows by*RY .., planes bz*kchunk .. of one
 // domain, with the CTA's shared memory `smem` (barriers initialised).  `ring`
 // counts the ring fills the CTA has consumed so far (it carries the slot and
-// phase from tile to tile); on return the leader has waited for the tile's
+// phase from tile to tile); on return the copy-engine leader has waited for the tile's
 // stores to read their staging, and the caller synchronises before the next
 // tile writes staging again.
 //
@@ -209,7 +210,9 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
   const int xl = xu >= L.Ni ? xu - L.Ni : xu, yl = yu >= L.Nj ? yu - L.Nj : yu;
   const int k0 = bz * kchunk;
   const int k1 = min(k0 + kchunk, L.Nk);
-  const bool leader = (w == 0 && lane == 0);
+  // The copy-engine leader (ring refills, bulk stores and their waits) is
+  // lane 0 of the halo-column warp, which has the least arithmetic per plane.
+  const bool leader = (w == RY + 1 && lane == 0);
   const int slot0 = (int)(ring % NS);
   const uint32_t phase0 = (ring / NS) & 1u;
   const bool tile_edge = x0 == 0 || x0 + nx == L.Ni || y0 == 0 || y0 + ny == L.Nj;
@@ -517,7 +520,7 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
   uint32_t ring = 0;
   fused1_tile<S, A, RY, kApps, kDenseJ, true>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z, kchunk, Jx, Jy,
                                               Jz, ss, step, err, smem, ring);
-  if (threadIdx.x == 0 && threadIdx.y == 0) bulk_wait_all();
+  if (threadIdx.x == 0 && threadIdx.y == RY + 1) bulk_wait_all();  // the copy-engine leader's stores
 }
 
 // Batched form: a persistent kernel; every CTA takes tiles (domain, bx, by,
@@ -563,8 +566,8 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
                                                ring);
     __syncthreads();
   }
+  if (threadIdx.x == 0 && threadIdx.y == RY + 1) bulk_wait_all();  // the copy-engine leader's stores
   if (leader) {
-    bulk_wait_all();
     __threadfence();
     if (atomicAdd(&counters[1], 1) == (int)(gridDim.x * gridDim.y * gridDim.z) - 1) {
       counters[0] = 0;
