@@ -30,23 +30,34 @@ __device__ __forceinline__ void unflatten(const PLayout& L, int64_t t, int& x, i
   x = (int)(r - (int64_t)y * L.Ni);
 }
 
-template <class S>
-__global__ void import_kernel(PLayout L, S st, int c, const double* __restrict__ src, int64_t off, int64_t n) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-    int x, y, z;
-    unflatten(L, off + t, x, y, z);
-    const Pair p = S::kComp ? split_f64(src[t]) : Pair{__double2float_rn(src[t]), 0.f};
-    store_with_ghosts(st, L, c, x, y, z, p);
+// Row-wise walk over the logical cells off .. off+n-1: blocks take grid rows
+// (y, z) in turn, threads take consecutive x, so every warp touches a
+// contiguous run of the flat FP64 array (host memory included, when the
+// caller's buffer is page-locked) and no per-element division is needed.
+template <class F>
+__device__ __forceinline__ void for_cells_by_row(const PLayout& L, int64_t off, int64_t n, F&& f) {
+  const int64_t row0 = off / L.Ni, row1 = (off + n + L.Ni - 1) / L.Ni;
+  for (int64_t row = row0 + blockIdx.x; row < row1; row += gridDim.x) {
+    const int z = (int)(row / L.Nj), y = (int)(row - (int64_t)z * L.Nj);
+    const int64_t first = row * L.Ni;
+    for (int x = threadIdx.x; x < L.Ni; x += blockDim.x) {
+      const int64_t t = first + x - off;  // position in the caller's buffer
+      if (t >= 0 && t < n) f(x, y, z, t);
+    }
   }
 }
 
 template <class S>
+__global__ void import_kernel(PLayout L, S st, int c, const double* __restrict__ src, int64_t off, int64_t n) {
+  for_cells_by_row(L, off, n, [&](int x, int y, int z, int64_t t) {
+    const Pair p = S::kComp ? split_f64(src[t]) : Pair{__double2float_rn(src[t]), 0.f};
+    store_with_ghosts(st, L, c, x, y, z, p);
+  });
+}
+
+template <class S>
 __global__ void export_kernel(PLayout L, S st, int c, double* __restrict__ dst, int64_t off, int64_t n) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-    int x, y, z;
-    unflatten(L, off + t, x, y, z);
-    dst[t] = st.load_f64(c, L.at(x, y, z));
-  }
+  for_cells_by_row(L, off, n, [&](int x, int y, int z, int64_t t) { dst[t] = st.load_f64(c, L.at(x, y, z)); });
 }
 
 __global__ void to_f32_kernel(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
