@@ -11,7 +11,8 @@ from .fdtd import (FDTD, FDTD_PML, FDTDBatch, Axis, Component, Const, CurrentPar
                    InvalidArgument, LogicError, OutOfMemory, Parameters, Precision,
                    SelectedFields, SeparableSource)
 from . import sources  # noqa: F401
+from .slabs import FDTDSlabs, Slab  # noqa: F401
 
 __all__ = ["FDTD", "FDTD_PML", "FDTDBatch", "Axis", "Component", "Const", "CurrentParameters", "Field", "FDTDError",
            "InvalidArgument", "LogicError", "OutOfMemory", "Parameters", "Precision",
-           "SelectedFields", "SeparableSource", "sources"]
+           "SelectedFields", "SeparableSource", "sources", "FDTDSlabs", "Slab"]

@@ -114,6 +114,14 @@ SIGNATURES = {
     "fdtd_batch_tiles": [_H, ctypes.POINTER(ctypes.c_int64)],
     "fdtd_batch_set_stream": [_H, ctypes.c_void_p],
     "fdtd_batch_synchronize": [_H],
+    # z slabs
+    "fdtd_slab_create": [ctypes.POINTER(Params), ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                         ctypes.POINTER(_H)],
+    "fdtd_slab_info": [_H, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+    "fdtd_slab_sweep": [_H, ctypes.c_int],
+    "fdtd_slab_plane": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                        ctypes.POINTER(ctypes.c_size_t)],
+    "fdtd_slab_exchange": [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int],
 }
 _RESTYPES = {"fdtd_last_error": ctypes.c_char_p}
 

@@ -74,6 +74,8 @@ void release(fdtd_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (void* p : h->allocations) cudaFree(p);
+  for (cudaEvent_t e : h->xev)
+    if (e) cudaEventDestroy(e);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   cudaSetDevice(prev);
   delete h;
@@ -100,9 +102,14 @@ int ensure_staging(fdtd_handle* h) {
 
 int ensure_jf(fdtd_handle* h) {
   if (h->form == Form::F64 || h->jf[0]) return FDTD_OK;
+  // a slab's currents carry its halo planes too (never read: J enters only
+  // the owned planes' E update), so they index like its fields
+  const int64_t halo = h->zhalo * h->g.plane, n = h->g.cells + 2 * halo;
   for (int c = 0; c < 3; ++c) {
-    FDTD_CUDA(dev_alloc(h, (void**)&h->jf[c], sizeof(float) * h->g.cells), "current arrays");
-    FDTD_CUDA(cudaMemsetAsync(h->jf[c], 0, sizeof(float) * h->g.cells, h->stream), "zero current");
+    float* base = nullptr;
+    FDTD_CUDA(dev_alloc(h, (void**)&base, sizeof(float) * n), "current arrays");
+    FDTD_CUDA(cudaMemsetAsync(base, 0, sizeof(float) * n, h->stream), "zero current");
+    h->jf[c] = base + halo;
   }
   return FDTD_OK;
 }
@@ -181,16 +188,17 @@ struct LaunchTimer {
 int run_b(fdtd_handle* h, int apps) {
   LaunchTimer lt(h, apps == 2 ? FDTD_KERNEL_B_DOUBLE : FDTD_KERNEL_B_HALF);
   cudaError_t e = cudaSuccess;
+  const Box box = h->sweep_box();
+  const StateView v = h->sweep_view();
   if (h->form == Form::F64) {
     Fp64Fields F;
-    for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c];
-    e = launch_b_fp64(h->g, h->main_box(), F, &h->coef[3], apps, h->stream);
+    for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c] - h->halo_elems();
+    e = launch_b_fp64(v.g, box, F, &h->coef[3], apps, h->stream);
   } else {
-    StateView v = h->view();
     switch (h->form) {
-      case Form::F32: e = launch_b_f32(h->L, v.s32, h->cs, apps, h->stream); break;
-      case Form::F32C: e = launch_b_f32(h->L, v.s32c, h->cs, apps, h->stream); break;
-      case Form::F16: e = launch_b_f32(h->L, v.s16, h->cs, apps, h->stream); break;
+      case Form::F32: e = launch_b_f32(v.L, v.s32, h->cs, apps, box.k0, box.k1, h->stream); break;
+      case Form::F32C: e = launch_b_f32(v.L, v.s32c, h->cs, apps, box.k0, box.k1, h->stream); break;
+      case Form::F16: e = launch_b_f32(v.L, v.s16, h->cs, apps, box.k0, box.k1, h->stream); break;
       default: break;
     }
   }
@@ -204,18 +212,21 @@ int run_e(fdtd_handle* h, int64_t step) {
   LaunchTimer lt(h, FDTD_KERNEL_E);
   SourceSet ss = h->source_set();
   cudaError_t e = cudaSuccess;
+  const Box box = h->sweep_box();
+  const StateView v = h->sweep_view();
   if (h->form == Form::F64) {
     Fp64Fields F;
-    for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c];
-    e = launch_e_fp64(h->g, h->main_box(), F, &h->coef[0], h->coef[6], h->dense_j, ss, step, h->stream);
+    for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c] - h->halo_elems();
+    e = launch_e_fp64(v.g, box, F, &h->coef[0], h->coef[6], h->dense_j, ss, step, h->stream);
   } else {
-    StateView v = h->view();
-    const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
+    // dense FP32 currents: the dense layout, with the same halo planes
+    const int64_t dj0 = h->zhalo * h->g.plane;
     const bool dj = h->dense_j && h->jf[0];
+    const float* J[3] = {dj ? h->jf[0] - dj0 : nullptr, dj ? h->jf[1] - dj0 : nullptr, dj ? h->jf[2] - dj0 : nullptr};
     switch (h->form) {
-      case Form::F32: e = launch_e_f32(h->L, v.s32, J, dj, h->cs, ss, step, h->stream); break;
-      case Form::F32C: e = launch_e_f32(h->L, v.s32c, J, dj, h->cs, ss, step, h->stream); break;
-      case Form::F16: e = launch_e_f32(h->L, v.s16, J, dj, h->cs, ss, step, h->stream); break;
+      case Form::F32: e = launch_e_f32(v.L, v.s32, J, dj, h->cs, ss, step, box.k0, box.k1, h->stream); break;
+      case Form::F32C: e = launch_e_f32(v.L, v.s32c, J, dj, h->cs, ss, step, box.k0, box.k1, h->stream); break;
+      case Form::F16: e = launch_e_f32(v.L, v.s16, J, dj, h->cs, ss, step, box.k0, box.k1, h->stream); break;
       default: break;
     }
   }
@@ -387,7 +398,9 @@ extern "C" {
 const char* fdtd_last_error(void) { return g_last_error.c_str(); }
 int fdtd_abi_version(void) { return FDTD_ABI_VERSION; }
 
-int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle** out) {
+// A handle of the grid `params` whose arrays carry `zhalo` extra planes
+// below and above it (0: an ordinary handle; 1: a z slab).
+static int create_handle(const fdtd_params* params, double dt, int precision, int zhalo, fdtd_handle** out) {
   if (!params || !out) return fail(FDTD_ERR_INVALID_ARGUMENT, "null argument");
   *out = nullptr;
   // src/FDTD_kokkos/FDTD_kokkos.cpp:7-12
@@ -397,6 +410,7 @@ int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle
     return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid precision");
 
   fdtd_handle* h = new fdtd_handle();
+  h->zhalo = zhalo;
   h->p = *params;
   h->dt = dt;
   h->precision = precision;
@@ -441,25 +455,39 @@ int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle
   h->L = PLayout::make(params->Ni, params->Nj, params->Nk);
   const size_t eb = elem_bytes(h->form);
   const int nfields = (h->form == Form::F64) ? 9 : 6;
-  const int64_t per_field = (h->form == Form::F64) ? h->g.cells : h->L.elems();
+  const int64_t halo = h->halo_elems();
+  const int64_t per_field = ((h->form == Form::F64) ? h->g.cells : h->L.elems()) + 2 * halo;
   for (int c = 0; c < nfields; ++c) {
-    e = dev_alloc(h, &h->field[c], eb * per_field);
-    if (e == cudaSuccess) e = cudaMemsetAsync(h->field[c], 0, eb * per_field, h->stream);
+    void* base = nullptr;
+    e = dev_alloc(h, &base, eb * per_field);
+    if (e == cudaSuccess) e = cudaMemsetAsync(base, 0, eb * per_field, h->stream);
     if (e != cudaSuccess) {
       int rc = cuda_fail(e, "field allocation");
       release(h);
       return rc;
     }
+    h->field[c] = static_cast<unsigned char*>(base) + eb * halo;
   }
   if (h->form == Form::F32C) {
     for (int c = 0; c < 6; ++c) {
-      e = dev_alloc(h, (void**)&h->lo[c], sizeof(LoT) * per_field);
-      if (e == cudaSuccess) e = cudaMemsetAsync(h->lo[c], 0, sizeof(LoT) * per_field, h->stream);
+      LoT* base = nullptr;
+      e = dev_alloc(h, (void**)&base, sizeof(LoT) * per_field);
+      if (e == cudaSuccess) e = cudaMemsetAsync(base, 0, sizeof(LoT) * per_field, h->stream);
       if (e != cudaSuccess) {
         int rc = cuda_fail(e, "compensation allocation");
         release(h);
         return rc;
       }
+      h->lo[c] = base + halo;
+    }
+  }
+  if (zhalo > 0) {
+    for (cudaEvent_t& x : h->xev)
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      int rc = cuda_fail(e, "slab event creation");
+      release(h);
+      return rc;
     }
   }
   e = dev_alloc(h, (void**)&h->d_partials, sizeof(double) * kDiagValues * kMaxDiagBlocks);
@@ -474,6 +502,10 @@ int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle
   }
   *out = h;
   return FDTD_OK;
+}
+
+int fdtd_create(const fdtd_params* params, double dt, int precision, fdtd_handle** out) {
+  return create_handle(params, dt, precision, 0, out);
 }
 
 int fdtd_create_pml(const fdtd_params* params, double dt, double pml_percent, int precision, fdtd_handle** out) {
@@ -593,6 +625,8 @@ int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t laun
 int fdtd_step(fdtd_handle* h, int64_t n) {
   if (int rc = check_handle(h)) return rc;
   if (n < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "negative step count");
+  if (h->zhalo)
+    return fail(FDTD_ERR_UNSUPPORTED, "a z slab steps through fdtd_slab_sweep and fdtd_slab_exchange");
   if (n == 0) return FDTD_OK;
   DeviceGuard dg(h->device);
   // src/FDTD_kokkos/FDTD_kokkos.cpp:91-104 repeated n times; the trailing B
@@ -750,29 +784,62 @@ int fdtd_add_source(fdtd_handle* h, const fdtd_source* src, int* index) {
   if (int rc = check_handle(h)) return rc;
   if (!src) return fail(FDTD_ERR_INVALID_ARGUMENT, "null source");
   if (src->comp_mask <= 0 || src->comp_mask > 7) return fail(FDTD_ERR_INVALID_ARGUMENT, "source comp_mask must be 1..7");
+  // a z slab takes sources in the coordinates of the whole grid
+  const int nk_grid = h->zhalo ? h->slab_nk_global : h->g.Nk;
   if (src->ni <= 0 || src->nj <= 0 || src->nk <= 0 || src->ni > h->g.Ni || src->nj > h->g.Nj ||
-      src->nk > h->g.Nk)
+      src->nk > nk_grid)
     return fail(FDTD_ERR_INVALID_ARGUMENT, "source box extents must be in 1..N per axis");
   if (src->i0 < 0 || src->i0 >= h->g.Ni || src->j0 < 0 || src->j0 >= h->g.Nj || src->k0 < 0 ||
-      src->k0 >= h->g.Nk)
+      src->k0 >= nk_grid)
     return fail(FDTD_ERR_INVALID_ARGUMENT, "source box origin outside the grid");
   if (!src->gx || !src->gy || !src->gz || src->n_amp < 0 || (src->n_amp > 0 && !src->amp))
     return fail(FDTD_ERR_INVALID_ARGUMENT, "source tables missing");
-  if ((int)h->sources.size() >= kMaxSources) return fail(FDTD_ERR_INVALID_ARGUMENT, "too many sources");
   DeviceGuard dg(h->device);
   HostSource hs;
   hs.s = *src;
   hs.s.gx = hs.s.gy = hs.s.gz = hs.s.amp = nullptr;
   hs.gx.assign(src->gx, src->gx + src->ni);
   hs.gy.assign(src->gy, src->gy + src->nj);
-  hs.gz.assign(src->gz, src->gz + src->nk);
   if (src->n_amp > 0) hs.amp.assign(src->amp, src->amp + src->n_amp);
-  h->sources.push_back(std::move(hs));
+  // The pieces to register: the whole box, or, on a z slab, each run of the
+  // box's planes (taken mod Nk) that lies in the slab's owned planes and is
+  // contiguous there, in the slab's storage numbering (k0 >= 1, and the
+  // piece ends at or before the halo above, so the kernels' index wrap never
+  // maps another plane into it).  A cell lies in one piece at most, so its
+  // sources still add up in registration order.
+  std::vector<HostSource> pieces;
+  if (!h->zhalo) {
+    hs.gz.assign(src->gz, src->gz + src->nk);
+    pieces.push_back(std::move(hs));
+  } else {
+    const int kb = h->slab_k0, ke = h->slab_k0 + h->g.Nk;
+    int t = 0;
+    while (t < src->nk) {
+      const int kg = (src->k0 + t) % nk_grid;
+      if (kg < kb || kg >= ke) {
+        ++t;
+        continue;
+      }
+      int len = 1;
+      while (t + len < src->nk && (src->k0 + t + len) % nk_grid == kg + len && kg + len < ke) ++len;
+      HostSource piece = hs;
+      piece.s.k0 = kg - kb + h->zhalo;
+      piece.s.nk = len;
+      piece.gz.assign(src->gz + t, src->gz + t + len);
+      pieces.push_back(std::move(piece));
+      t += len;
+    }
+  }
+  if ((int)(h->sources.size() + pieces.size()) > kMaxSources)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "too many sources");
+  const size_t before = h->sources.size();
+  for (HostSource& q : pieces) h->sources.push_back(std::move(q));
   if (int rc = upload_sources(h)) {
-    h->sources.pop_back();
+    h->sources.resize(before);
     return rc;
   }
-  if (index) *index = (int)h->sources.size() - 1;
+  if (index) *index = h->source_calls;
+  ++h->source_calls;
   return FDTD_OK;
 }
 
@@ -780,6 +847,7 @@ int fdtd_clear_sources(fdtd_handle* h) {
   if (int rc = check_handle(h)) return rc;
   DeviceGuard dg(h->device);
   h->sources.clear();
+  h->source_calls = 0;
   return upload_sources(h);
 }
 
@@ -808,6 +876,8 @@ int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int 
   if (kchunk < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "kchunk must be >= 0");
   if (cells_per_thread < 0 || cells_per_thread > 2)
     return fail(FDTD_ERR_INVALID_ARGUMENT, "cells_per_thread must be 0 (default), 1 or 2");
+  if (h->zhalo && pipeline == FDTD_PIPELINE_FUSED)
+    return fail(FDTD_ERR_UNSUPPORTED, "a z slab runs the split sweeps");
   h->pipeline = pipeline;
   h->fused_cfg.tile_y = tile_y ? tile_y : 14;
   h->fused_cfg.kchunk = kchunk ? kchunk : 24;
@@ -818,6 +888,7 @@ int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int 
 int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out) {
   if (int rc = check_handle(h)) return rc;
   if (h->form == Form::F64) return fail(FDTD_ERR_UNSUPPORTED, "the FP64 form has one pipeline; nothing to tune");
+  if (h->zhalo) return fail(FDTD_ERR_UNSUPPORTED, "a z slab runs the split sweeps; nothing to tune");
   if (sweeps <= 0) sweeps = 10;
   DeviceGuard dg(h->device);
   const TuneKey key{(int)h->form, h->g.Ni, h->g.Nj, h->g.Nk};
@@ -951,6 +1022,138 @@ int fdtd_set_fp16_exponents(fdtd_handle* h, const int exponents[6]) {
     h->fp16_exp[c] = exponents[c];
   }
   FDTD_CUDA(cudaStreamSynchronize(h->stream), "rescale");
+  return FDTD_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// z slabs: the decomposition of the reference's coarray program
+// (coarray/fdtd.F90:90-98), where image s owns a range of z planes and reads
+// the neighbours' boundary planes of E (for B at k+1, kokkos_functors.h:141)
+// and of B (for E at k-1, :78) between the sweeps.
+
+int fdtd_slab_create(const fdtd_params* params, double dt, int precision, int k_begin, int k_end,
+                     fdtd_handle** out) {
+  if (!params || !out) return fail(FDTD_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (params->Ni <= 0 || params->Nj <= 0 || params->Nk <= 0 || !(dt > 0))
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "ERROR: invalid parameters");
+  if (k_begin < 0 || k_end <= k_begin || k_end > params->Nk)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "slab planes must satisfy 0 <= k_begin < k_end <= Nk");
+  fdtd_params owned = *params;
+  owned.Nk = k_end - k_begin;
+  owned.az = params->az + k_begin * params->dz;
+  owned.bz = owned.az + owned.Nk * params->dz;
+  fdtd_handle* h = nullptr;
+  if (int rc = create_handle(&owned, dt, precision, 1, &h)) return rc;
+  h->slab_k0 = k_begin;
+  h->slab_nk_global = params->Nk;
+  h->pipeline = FDTD_PIPELINE_SPLIT;
+  *out = h;
+  return FDTD_OK;
+}
+
+int fdtd_slab_info(fdtd_handle* h, int* k_begin, int* k_end, int* nk_global) {
+  if (int rc = check_handle(h)) return rc;
+  const bool slab = h->zhalo != 0;
+  if (k_begin) *k_begin = slab ? h->slab_k0 : 0;
+  if (k_end) *k_end = slab ? h->slab_k0 + h->g.Nk : h->g.Nk;
+  if (nk_global) *nk_global = slab ? h->slab_nk_global : h->g.Nk;
+  return FDTD_OK;
+}
+
+int fdtd_slab_sweep(fdtd_handle* h, int sweep) {
+  if (int rc = check_handle(h)) return rc;
+  if (h->pml) return fail(FDTD_ERR_UNSUPPORTED, "the PML form steps through fdtd_step");
+  if (sweep < FDTD_SWEEP_B_HALF || sweep > FDTD_SWEEP_E) return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid sweep");
+  DeviceGuard dg(h->device);
+  if (sweep == FDTD_SWEEP_E) {
+    if (int rc = run_e(h, h->host_step)) return rc;
+    ++h->host_step;
+    return FDTD_OK;
+  }
+  return run_b(h, sweep == FDTD_SWEEP_B_DOUBLE ? 2 : 1);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Device address and byte size of one stored plane of component c (0..5):
+// its E/B words (part 0) or its compensation words (part 1).
+unsigned char* slab_plane(fdtd_handle* h, int c, int plane, int part, size_t* bytes) {
+  const int64_t pe = h->form == Form::F64 ? h->g.plane : h->L.pplane;
+  const int64_t k = plane == FDTD_PLANE_HALO_BELOW ? -1
+                    : plane == FDTD_PLANE_FIRST    ? 0
+                    : plane == FDTD_PLANE_LAST     ? h->g.Nk - 1
+                                                   : h->g.Nk;
+  const size_t eb = part == 0 ? elem_bytes(h->form) : sizeof(LoT);
+  unsigned char* base = part == 0 ? static_cast<unsigned char*>(h->field[c]) : reinterpret_cast<unsigned char*>(h->lo[c]);
+  *bytes = eb * (size_t)pe;
+  return base + (int64_t)eb * pe * k;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdtd_slab_plane(fdtd_handle* h, int comp, int plane, int part, void** device_ptr, size_t* bytes) {
+  if (int rc = check_handle(h)) return rc;
+  if (!device_ptr || !bytes) return fail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  if (comp < FDTD_EX || comp > FDTD_BZ) return fail(FDTD_ERR_LOGIC, "ERROR: Invalid field component");
+  if (plane < FDTD_PLANE_HALO_BELOW || plane > FDTD_PLANE_HALO_ABOVE)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid plane");
+  if (!h->zhalo && (plane == FDTD_PLANE_HALO_BELOW || plane == FDTD_PLANE_HALO_ABOVE))
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "only a z slab has halo planes");
+  if (part != 0 && !(part == 1 && h->form == Form::F32C))
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "part 1 (compensation words) exists in the FP32_COMP form only");
+  *device_ptr = slab_plane(h, comp, plane, part, bytes);
+  return FDTD_OK;
+}
+
+int fdtd_slab_exchange(fdtd_handle* const* slabs, int n, int halo) {
+  if (!slabs || n <= 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "no slabs");
+  if (halo != FDTD_HALO_E && halo != FDTD_HALO_B) return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid halo");
+  for (int s = 0; s < n; ++s) {
+    const fdtd_handle* h = slabs[s];
+    if (!h || !h->zhalo) return fail(FDTD_ERR_INVALID_ARGUMENT, "every handle must be a z slab");
+    const fdtd_handle* h0 = slabs[0];
+    if (h->form != h0->form || h->g.Ni != h0->g.Ni || h->g.Nj != h0->g.Nj || h->device != h0->device ||
+        h->slab_nk_global != h0->slab_nk_global)
+      return fail(FDTD_ERR_INVALID_ARGUMENT, "slabs must share the form, the x-y grid and the device");
+    for (int c = 0; c < 6; ++c)
+      if (h->fp16_exp[c] != h0->fp16_exp[c]) return fail(FDTD_ERR_INVALID_ARGUMENT, "slabs must share FP16 exponents");
+    const int next = s + 1 < n ? slabs[s + 1]->slab_k0 : h0->slab_nk_global;
+    if ((s == 0 && h->slab_k0 != 0) || h->slab_k0 + h->g.Nk != next)
+      return fail(FDTD_ERR_INVALID_ARGUMENT, "slabs must tile the grid's planes in order");
+  }
+  DeviceGuard dg(slabs[0]->device);
+  // E: slab s's first owned plane of Ex, Ey becomes the halo above of slab
+  // s-1.  B: slab s's last owned plane of Bx, By becomes the halo below of
+  // slab s+1.  The ring closes periodically, as the reference's z wrap does.
+  const bool e_halo = halo == FDTD_HALO_E;
+  const int c0 = e_halo ? FDTD_EX : FDTD_BX;
+  const int from = e_halo ? FDTD_PLANE_FIRST : FDTD_PLANE_LAST;
+  const int to = e_halo ? FDTD_PLANE_HALO_ABOVE : FDTD_PLANE_HALO_BELOW;
+  const int parts = slabs[0]->form == Form::F32C ? 2 : 1;
+  auto dest = [&](int s) { return slabs[e_halo ? (s + n - 1) % n : (s + 1) % n]; };
+  for (int s = 0; s < n; ++s) FDTD_CUDA(cudaEventRecord(slabs[s]->xev[0], slabs[s]->stream), "halo exchange");
+  for (int s = 0; s < n; ++s) {
+    fdtd_handle* src = slabs[s];
+    fdtd_handle* dst = dest(s);
+    FDTD_CUDA(cudaStreamWaitEvent(dst->stream, src->xev[0], 0), "halo exchange");
+    for (int c = c0; c < c0 + 2; ++c)
+      for (int part = 0; part < parts; ++part) {
+        size_t nb = 0, nb2 = 0;
+        unsigned char* a = slab_plane(src, c, from, part, &nb);
+        unsigned char* b = slab_plane(dst, c, to, part, &nb2);
+        FDTD_CUDA(cudaMemcpyAsync(b, a, nb, cudaMemcpyDeviceToDevice, dst->stream), "halo exchange");
+      }
+  }
+  // A slab rewrites the planes it sent only after the copies have read them.
+  for (int s = 0; s < n; ++s) FDTD_CUDA(cudaEventRecord(slabs[s]->xev[1], slabs[s]->stream), "halo exchange");
+  for (int s = 0; s < n; ++s)
+    FDTD_CUDA(cudaStreamWaitEvent(slabs[s]->stream, dest(s)->xev[1], 0), "halo exchange");
   return FDTD_OK;
 }
 

@@ -59,13 +59,14 @@ cudaError_t launch_e_pml_fp64(const Grid& g, const Box& box, const Fp64Fields& F
 cudaError_t launch_b_pml_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const PmlFields& P,
                               cudaStream_t st);
 
-// kernels_f32.cu (padded layout)
+// kernels_f32.cu (padded layout): the sweeps over planes [kbeg, kend).
 template <class S>
-cudaError_t launch_b_f32(const PLayout& L, const S& st, const CoefSet& cs, int applications,
+cudaError_t launch_b_f32(const PLayout& L, const S& st, const CoefSet& cs, int applications, int kbeg, int kend,
                          cudaStream_t stream);
 template <class S>
 cudaError_t launch_e_f32(const PLayout& L, const S& st, const float* const J[3], bool dense_j,
-                         const CoefSet& cs, const SourceSet& ss, int64_t step, cudaStream_t stream);
+                         const CoefSet& cs, const SourceSet& ss, int64_t step, int kbeg, int kend,
+                         cudaStream_t stream);
 // Reads the state from `st` (through the TMA maps in `maps`, a TmaMaps
 // built by build_tma_maps for `st`'s arrays), writes the stepped state to `out`.
 template <class S>

@@ -69,6 +69,7 @@ struct fdtd_handle {
   double* d_tables = nullptr;
   float* d_tables_f = nullptr;  // FP32 hi tables, then FP32 lo tables
   int64_t tables_lo_off = 0;
+  int source_calls = 0;   // fdtd_add_source calls since the last clear (the index it returns)
   int64_t host_step = 0;  // completed update_fields steps
 
   // Step pipeline of the FP32-arithmetic forms (FP64 always uses the split
@@ -85,6 +86,26 @@ struct fdtd_handle {
   Box main_box() const {
     return Box{pml_size[0], g.Ni - pml_size[0], pml_size[1], g.Nj - pml_size[1], pml_size[2], g.Nk - pml_size[2]};
   }
+
+  // z slab (fdtd_slab_create): the handle owns planes [slab_k0, slab_k0 +
+  // g.Nk) of a grid of slab_nk_global planes.  Its arrays hold zhalo (1)
+  // more plane below and above the owned ones, which the halo exchange fills
+  // with the neighbouring slabs' boundary planes; field / lo / jf point at
+  // the first owned plane, so every host-facing call sees the owned grid.
+  // zhalo is 0 for an ordinary handle.
+  int zhalo = 0;
+  int slab_k0 = 0;
+  int slab_nk_global = 0;
+  cudaEvent_t xev[2] = {nullptr, nullptr};  // halo exchange ordering (sent, received)
+  // The planes a sweep updates, in the storage's plane numbering.
+  Box sweep_box() const {
+    Box b = main_box();
+    b.k0 += zhalo;
+    b.k1 += zhalo;
+    return b;
+  }
+  // Elements between the first stored plane and the first owned plane.
+  int64_t halo_elems() const { return form == Form::F64 ? zhalo * g.plane : zhalo * L.pplane; }
 
   int pipeline = FDTD_PIPELINE_AUTO;
   FusedConfig fused_cfg;
@@ -134,6 +155,24 @@ struct fdtd_handle {
   }
   StateView view() const { return make_view(field, lo); }
   StateView view_alt() const { return make_view(alt_field, alt_lo); }
+  // The storage the sweeps index: the owned planes and the halo planes.
+  StateView sweep_view() const {
+    StateView v = view();
+    if (zhalo == 0) return v;
+    v.g.Nk += 2 * zhalo;
+    v.g.cells = v.g.plane * v.g.Nk;
+    v.L = PLayout::make(g.Ni, g.Nj, g.Nk + 2 * zhalo);
+    const int64_t d = halo_elems();
+    for (int c = 0; c < 6; ++c) {
+      switch (form) {
+        case Form::F64: v.f64[c] -= d; break;
+        case Form::F32: v.s32.v[c] -= d; break;
+        case Form::F32C: v.s32c.hi[c] -= d; v.s32c.lo[c] -= d; break;
+        case Form::F16: v.s16.v[c] -= d; break;
+      }
+    }
+    return v;
+  }
   SourceSet source_set() const {
     SourceSet ss{};
     ss.count = (int)sources.size();

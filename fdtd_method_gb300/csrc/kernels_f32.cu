@@ -14,12 +14,12 @@
 
 namespace fdtd {
 
-// B update of column (i, j), planes k0 .. k0+kchunk-1.
+// B update of column (i, j), planes k0 .. min(k0+kchunk, kend)-1.
 template <class S, class A, int kApplications>
 __device__ __forceinline__ void b_column(const PLayout& L, const S& st, const CoefSet& cs, int i, int j, int k0,
-                                         int kchunk) {
-  if (i >= L.Ni || j >= L.Nj || k0 >= L.Nk) return;
-  const int k1 = min(k0 + kchunk, L.Nk);
+                                         int kchunk, int kend) {
+  if (i >= L.Ni || j >= L.Nj || k0 >= kend) return;
+  const int k1 = min(k0 + kchunk, kend);
   const Coef cx = cs.cb[0], cy = cs.cb[1], cz = cs.cb[2];
   const int64_t col = L.at(i, j, 0), col_in = L.at(i + 1, j, 0), col_jn = L.at(i, j + 1, 0);
 
@@ -48,9 +48,9 @@ __device__ __forceinline__ void b_column(const PLayout& L, const S& st, const Co
 }
 
 template <class S, class A, int kApplications>
-__global__ void __launch_bounds__(256) b_sweep(PLayout L, S st, CoefSet cs, int kchunk) {
+__global__ void __launch_bounds__(256) b_sweep(PLayout L, S st, CoefSet cs, int kchunk, int kbeg, int kend) {
   b_column<S, A, kApplications>(L, st, cs, blockIdx.x * blockDim.x + threadIdx.x,
-                                blockIdx.y * blockDim.y + threadIdx.y, blockIdx.z * kchunk, kchunk);
+                                blockIdx.y * blockDim.y + threadIdx.y, kbeg + blockIdx.z * kchunk, kchunk, kend);
 }
 
 // The leading B half step of every domain of a batch: block b belongs to the
@@ -70,20 +70,20 @@ __global__ void __launch_bounds__(256) b_sweep_batch(const BatchDomain<S>* __res
   const int nbx = (d.L.Ni + 31) / 32, nby = (d.L.Nj + 7) / 8;
   const int bx = (int)(local % nbx), by = (int)((local / nbx) % nby), bz = (int)(local / ((int64_t)nbx * nby));
   b_column<S, A, 1>(d.L, d.s[parity], d.cs, bx * 32 + threadIdx.x, by * 8 + threadIdx.y, bz * kBatchBChunk,
-                    kBatchBChunk);
+                    kBatchBChunk, d.L.Nk);
 }
 
 template <class S, class A, bool kDenseJ, bool kSources>
 __global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __restrict__ Jx,
                                                const float* __restrict__ Jy,
                                                const float* __restrict__ Jz, CoefSet cs, int kchunk,
-                                               SourceSet ss, int64_t step) {
+                                               int kbeg, int kend, SourceSet ss, int64_t step) {
   using T = typename A::Cur;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k0 = blockIdx.z * kchunk;
-  if (i >= L.Ni || j >= L.Nj || k0 >= L.Nk) return;
-  const int k1 = min(k0 + kchunk, L.Nk);
+  const int k0 = kbeg + blockIdx.z * kchunk;
+  if (i >= L.Ni || j >= L.Nj || k0 >= kend) return;
+  const int k1 = min(k0 + kchunk, kend);
   const Coef cx = cs.ce[0], cy = cs.ce[1], cz = cs.ce[2];
   const int64_t col = L.at(i, j, 0), col_ip = L.at(i - 1, j, 0), col_jp = L.at(i, j - 1, 0);
   const int64_t dcol = i + (int64_t)j * L.Ni;  // dense current index
@@ -127,30 +127,35 @@ __global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __r
 template <class S> struct ArithOf { using type = ArithPlain; };
 template <> struct ArithOf<StoreF32C> { using type = ArithComp; };
 
-static dim3 sweep_grid(const PLayout& L, int kchunk) {
-  return dim3((L.Ni + 31) / 32, (L.Nj + 7) / 8, (L.Nk + kchunk - 1) / kchunk);
+static dim3 sweep_grid(const PLayout& L, int kbeg, int kend, int kchunk) {
+  return dim3((L.Ni + 31) / 32, (L.Nj + 7) / 8, (kend - kbeg + kchunk - 1) / kchunk);
 }
 
 template <class S>
-cudaError_t launch_b_f32(const PLayout& L, const S& st, const CoefSet& cs, int applications,
+cudaError_t launch_b_f32(const PLayout& L, const S& st, const CoefSet& cs, int applications, int kbeg, int kend,
                          cudaStream_t stream) {
   using A = typename ArithOf<S>::type;
+  if (kbeg < 0 || kend > L.Nk) return cudaErrorInvalidValue;
+  if (kend <= kbeg) return cudaSuccess;
   const int kchunk = 16;
-  dim3 block(32, 8), grid = sweep_grid(L, kchunk);
-  if (applications == 2) b_sweep<S, A, 2><<<grid, block, 0, stream>>>(L, st, cs, kchunk);
-  else b_sweep<S, A, 1><<<grid, block, 0, stream>>>(L, st, cs, kchunk);
+  dim3 block(32, 8), grid = sweep_grid(L, kbeg, kend, kchunk);
+  if (applications == 2) b_sweep<S, A, 2><<<grid, block, 0, stream>>>(L, st, cs, kchunk, kbeg, kend);
+  else b_sweep<S, A, 1><<<grid, block, 0, stream>>>(L, st, cs, kchunk, kbeg, kend);
   return cudaGetLastError();
 }
 
 template <class S>
 cudaError_t launch_e_f32(const PLayout& L, const S& st, const float* const J[3], bool dense_j,
-                         const CoefSet& cs, const SourceSet& ss, int64_t step, cudaStream_t stream) {
+                         const CoefSet& cs, const SourceSet& ss, int64_t step, int kbeg, int kend,
+                         cudaStream_t stream) {
   using A = typename ArithOf<S>::type;
+  if (kbeg < 0 || kend > L.Nk) return cudaErrorInvalidValue;
+  if (kend <= kbeg) return cudaSuccess;
   const int kchunk = 16;
-  dim3 block(32, 8), grid = sweep_grid(L, kchunk);
+  dim3 block(32, 8), grid = sweep_grid(L, kbeg, kend, kchunk);
   const bool src = ss.count > 0;
 #define FDTD_E32(DJ, SRC) \
-  e_sweep<S, A, DJ, SRC><<<grid, block, 0, stream>>>(L, st, J[0], J[1], J[2], cs, kchunk, ss, step)
+  e_sweep<S, A, DJ, SRC><<<grid, block, 0, stream>>>(L, st, J[0], J[1], J[2], cs, kchunk, kbeg, kend, ss, step)
   if (dense_j && src) FDTD_E32(true, true);
   else if (dense_j) FDTD_E32(true, false);
   else if (src) FDTD_E32(false, true);
@@ -171,10 +176,10 @@ cudaError_t launch_b_f32_batch(const void* doms, const int64_t* block_start, int
 }
 
 #define FDTD_INSTANTIATE(S)                                                                            \
-  template cudaError_t launch_b_f32<S>(const PLayout&, const S&, const CoefSet&, int, cudaStream_t); \
+  template cudaError_t launch_b_f32<S>(const PLayout&, const S&, const CoefSet&, int, int, int, cudaStream_t); \
   template cudaError_t launch_b_f32_batch<S>(const void*, const int64_t*, int, int64_t, int, cudaStream_t); \
   template cudaError_t launch_e_f32<S>(const PLayout&, const S&, const float* const[3], bool,         \
-                                       const CoefSet&, const SourceSet&, int64_t, cudaStream_t);
+                                       const CoefSet&, const SourceSet&, int64_t, int, int, cudaStream_t);
 FDTD_INSTANTIATE(StoreF32)
 FDTD_INSTANTIATE(StoreF32C)
 FDTD_INSTANTIATE(StoreF16)

@@ -288,6 +288,59 @@ int fdtd_batch_synchronize(fdtd_batch* b);
  * calls that overlap on the GPU race. */
 int fdtd_field_sums_noalloc(const double* const fields[6], int64_t cells, double* out_device, void* stream);
 
+/* ------------------------------------------------------------------------
+ * z slabs: the domain decomposition of the reference's coarray program
+ * (coarray/fdtd.F90:90-98, 149-164).  A slab handle owns planes
+ * [k_begin, k_end) of the grid `params` plus one halo plane below and one
+ * above.  Every host-facing call (fdtd_copy_field_*, fdtd_get_field,
+ * fdtd_export_field, fdtd_field_sums, fdtd_get_params) sees the owned planes
+ * only: a grid of Ni x Nj x (k_end - k_begin), az/bz moved to the slab.
+ * fdtd_add_source takes boxes in the coordinates of the whole grid and
+ * keeps the part in the owned planes.
+ *
+ * A set of slabs that tile the planes in order (k_begin of the first 0, each
+ * k_end the next k_begin, the last k_end Nk) steps like one handle of the
+ * whole grid when every slab runs, per update_fields,
+ *     B_HALF (B_DOUBLE between steps), exchange B, E, exchange E, B_HALF,
+ * and exchange E once before the first B sweep (after the fields were set):
+ * the results are the whole-grid handle's bit for bit, in every precision.
+ * fdtd_step on a slab gives FDTD_ERR_UNSUPPORTED; slabs run the split sweeps
+ * (no fused pipeline, no autotuner) and have no PML.
+ *
+ * One GPU: fdtd_slab_exchange copies the boundary planes between the slabs
+ * of one device.  Several GPUs: each rank exchanges the planes that
+ * fdtd_slab_plane addresses with its neighbours (NCCL send / receive), in
+ * the same order. */
+int fdtd_slab_create(const fdtd_params* params, double dt, int precision, int k_begin, int k_end,
+                     fdtd_handle** out);
+/* Owned planes and the whole grid's plane count (an ordinary handle: 0, Nk, Nk). */
+int fdtd_slab_info(fdtd_handle* h, int* k_begin, int* k_end, int* nk_global);
+
+enum fdtd_sweep {
+    FDTD_SWEEP_B_HALF = 0,   /* B += curl term (kokkos_functors.h:128-151), once  */
+    FDTD_SWEEP_B_DOUBLE = 1, /* the same term added twice (two half steps)        */
+    FDTD_SWEEP_E = 2         /* E update of the current step; the step count + 1  */
+};
+/* One sweep over the owned planes (any non-PML handle: the whole grid). */
+int fdtd_slab_sweep(fdtd_handle* h, int sweep);
+
+enum fdtd_plane {
+    FDTD_PLANE_HALO_BELOW = 0, FDTD_PLANE_FIRST = 1, FDTD_PLANE_LAST = 2, FDTD_PLANE_HALO_ABOVE = 3
+};
+enum fdtd_halo {
+    FDTD_HALO_E = 0, /* Ex, Ey of each slab's first plane -> the halo above of the slab below */
+    FDTD_HALO_B = 1  /* Bx, By of each slab's last plane  -> the halo below of the slab above */
+};
+/* Device address and size in bytes of one stored plane of component comp
+ * (FDTD_EX..FDTD_BZ) in the handle's storage form: part 0 the E/B words,
+ * part 1 the compensation words (FP32_COMP).  The FP32-arithmetic forms store
+ * padded planes; a plane is copied whole. */
+int fdtd_slab_plane(fdtd_handle* h, int comp, int plane, int part, void** device_ptr, size_t* bytes);
+/* Halo exchange between the n slabs of one device, listed in plane order
+ * (the last one's neighbour above is the first: the grid is periodic).
+ * Asynchronous: ordered after each slab's queued work and before its next. */
+int fdtd_slab_exchange(fdtd_handle* const* slabs, int n, int halo);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,10 @@ class OracleSource(ctypes.Structure):
                 ("gx", _D), ("gy", _D), ("gz", _D), ("amp", _D), ("n_amp", ctypes.c_long)]
 
 
+class OracleBox(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_long) for n in ("i0", "i1", "j0", "j1", "k0", "k1")]
+
+
 def build_oracle(force=False):
     """Compiles liboracle.so (and nothing else) with the oracle's Makefile."""
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "fdtd_oracle.c")):
@@ -69,6 +73,13 @@ def oracle_lib():
                                        ctypes.POINTER(OracleSource), ctypes.c_int, ctypes.c_long, ctypes.c_int,
                                        ctypes.POINTER(_D)]
         lib.oracle_pml_run.restype = None
+        for name in ("oracle_update_B_box",):
+            getattr(lib, name).argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, OracleBox] + [_D] * 6 + \
+                [ctypes.c_double] * 3
+            getattr(lib, name).restype = None
+        lib.oracle_update_E_box.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, OracleBox] + [_D] * 9 + \
+            [ctypes.c_double] * 4
+        lib.oracle_update_E_box.restype = None
         lib.oracle_field_sums.argtypes = [ctypes.c_long, ctypes.POINTER(_D), _D]
         lib.oracle_field_sums.restype = None
         lib.oracle_threads.restype = ctypes.c_int
@@ -202,6 +213,43 @@ class OraclePML(Oracle):
 
     def step_driver(self, n=1):
         raise NotImplementedError("the PML oracle steps through step()")
+
+
+class OracleSlab:
+    """A z slab of the oracle: planes [k_begin, k_end) of the grid `params`
+    stored with one halo plane below and above (the layout of the coarray
+    program's slabs with their next_E / pred_B halo arrays,
+    coarray/fdtd.F90:90-98), updated by the box sweeps of fdtd_oracle.c over
+    the owned planes.  J is dense (the owned planes of the whole grid's J)."""
+
+    def __init__(self, params, dt, k_begin, k_end):
+        self.coef = coefficients(params, dt)
+        self.Ni, self.Nj = params.Ni, params.Nj
+        self.nk = int(k_end) - int(k_begin)
+        self.plane = params.Ni * params.Nj
+        self.f = [np.zeros(self.plane * (self.nk + 2)) for _ in range(9)]
+        self.step_index = 0
+
+    def owned(self, comp):
+        """View of the owned planes of component comp (flat, i fastest)."""
+        return self.f[int(comp)][self.plane:self.plane * (self.nk + 1)]
+
+    def plane_view(self, comp, k):
+        """View of stored plane k (0: halo below, nk + 1: halo above)."""
+        return self.f[int(comp)][self.plane * k:self.plane * (k + 1)]
+
+    def sweep(self, kind):
+        """kind 0: B half step, 1: two B half steps, 2: E (kokkos_functors.h:128-151, :64-90)."""
+        box = OracleBox(0, self.Ni, 0, self.Nj, 1, self.nk + 1)
+        nk = self.nk + 2
+        f, c = self.f, self.coef
+        if kind == 2:
+            oracle_lib().oracle_update_E_box(self.Ni, self.Nj, nk, box, *[_ptr(f[q]) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)],
+                                             c[6], c[0], c[1], c[2])
+            self.step_index += 1
+            return
+        for _ in range(2 if kind == 1 else 1):
+            oracle_lib().oracle_update_B_box(self.Ni, self.Nj, nk, box, *[_ptr(f[q]) for q in range(6)], c[3], c[4], c[5])
 
 
 # ---------------------------------------------------------------------------
