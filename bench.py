@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=512, help="grid edge (cells)")
+    ap.add_argument("--grid", type=int, nargs=3, metavar=("NI", "NJ", "NK"), default=None,
+                    help="grid extents (overrides --n; profiling captures of part of the benchmark grid)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--precision", default="fp32_comp", choices=["fp32_comp", "fp32", "fp16_scaled"])
     ap.add_argument("--pipeline", default="auto", choices=["auto", "fused", "split"])
@@ -80,15 +82,16 @@ def parse_args():
 
 def workload(args):
     from fdtd_method_gb300.sources import baseline_pulse, normalised_parameters
-    p = normalised_parameters(args.n, args.n, args.n)
+    p = normalised_parameters(*(args.grid or (args.n, args.n, args.n)))
     src = baseline_pulse(p, seed=args.seed, n_steps=args.run_length)
     return p, src
 
 
 def config_dict(args, p, src):
     m = src.meta
-    return {"workload": "%d^3 periodic Yee step, 1 Jz Gaussian pulse (sigma 8 cells, A=%.3f, T=%.2f steps, seed %d), "
-                        "FP32-compensated vs FP64" % (args.n, m["A"], m["T"], args.seed),
+    shape = "%d^3" % args.n if not args.grid else "%dx%dx%d" % tuple(args.grid)
+    return {"workload": "%s periodic Yee step, 1 Jz Gaussian pulse (sigma 8 cells, A=%.3f, T=%.2f steps, seed %d), "
+                        "FP32-compensated vs FP64" % (shape, m["A"], m["T"], args.seed),
             "grid": [p.Ni, p.Nj, p.Nk], "cells": p.cells, "dt": "0.5/sqrt(3) (c=1, dx=1)",
             "chosen_precision": args.precision, "run_length": args.run_length,
             "l2": "inputs larger than L2 (state >= 4 GB per form vs 129 MB L2); no flush",
@@ -123,7 +126,7 @@ def cpu_worker(args):
 def run_cpu_baseline(args, steps=0, warmup=1, budget=15.0):
     cmd = [sys.executable, os.path.abspath(__file__), "--cpu-worker", "--n", str(args.n), "--seed", str(args.seed),
            "--run-length", str(args.run_length), "--cpu-steps", str(steps), "--cpu-warmup", str(warmup),
-           "--cpu-budget-s", str(budget)]
+           "--cpu-budget-s", str(budget)] + (["--grid"] + [str(v) for v in args.grid] if args.grid else [])
     env = dict(os.environ)
     env.setdefault("OMP_PROC_BIND", "close")
     r = subprocess.run(cmd, capture_output=True, text=True, env=env)

@@ -334,7 +334,7 @@ int fdtd_batch_set_config(fdtd_batch* b, int tile_y, int kchunk, int use_graphs)
     return bfail(FDTD_ERR_INVALID_ARGUMENT, "tile_y must be 0 (default), 6, 14 or 30");
   if (kchunk < 0) return bfail(FDTD_ERR_INVALID_ARGUMENT, "kchunk must be >= 0");
   b->cfg.tile_y = tile_y ? tile_y : 14;
-  b->cfg.kchunk = kchunk ? kchunk : 24;
+  b->cfg.kchunk = kchunk ? kchunk : 48;
   b->cfg.cells_per_thread = 1;
   b->use_graphs = use_graphs != 0;
   b->dirty = true;
@@ -388,7 +388,7 @@ int fdtd_batch_autotune(fdtd_batch* b, int sweeps, fdtd_tune_result* out) {
   // The timed sweeps read copy `parity` and write the other copy: the state
   // is left as it was.  Tables are rebuilt per candidate (copy 0 = current).
   static const int rows[] = {6, 14, 30};
-  static const int chunks[] = {16, 24, 32, 48};
+  static const int chunks[] = {16, 24, 32, 48, 64};
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   FDTD_BCUDA(cudaEventCreate(&e0), "autotune events");
   if (cudaEventCreate(&e1) != cudaSuccess) {

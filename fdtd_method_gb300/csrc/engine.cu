@@ -281,7 +281,7 @@ int run_fused(fdtd_handle* h, int64_t step, int apps) {
 // two cells per thread: 6 or 14), each with every chunk length.
 constexpr int kTuneRows1[] = {6, 14, 30};
 constexpr int kTuneRows2[] = {6, 14};
-constexpr int kTuneChunks[] = {16, 24, 32, 48};
+constexpr int kTuneChunks[] = {16, 24, 32, 48, 64, 96};
 
 struct TuneKey {
   int form, Ni, Nj, Nk;
@@ -880,7 +880,7 @@ int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int 
     return fail(FDTD_ERR_UNSUPPORTED, "a z slab runs the split sweeps");
   h->pipeline = pipeline;
   h->fused_cfg.tile_y = tile_y ? tile_y : 14;
-  h->fused_cfg.kchunk = kchunk ? kchunk : 24;
+  h->fused_cfg.kchunk = kchunk ? kchunk : 48;
   h->fused_cfg.cells_per_thread = cells_per_thread ? cells_per_thread : 1;
   return FDTD_OK;
 }

@@ -27,7 +27,7 @@ struct CoefSet {
 // planes per tile.
 struct FusedConfig {
   int tile_y = 14;
-  int kchunk = 24;  // short chunks keep neighbouring tiles in step, so halo sectors hit in L2
+  int kchunk = 48;  // planes per tile (the autotuner picks from 16 to 96)
   int cells_per_thread = 1;  // 1: 32-wide tiles (kernels_fused1.cu); 2: 64-wide, packed float2
 };
 
@@ -121,8 +121,8 @@ cudaError_t launch_b_f32_batch(const void* doms, const int64_t* block_start, int
 // tma_maps.cu: tensor maps of the six hi arrays (and six lo arrays of the
 // compensated form) for a fused tile of `tile_y` interior rows.
 enum class HiType { F32, F16 };
-// Store maps of the fused1 kernel: the grid cells of each array (ghosts and
-// margins excluded), box 32 x tile_y.
+// Store maps of the fused1 kernel: the grid rows of each array with their x
+// margins (x coordinate kPadX + x is cell x), box 32 x tile_y.
 cudaError_t build_tma_store_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], LoT* const lo[6],
                                  int tile_y);
 // trimmed (the one-cell-per-thread kernel): boxes of components other than

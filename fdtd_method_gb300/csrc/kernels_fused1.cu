@@ -15,11 +15,12 @@
 //        planes ahead through an mbarrier ring;
 //   out  E'(t) and B'(t-1) are written to shared staging boxes of 32 x RY in
 //        their stored encoding; one thread stores them with TMA through
-//        interior-only tensor maps (the copy engine clips rows past the
-//        grid; a tile narrower than 32 columns stores with plain stores,
-//        since clipping along x is in 16-byte units).  Tiles on the grid's
-//        edges also write the ghost copies of their edge cells with plain
-//        stores.
+//        tensor maps of the grid rows (the copy engine clips rows past the
+//        grid; a tile narrower than 32 columns stores with plain stores).
+//        The first and last tile columns store the same boxes into the x
+//        margins as well, which fills the ghost columns with bulk copies
+//        where the alignment allows; the remaining ghost copies (ghost
+//        rows, corners, unaligned columns) are plain stores.
 // The E' staging box doubles as the exchange plane from which the next
 // iteration reads E'(t-1) at i+1 and j+1; it has two extra rows, holding the
 // halo row's and the halo column's E'.
@@ -221,7 +222,22 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
   // grid's last cell.  Such tiles (the last tile column when Ni is not a
   // multiple of 32) store with plain per-thread stores instead.
   const bool tma_out = (nx == 32);
-  const bool edge_cell = interior && (xl == 0 || xl == L.Ni - 1 || yl == 0 || yl == L.Nj - 1);
+  // Ghost columns.  By bulk copy (compensated form): the first tile column
+  // also stores its boxes into the right margin (cells 0..31 at
+  // x = Ni..Ni+31) when that start is on a 16-byte boundary for every element
+  // size (Ni a multiple of 8); the last one, when full, into the left margin
+  // (cells Ni-32..Ni-1 at x = -32..-1).  Every value there is a periodic
+  // copy.  Otherwise the
+  // halo-row warp copies the edge column's stored words from staging to the
+  // ghost column, one lane per row.  Threads write only the ghost rows and
+  // their corners.  (The flags are recomputed where used: cheaper than
+  // keeping them live across the loop.)
+  // The bulk copies pay for their extra margin bytes in the compensated form
+  // (whose scalar ghost stores are twice as many: hi and lo words); the plain
+  // forms run faster with the halo-row warp's copies alone.
+  auto ghost_r = [&]() { return P::kLo && tma_out && x0 == 0 && L.Ni % 8 == 0; };
+  auto ghost_l = [&]() { return P::kLo && tma_out && x0 + 32 == L.Ni; };
+  const bool edge_cell = interior && (yl == 0 || yl == L.Nj - 1);
 
   // Element offsets of this thread in the exchange rows: where it publishes
   // E', and where it finds E' at (r+1, cx) and (r, cx+1).
@@ -412,14 +428,14 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
     // Ghost copies of edge cells (their tiles only).
     if (tile_edge && edge_cell) {
       if (t < k1) {
-        store_ghost_copies(out, L, 0, xl, yl, t, nex);
-        store_ghost_copies(out, L, 1, xl, yl, t, ney);
-        store_ghost_copies(out, L, 2, xl, yl, t, nez);
+        store_ghost_rows(out, L, true, true, 0, xl, yl, t, nex);
+        store_ghost_rows(out, L, true, true, 1, xl, yl, t, ney);
+        store_ghost_rows(out, L, true, true, 2, xl, yl, t, nez);
       }
       if (t > k0) {
-        store_ghost_copies(out, L, 3, xl, yl, t - 1, nbx);
-        store_ghost_copies(out, L, 4, xl, yl, t - 1, nby);
-        store_ghost_copies(out, L, 5, xl, yl, t - 1, nbz);
+        store_ghost_rows(out, L, true, true, 3, xl, yl, t - 1, nbx);
+        store_ghost_rows(out, L, true, true, 4, xl, yl, t - 1, nby);
+        store_ghost_rows(out, L, true, true, 5, xl, yl, t - 1, nbz);
       }
     }
 
@@ -434,17 +450,45 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
     // again next iteration) before anyone passes this barrier.
     if (leader) bulk_wait_read_all();
     __syncthreads();
+    if (w == RY && lane < ny && (x0 == 0 || x0 + nx == L.Ni)) {
+      // ghost columns the bulk copies do not write: x = Ni from column 0,
+      // x = -1 from column nx-1, row y0+lane, copied as stored words
+#pragma unroll 1
+      for (int side = 0; side < 2; ++side) {
+        const bool on = side == 0 ? (x0 == 0 && !ghost_r()) : (x0 + nx == L.Ni && !ghost_l());
+        if (!on) continue;
+        const int col = side == 0 ? 0 : nx - 1;
+        const int64_t g = L.at(side == 0 ? L.Ni : -1, y0 + lane, 0);
+        const HiT* eh = reinterpret_cast<const HiT*>(xb + P::kXHi) + lane * 32 + col;
+        const LoT* eq = reinterpret_cast<const LoT*>(xb + P::kXLo) + lane * 32 + col;
+        const HiT* bh = reinterpret_cast<const HiT*>(bb) + lane * 32 + col;
+        const LoT* bq = reinterpret_cast<const LoT*>(bb + P::kBLo) + lane * 32 + col;
+        if (t < k1)
+          for (int c = 0; c < 3; ++c)
+            out.store_words(c, g + (int64_t)t * L.pplane, eh[c * P::kXComp], P::kLo ? eq[c * P::kXComp] : LoT(0));
+        if (t > k0)
+          for (int c = 0; c < 3; ++c)
+            out.store_words(3 + c, g + (int64_t)(t - 1) * L.pplane, bh[c * P::kBComp],
+                            P::kLo ? bq[c * P::kBComp] : LoT(0));
+      }
+    }
     if (leader) {
-      if (tma_out && t < k1)
-        for (int c = 0; c < 3; ++c) {
-          tma_store_3d(&maps.st.hi[c], xb + P::kXHi + c * P::kXComp * P::HS, x0, y0, t);
-          if (P::kLo) tma_store_3d(&maps.st.lo[c], xb + P::kXLo + c * P::kXComp * P::LS, x0, y0, t);
-        }
-      if (tma_out && t > k0)
-        for (int c = 0; c < 3; ++c) {
-          tma_store_3d(&maps.st.hi[3 + c], bb + c * P::kBComp * P::HS, x0, y0, t - 1);
-          if (P::kLo) tma_store_3d(&maps.st.lo[3 + c], bb + P::kBLo + c * P::kBComp * P::LS, x0, y0, t - 1);
-        }
+      // the tile's boxes at its own columns, then the margins it fills
+#pragma unroll 1
+      for (int g = 0; g < 3 && tma_out; ++g) {
+        if ((g == 1 && !ghost_r()) || (g == 2 && !ghost_l())) continue;
+        const int xs = g == 0 ? x0 + kPadX : g == 1 ? L.Ni + kPadX : 0;
+        if (t < k1)
+          for (int c = 0; c < 3; ++c) {
+            tma_store_3d(&maps.st.hi[c], xb + P::kXHi + c * P::kXComp * P::HS, xs, y0, t);
+            if (P::kLo) tma_store_3d(&maps.st.lo[c], xb + P::kXLo + c * P::kXComp * P::LS, xs, y0, t);
+          }
+        if (t > k0)
+          for (int c = 0; c < 3; ++c) {
+            tma_store_3d(&maps.st.hi[3 + c], bb + c * P::kBComp * P::HS, xs, y0, t - 1);
+            if (P::kLo) tma_store_3d(&maps.st.lo[3 + c], bb + P::kBLo + c * P::kBComp * P::LS, xs, y0, t - 1);
+          }
+      }
       bulk_commit();
       if (t + NS <= k1) issue(t + NS);
     }
@@ -612,7 +656,7 @@ cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const
                               const float* const J[3], bool dense_j, const CoefSet& cs, const SourceSet& ss,
                               int64_t step, int applications, const FusedConfig& cfg, int* err,
                               cudaStream_t stream) {
-  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 24;
+  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 48;
   const StepMaps& m = *static_cast<const StepMaps*>(maps);
   if (cfg.tile_y == 6)
     return launch1_ry<S, 6>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);

@@ -62,6 +62,26 @@ __device__ __forceinline__ void store_ghost_copies(const S& st, const PLayout& L
   }
 }
 
+// store_ghost_copies without the ghost column of the cell's own row where a
+// bulk copy writes it: x = Ni (cell 0) when `right`, x = -1 (cell Ni-1)
+// when `left`.  The ghost rows and their corners are still written.
+template <class S, class V>
+__device__ __forceinline__ void store_ghost_rows(const S& st, const PLayout& L, bool right, bool left, int c,
+                                                 int x, int y, int z, V v) {
+  const bool xl = (x == 0), xh = (x == L.Ni - 1), yl = (y == 0), yh = (y == L.Nj - 1);
+  if (xl && !right) st.store(c, L.at(L.Ni, y, z), v);
+  if (xh && !left) st.store(c, L.at(-1, y, z), v);
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    const bool on = b == 0 ? yl : yh;
+    if (!on) continue;
+    const int yg = b == 0 ? L.Nj : -1;
+    st.store(c, L.at(x, yg, z), v);
+    if (xl) st.store(c, L.at(L.Ni, yg, z), v);
+    if (xh) st.store(c, L.at(-1, yg, z), v);
+  }
+}
+
 // Stores v at (x, y, z) and at every ghost position that mirrors it.
 template <class S, class V>
 __device__ __forceinline__ void store_with_ghosts(const S& st, const PLayout& L, int c, int x, int y,

@@ -33,6 +33,8 @@ struct StoreF32 {
   __device__ __forceinline__ Pair decode(int, float h, uint16_t) const { return Pair{h, 0.f}; }
   __device__ __forceinline__ Pair load(int c, int64_t idx) const { return Pair{v[c][idx], 0.f}; }
   __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const { v[c][idx] = p.hi; }
+  // Stores already encoded words (enc_hi / enc_lo).
+  __device__ __forceinline__ void store_words(int c, int64_t idx, float h, uint16_t) const { v[c][idx] = h; }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const { return (double)v[c][idx]; }
   // The value a store followed by a load returns.
   __device__ __forceinline__ Pair quantize(int, Pair p) const { return Pair{p.hi, 0.f}; }
@@ -55,6 +57,7 @@ struct StoreF16 {
   __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const {
     v[c][idx] = __float2half_rn(__fmul_rn(p.hi, scale[c]));
   }
+  __device__ __forceinline__ void store_words(int c, int64_t idx, __half h, uint16_t) const { v[c][idx] = h; }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const {
     return (double)__half2float(v[c][idx]) * (double)inv_scale[c];
   }
@@ -87,6 +90,10 @@ struct StoreF32C {
   __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const {
     hi[c][idx] = p.hi;
     lo[c][idx] = float_to_bf16_bits(p.lo);
+  }
+  __device__ __forceinline__ void store_words(int c, int64_t idx, float h, LoT q) const {
+    hi[c][idx] = h;
+    lo[c][idx] = q;
   }
   __device__ __forceinline__ Pair quantize(int, Pair p) const {
     return Pair{p.hi, bf16_bits_to_float(float_to_bf16_bits(p.lo))};

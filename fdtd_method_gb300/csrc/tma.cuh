@@ -15,8 +15,8 @@ struct TmaMaps {
 };
 
 // Maps of one fused step launch: tile loads from the current copy and tile
-// stores into the second copy (interior-only maps, so stores past the grid's
-// last row or column are clipped by the copy engine).
+// stores into the second copy (maps of the grid rows and their x margins, so
+// stores past the grid's last row are clipped by the copy engine).
 struct StepMaps {
   TmaMaps ld;
   TmaMaps st;

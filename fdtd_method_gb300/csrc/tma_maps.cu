@@ -46,15 +46,17 @@ bool encode(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// One 3-D map over the grid cells of a padded array (ghosts and margins
-// excluded): dims {Ni, Nj, Nk}, box {32, tile_y, 1}.  A store through it
-// writes nothing outside the grid.
-bool encode_interior(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const PLayout& L,
-                     int tile_y) {
+// One 3-D map over the grid rows of a padded array with their x margins
+// (ghost rows excluded): dims {kPadX + Ni + kPadX, Nj, Nk} from padded
+// column 0, box {32, tile_y, 1}.  x coordinate kPadX + x is cell x; a store
+// at 0 fills the left margin (cells -32 .. -1) and one at kPadX + Ni the
+// right margin's first 32 columns.  Rows outside the grid are not written.
+bool encode_store(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const PLayout& L,
+                  int tile_y) {
   EncodeTiled fn = encode_fn();
   if (!fn) return false;
-  void* origin = static_cast<unsigned char*>(base) + L.at(0, 0, 0) * es;
-  const cuuint64_t dims[3] = {(cuuint64_t)L.Ni, (cuuint64_t)L.Nj, (cuuint64_t)L.Nk};
+  void* origin = static_cast<unsigned char*>(base) + L.at(-kPadX, 0, 0) * es;
+  const cuuint64_t dims[3] = {(cuuint64_t)(L.Ni + 2 * kPadX), (cuuint64_t)L.Nj, (cuuint64_t)L.Nk};
   const cuuint64_t strides[2] = {(cuuint64_t)(L.pitch * es), (cuuint64_t)(L.pplane * es)};
   const cuuint32_t box[3] = {32, (cuuint32_t)tile_y, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
@@ -72,8 +74,8 @@ cudaError_t build_tma_store_maps(void* maps, const PLayout& L, HiType ht, void* 
   const CUtensorMapDataType dt = ht == HiType::F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
   const size_t es = ht == HiType::F32 ? 4 : 2;
   for (int c = 0; c < 6; ++c) {
-    if (!encode_interior(&m->hi[c], dt, es, hi[c], L, tile_y)) return cudaErrorInvalidValue;
-    if (lo && lo[c] && !encode_interior(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, sizeof(LoT), lo[c], L, tile_y))
+    if (!encode_store(&m->hi[c], dt, es, hi[c], L, tile_y)) return cudaErrorInvalidValue;
+    if (lo && lo[c] && !encode_store(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, sizeof(LoT), lo[c], L, tile_y))
       return cudaErrorInvalidValue;
   }
   return cudaSuccess;

@@ -209,7 +209,7 @@ int fdtd_set_kernel_timing(fdtd_handle* h, int enabled);
  * one sweep per half step.  All give bit-identical results.  The fused
  * launch is shaped by tile_y (interior rows of a tile: 6, 14 or 30; 0 = 14;
  * 30 only with cells_per_thread 1),
- * kchunk (planes per tile; 0 = 24) and cells_per_thread (1: 32-wide tiles,
+ * kchunk (planes per tile; 0 = 48) and cells_per_thread (1: 32-wide tiles,
  * 2: 64-wide tiles with packed two-cell arithmetic; 0 = 1).  The FP64 form
  * always uses the split sweeps. */
 enum fdtd_pipeline { FDTD_PIPELINE_AUTO = 0, FDTD_PIPELINE_SPLIT = 1, FDTD_PIPELINE_FUSED = 2 };
@@ -219,7 +219,7 @@ int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t laun
 /* Autotuner (new).  Times `sweeps` fused sweeps (0 = 10) for every candidate
  * launch shape of the FP32-arithmetic forms (cells_per_thread 1 with tile_y
  * 6, 14 and 30; cells_per_thread 2 with tile_y 6 and 14; each with kchunk 16,
- * 24, 32 and 48) on the handle's own grid, and keeps the fastest
+ * 24, 32, 48, 64 and 96) on the handle's own grid, and keeps the fastest
  * (fdtd_set_pipeline's shape arguments).  The timed sweeps read the current
  * state and write the handle's second copy, so the simulation state does not
  * change.  Results are cached per (precision, Ni, Nj, Nk) in the process;
@@ -269,7 +269,7 @@ int fdtd_batch_get_step(fdtd_batch* b, int64_t* step);
 int fdtd_batch_tiles(fdtd_batch* b, int64_t* tiles);
 int fdtd_batch_set_stream(fdtd_batch* b, void* stream);
 /* Autotuner of the batch: times `sweeps` (0 = 5) persistent fused sweeps of
- * every domain for tile_y 6, 14 and 30 with kchunk 16, 24, 32 and 48, and
+ * every domain for tile_y 6, 14 and 30 with kchunk 16, 24, 32, 48 and 64, and
  * keeps the fastest; the state does not change.  Synchronous. */
 int fdtd_batch_autotune(fdtd_batch* b, int sweeps, fdtd_tune_result* out);
 int fdtd_batch_synchronize(fdtd_batch* b);

@@ -134,7 +134,8 @@ def _run(p, prec, vals, srcs, steps, pipeline, tile_y=0, kchunk=0, dense_j=None,
                                                  ((64, 28, 16), 14, 8), ((31, 15, 129), 6, 64),
                                                  ((2, 70, 3), 6, 2), ((33, 9, 40), 14, 7),
                                                  ((96, 42, 5), 6, 3), ((70, 61, 9), 30, 4),
-                                                 ((33, 31, 6), 30, 64)])
+                                                 ((33, 31, 6), 30, 64), ((32, 20, 11), 14, 24),
+                                                 ((40, 17, 9), 14, 24), ((128, 30, 12), 30, 24)])
 def test_fused_step_equals_split_sweeps(prec, shape, tile_y, kchunk, cpt):
     if tile_y == 30 and cpt == 2:
         pytest.skip("30-row tiles exist for one cell per thread only")
