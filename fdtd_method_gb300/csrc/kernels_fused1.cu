@@ -223,11 +223,11 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
   // multiple of 32) store with plain per-thread stores instead.
   const bool tma_out = (nx == 32);
   // Ghost columns.  By bulk copy (compensated form): the first tile column
-  // also stores its boxes into the right margin (cells 0..31 at
-  // x = Ni..Ni+31) when that start is on a 16-byte boundary for every element
-  // size (Ni a multiple of 8); the last one, when full, into the left margin
-  // (cells Ni-32..Ni-1 at x = -32..-1).  Every value there is a periodic
-  // copy.  Otherwise the
+  // also stores its boxes into the right margin (cells 0..7 at x = Ni..Ni+7:
+  // the store map ends there) when that start is on a 16-byte boundary for
+  // every element size (Ni a multiple of 8); the last one, when full, into
+  // the left margin (cells Ni-32..Ni-1 at x = -32..-1).  Every value there is
+  // a periodic copy.  Otherwise the
   // halo-row warp copies the edge column's stored words from staging to the
   // ghost column, one lane per row.  Threads write only the ghost rows and
   // their corners.  (The flags are recomputed where used: cheaper than

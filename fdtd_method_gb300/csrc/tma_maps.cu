@@ -46,17 +46,22 @@ bool encode(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Columns of the right margin a store map covers: the ghost column and the
+// rest of the 16-byte unit that holds it for 2-byte words.
+constexpr int kRightMargin = 8;
+
 // One 3-D map over the grid rows of a padded array with their x margins
-// (ghost rows excluded): dims {kPadX + Ni + kPadX, Nj, Nk} from padded
+// (ghost rows excluded): dims {kPadX + Ni + kRightMargin, Nj, Nk} from padded
 // column 0, box {32, tile_y, 1}.  x coordinate kPadX + x is cell x; a store
-// at 0 fills the left margin (cells -32 .. -1) and one at kPadX + Ni the
-// right margin's first 32 columns.  Rows outside the grid are not written.
+// at 0 fills the left margin (cells -32 .. -1), one at kPadX + Ni the first
+// kRightMargin columns of the right margin (the copy engine clips the rest).
+// Rows outside the grid are not written.
 bool encode_store(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const PLayout& L,
                   int tile_y) {
   EncodeTiled fn = encode_fn();
   if (!fn) return false;
   void* origin = static_cast<unsigned char*>(base) + L.at(-kPadX, 0, 0) * es;
-  const cuuint64_t dims[3] = {(cuuint64_t)(L.Ni + 2 * kPadX), (cuuint64_t)L.Nj, (cuuint64_t)L.Nk};
+  const cuuint64_t dims[3] = {(cuuint64_t)(L.Ni + kPadX + kRightMargin), (cuuint64_t)L.Nj, (cuuint64_t)L.Nk};
   const cuuint64_t strides[2] = {(cuuint64_t)(L.pitch * es), (cuuint64_t)(L.pplane * es)};
   const cuuint32_t box[3] = {32, (cuuint32_t)tile_y, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
