@@ -73,6 +73,45 @@ def test_slabs_equal_the_whole_grid(prec, n):
     whole.close()
 
 
+@pytest.mark.parametrize("prec", [Precision.FP64, Precision.FP32_COMP])
+def test_one_plane_slabs(prec):
+    # as many slabs as planes: every slab sends and receives its only plane
+    p = normalised_parameters(24, 10, 7)
+    rng = np.random.default_rng(11)
+    f = [rng.standard_normal(p.cells) for _ in range(6)]
+    src = [sources.gaussian_pulse(p, (12, 5, 3), 1.5, 1.0, 15.0, 6.0, 4.0, 30, comp="z")]
+    whole = FDTD(p, COURANT_DT, prec)
+    if prec != Precision.FP64:
+        whole.set_pipeline("split")
+    _load(whole, f, src, prec)
+    whole.step(5)
+    with FDTDSlabs(p, COURANT_DT, p.Nk, prec) as sl:
+        _load(sl, f, src, prec)
+        sl.step(5)
+        for c in range(6):
+            assert np.array_equal(sl.copy_to_host(c), whole.copy_to_host(c)), c
+    whole.close()
+
+
+def test_fp16_slabs_with_per_component_exponents():
+    p, f, srcs = _case(8)
+    exps = [3, 1, -2, 0, 4, 2]
+    whole = FDTD(p, COURANT_DT, Precision.FP16_SCALED)
+    whole.set_pipeline("split")
+    whole.set_fp16_exponents(exps)
+    with FDTDSlabs(p, COURANT_DT, 3, Precision.FP16_SCALED) as sl:
+        sl.set_fp16_exponents(exps)
+        for sim in (whole, sl):
+            for c in range(6):
+                sim.copy_from_host(c, f[c] * 0.25)
+            for q in srcs:
+                sim.add_source(q)
+            sim.step(6)
+        for c in range(6):
+            assert np.array_equal(sl.copy_to_host(c), whole.copy_to_host(c)), c
+    whole.close()
+
+
 @pytest.mark.parametrize("prec", [Precision.FP32, Precision.FP32_COMP])
 def test_slabs_equal_the_fused_pipeline(prec):
     # the whole grid's default (fused) pipeline reproduces the split sweeps
