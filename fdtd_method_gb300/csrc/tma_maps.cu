@@ -31,13 +31,17 @@ EncodeTiled encode_fn() {
   return fn;
 }
 
-// One 3-D map over a padded array: dims {pitch, Nj + 2, Nk}, box
-// {box_w, tile_y + 2, 1}.
+// One 3-D map over a padded array for the tile loads: dims {kPadX + Ni + 1,
+// Nj + 2, Nk} (the left margin, the grid and the right ghost column, the
+// last column a tile reads), box {box_w, tile_y + 2, 1}.  Box columns past
+// the ghost column are outside the map: the copy engine fills them with
+// zeros instead of reading memory (a tile narrower than 32 columns reads only
+// what it uses).
 bool encode(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const PLayout& L, int box_w,
             int tile_y) {
   EncodeTiled fn = encode_fn();
   if (!fn) return false;
-  const cuuint64_t dims[3] = {(cuuint64_t)L.pitch, (cuuint64_t)(L.Nj + 2), (cuuint64_t)L.Nk};
+  const cuuint64_t dims[3] = {(cuuint64_t)(kPadX + L.Ni + 1), (cuuint64_t)(L.Nj + 2), (cuuint64_t)L.Nk};
   const cuuint64_t strides[2] = {(cuuint64_t)(L.pitch * es), (cuuint64_t)(L.pplane * es)};
   const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)(tile_y + 2), 1};
   const cuuint32_t estr[3] = {1, 1, 1};
