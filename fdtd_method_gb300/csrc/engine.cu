@@ -1114,9 +1114,10 @@ int fdtd_slab_plane(fdtd_handle* h, int comp, int plane, int part, void** device
 int fdtd_slab_exchange(fdtd_handle* const* slabs, int n, int halo) {
   if (!slabs || n <= 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "no slabs");
   if (halo != FDTD_HALO_E && halo != FDTD_HALO_B) return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid halo");
+  for (int s = 0; s < n; ++s)
+    if (!slabs[s] || !slabs[s]->zhalo) return fail(FDTD_ERR_INVALID_ARGUMENT, "every handle must be a z slab");
   for (int s = 0; s < n; ++s) {
     const fdtd_handle* h = slabs[s];
-    if (!h || !h->zhalo) return fail(FDTD_ERR_INVALID_ARGUMENT, "every handle must be a z slab");
     const fdtd_handle* h0 = slabs[0];
     if (h->form != h0->form || h->g.Ni != h0->g.Ni || h->g.Nj != h0->g.Nj || h->device != h0->device ||
         h->slab_nk_global != h0->slab_nk_global)
