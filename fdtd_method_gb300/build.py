@@ -72,7 +72,7 @@ def build(force=False, verbose=False, extra_flags=()):
 
 
 CPP = os.path.join(HERE, "cpp")
-PROGRAMS = ("fdtd_sample", "convergence_tests")
+PROGRAMS = ("fdtd_sample", "convergence_tests", "fdtd_coarray_sample")
 
 
 def build_programs():

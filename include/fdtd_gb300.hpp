@@ -18,6 +18,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "fdtd_gb300.h"
@@ -195,6 +196,92 @@ class FDTD_PML : public FDTD {
   FDTD_PML(Parameters parameters, FP dt, FP pml_percent)
       : FDTD(parameters, dt, create_pml(parameters, dt, pml_percent)) {}
   void update_fields() override { check(fdtd_update_fields(handle())); }
+};
+
+// A periodic grid stepped as z slabs on one GPU: the decomposition of the
+// reference's coarray program (coarray/fdtd.F90:149-164: the first Nk mod n
+// slabs get one plane more) with its halo exchange (:86-102) as device
+// copies.  Results equal one FDTD of the whole grid in the same precision,
+// bit for bit.
+class Slabs {
+ public:
+  Slabs(Parameters parameters, FP dt, int n_slabs, Precision precision = Precision::FP64)
+      : parameters_(parameters) {
+    if (n_slabs <= 0 || n_slabs > parameters.Nk) throw std::invalid_argument("need 1 <= slabs <= Nk");
+    fdtd_params p{parameters.Ni, parameters.Nj, parameters.Nk, parameters.ax, parameters.bx, parameters.ay,
+                  parameters.by, parameters.az, parameters.bz, parameters.dx, parameters.dy, parameters.dz};
+    const int base = parameters.Nk / n_slabs, extra = parameters.Nk % n_slabs;
+    int k = 0;
+    for (int s = 0; s < n_slabs; ++s) {
+      const int size = base + (s < extra ? 1 : 0);
+      fdtd_handle* h = nullptr;
+      const int rc = fdtd_slab_create(&p, dt, static_cast<int>(precision), k, k + size, &h);
+      if (rc != FDTD_OK) {
+        release();
+        check(rc);
+      }
+      slabs_.push_back(h);
+      bounds_.push_back({k, k + size});
+      k += size;
+    }
+  }
+  Slabs(const Slabs&) = delete;
+  Slabs& operator=(const Slabs&) = delete;
+  ~Slabs() { release(); }
+
+  int size() const { return static_cast<int>(slabs_.size()); }
+  // Planes [first, second) of slab s.
+  std::pair<int, int> bounds(int s) const { return bounds_.at(s); }
+  fdtd_handle* slab(int s) const { return slabs_.at(s); }
+
+  // A source in whole-grid coordinates; every slab keeps its part.
+  void add_source(const fdtd_source& src) {
+    for (fdtd_handle* h : slabs_) check(fdtd_add_source(h, &src, nullptr));
+  }
+  // n update_fields steps: exchange E, B/2, then per step exchange B, E,
+  // exchange E, B (the trailing and leading B halves of consecutive steps in
+  // one sweep).
+  void step(int64_t n) {
+    if (n <= 0) return;
+    exchange(FDTD_HALO_E);
+    sweep(FDTD_SWEEP_B_HALF);
+    for (int64_t s = 0; s < n; ++s) {
+      exchange(FDTD_HALO_B);
+      sweep(FDTD_SWEEP_E);
+      exchange(FDTD_HALO_E);
+      sweep(s + 1 < n ? FDTD_SWEEP_B_DOUBLE : FDTD_SWEEP_B_HALF);
+    }
+  }
+  void fence() {
+    for (fdtd_handle* h : slabs_) check(fdtd_synchronize(h));
+  }
+  // Whole-grid copies (Ni*Nj*Nk values, flat index i + j*Ni + k*Ni*Nj).
+  void copy_field_to_host(Component c, double* host) const {
+    const std::size_t plane = static_cast<std::size_t>(parameters_.Ni) * parameters_.Nj;
+    for (std::size_t s = 0; s < slabs_.size(); ++s)
+      check(fdtd_copy_field_to_host(slabs_[s], static_cast<int>(c), host + plane * bounds_[s].first,
+                                    plane * (bounds_[s].second - bounds_[s].first)));
+  }
+  void copy_field_from_host(Component c, const double* host) {
+    const std::size_t plane = static_cast<std::size_t>(parameters_.Ni) * parameters_.Nj;
+    for (std::size_t s = 0; s < slabs_.size(); ++s)
+      check(fdtd_copy_field_from_host(slabs_[s], static_cast<int>(c), host + plane * bounds_[s].first,
+                                      plane * (bounds_[s].second - bounds_[s].first)));
+  }
+  const Parameters& parameters() const { return parameters_; }
+
+ private:
+  void exchange(int halo) { check(fdtd_slab_exchange(slabs_.data(), size(), halo)); }
+  void sweep(int kind) {
+    for (fdtd_handle* h : slabs_) check(fdtd_slab_sweep(h, kind));
+  }
+  void release() {
+    for (fdtd_handle* h : slabs_) fdtd_destroy(h);
+    slabs_.clear();
+  }
+  Parameters parameters_;
+  std::vector<fdtd_handle*> slabs_;
+  std::vector<std::pair<int, int>> bounds_;
 };
 
 }  // namespace FDTD_gb300

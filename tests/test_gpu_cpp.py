@@ -69,3 +69,48 @@ def test_cpp_sample_pml_run_uses_the_pml_class():
     s.add_source(src)
     s.step(60)
     assert value == pytest.approx(float(s.field_sums()[:6].sum()), rel=1e-6)
+
+
+def _coarray_job(n, iterations):
+    """The coarray program's grid and box current (coarray/fdtd.F90:36-52 and
+    init_currents, :184-204), as a whole-grid source."""
+    import math
+
+    import numpy as np
+
+    from fdtd_method_gb300 import Const, Parameters, SeparableSource
+    C, PI = Const.C, Const.PI
+    dx, dt, TT = C, 0.2, 8.0
+    Tx = 4 * C
+    current_time = min(int(TT / dt), iterations)
+    bnd = n / 2.0 * dx
+    start = int(math.floor((-Tx / 4.0 + bnd) / dx))
+    stop = int(math.floor((Tx / 4.0 + bnd) / dx))
+    g = np.array([math.pow(math.cos(2.0 * PI * v * dx / Tx), 2.0) for v in range(start, stop + 1)])
+    amp = np.array([math.sin(2.0 * PI * (t + 1) * dt / TT) for t in range(current_time)])
+    p = Parameters(n, n, n, -bnd, bnd, -bnd, bnd, -bnd, bnd, dx, dx, dx)
+    return p, dt, SeparableSource(7, start % n, start % n, start % n, g, g, g, amp)
+
+
+@pytest.mark.parametrize("slabs", [1, 3, 5])
+def test_cpp_coarray_twin_slabs_print_the_whole_grid_slice(slabs):
+    """The coarray program's twin on z slabs prints the slice that one
+    whole-grid handle computes for the same job, digit for digit."""
+    from fdtd_method_gb300 import FDTD
+    n, it = 32, 20
+    r = subprocess.run([os.path.join(BIN, "fdtd_coarray_sample"), str(n), str(it), str(slabs)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    assert lines[0] == "Running on %d images" % slabs
+    assert lines[1].startswith("Total execution time: ") and lines[1].endswith(" seconds")
+    got = [ln.split() for ln in lines[2:] if ln.strip()]
+    p, dt, src = _coarray_job(n, it)
+    sim = FDTD(p, dt)
+    sim.add_source(src)
+    sim.step(it)
+    ex = sim.get_field(0).numpy().reshape(n, n, n)  # (k, j, i)
+    want = [["%.5f" % ex[n // 2, j, i] for i in range(n // 2 - 5, n // 2 + 5)] for j in range(n // 2 - 5, n // 2 + 5)]
+    assert got == want
+    assert any(float(v) != 0.0 for row in got for v in row)
+    sim.close()
