@@ -290,7 +290,7 @@ def ref_lib():
 
 class RefKokkos:
     """FDTD_kokkos::FDTD from the reference's own sources (oracle/_ref).
-    kind="kokkos" (the north-star path) or "openmp" (its OpenMP twin)."""
+    kind="kokkos" (the Kokkos solver class, the path the engine replaces) or "openmp" (its OpenMP twin)."""
 
     def __init__(self, params, dt, kind="kokkos", pml_percent=None):
         lib = ref_lib()
