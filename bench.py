@@ -21,6 +21,9 @@ update_fields (B/2, E, B/2) over the whole grid.
   batched    the batched form on its own workload (256 domains with edges
              uniform in 32..160 cells, plane wave + one pulse each), CUDA-graph
              step groups, one persistent launch per fused sweep.
+  forms      the other storage forms (FP32, FP16 with per-component scale, or
+             the compensated form) on the same workload and timing: value and
+             their fused kernel's roofline.
 
 --impl reference runs only that CPU path on the same workload and prints its
 own line.  Under torchrun every rank runs its own replica (no data exchange;
@@ -69,6 +72,7 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=0, help="timed FP64 steps (default max(20, K/5))")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--no-forms", action="store_true", help="skip the other storage forms' lines")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form leg")
     ap.add_argument("--batch-only", action="store_true", help="run only the batched-form leg and print it")
     ap.add_argument("--batch-domains", type=int, default=256)
@@ -340,6 +344,36 @@ def run_batched(args, stream, world):
                         % (len(wl), args.seed, args.precision)}
 
 
+def time_form(args, p, src, precision, stream, world):
+    """K autotuned steps of one storage form on the workload: Gcell-steps/s
+    and its fused kernel's mean launch time against the HBM roofline."""
+    cells, K, W = p.cells, args.steps, args.warmup
+    sim = make_sim(p, precision)
+    sim.set_stream(stream.cuda_stream)
+    sim.add_source(src)
+    tuned = None if args.no_autotune else sim.autotune(sweeps=10, reuse=False)
+    sim.step(W)
+    sim.synchronize()
+    sim.kernel_times()
+    sim.set_kernel_timing(True)
+    ms = max_over_ranks(world, timed_steps(sim, stream, K, world))
+    kt = sim.kernel_times()
+    sim.set_kernel_timing(False)
+    del sim
+    hbm, note = measured_peaks()
+    fused = kt.get("fused_step")
+    out = {"value": replica_value(world, cells, K, ms), "unit": UNIT, "ms_per_step": ms / K, "autotune": tuned}
+    if fused and fused[1] > 0:
+        launch_ms = fused[0] / fused[1]
+        alg = 12 * BYTES_PER_VALUE[precision] * cells
+        gbs = alg / (launch_ms / 1e3) / 1e9
+        traffic_pc = ncu_traffic("fused_step", precision)
+        out["roofline"] = {"bound": "hbm", "kernel": "fused_step", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                           "frac": gbs / hbm, "peak_note": note, "mean_launch_ms": launch_ms,
+                           "traffic": traffic_pc * cells if traffic_pc else None}
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -401,6 +435,15 @@ def run_ours(args):
                  "achieved": step_alg * cells * K / (ms / 1e3) / 1e9, "frac": step_alg * cells * K / (ms / 1e3) / 1e9 / hbm}
     del sim
     torch.cuda.empty_cache()
+
+    # --- the other FP32-arithmetic forms (same workload and timing) -------
+    forms = None
+    if not args.no_forms:
+        forms = {}
+        for name in ("fp32_comp", "fp32", "fp16_scaled"):
+            if name != args.precision:
+                forms[name] = time_form(args, p, src, name, stream, world)
+                torch.cuda.empty_cache()
 
     # --- batched form ------------------------------------------------------
     batched = None
@@ -500,7 +543,7 @@ def run_ours(args):
                          "roofline": {"bound": "fp64-pipe", "achieved_instr_per_s": v64 * 1e9 * FP64_INSTR_PER_CELL_STEP / world,
                                       "peak_instr_per_s": FP64_PIPE_PEAK,
                                       "frac": v64 * 1e9 * FP64_INSTR_PER_CELL_STEP / world / FP64_PIPE_PEAK}},
-                "accuracy": acc, "batched": batched}
+                "accuracy": acc, "batched": batched, "forms": forms}
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
