@@ -62,7 +62,8 @@ class Source(ctypes.Structure):
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("tile_y", ctypes.c_int), ("kchunk", ctypes.c_int), ("cells_per_thread", ctypes.c_int),
-                ("ms_per_sweep", ctypes.c_double), ("candidates", ctypes.c_int), ("cached", ctypes.c_int)]
+                ("ms_per_sweep", ctypes.c_double), ("candidates", ctypes.c_int), ("cached", ctypes.c_int),
+                ("split_sources", ctypes.c_int)]
 
 
 _H = ctypes.c_void_p
@@ -114,6 +115,7 @@ SIGNATURES = {
     "fdtd_batch_tiles": [_H, ctypes.POINTER(ctypes.c_int64)],
     "fdtd_batch_set_stream": [_H, ctypes.c_void_p],
     "fdtd_batch_synchronize": [_H],
+    "fdtd_batch_set_split_sources": [_H, ctypes.c_int],
     # z slabs
     "fdtd_slab_create": [ctypes.POINTER(Params), ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                          ctypes.POINTER(_H)],

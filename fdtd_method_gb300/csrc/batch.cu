@@ -406,22 +406,26 @@ int fdtd_batch_autotune(fdtd_batch* b, int sweeps, fdtd_tune_result* out) {
       b->cfg.kchunk = kc;
       b->cfg.cells_per_thread = 1;
       if ((rc = build_tables(b)) != FDTD_OK) break;
-      cudaError_t e = launch_fused_all(b, 0, 2, 0);  // warm-up
-      if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
-      for (int q = 0; q < sweeps && e == cudaSuccess; ++q) e = launch_fused_all(b, 0, 2, 0);
-      if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
-      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-      float ms = 0.f;
-      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-      if (e != cudaSuccess) {
-        rc = bcuda(e, "batch autotune sweep");
-        break;
-      }
-      best.candidates += 1;
-      if (ms / sweeps < best.ms_per_sweep) {
-        best.ms_per_sweep = ms / sweeps;
-        best.tile_y = ty;
-        best.kchunk = kc;
+      for (int split = 0; split < 2 && rc == FDTD_OK; ++split) {
+        b->cfg.split_sources = split != 0;
+        cudaError_t e = launch_fused_all(b, 0, 2, 0);  // warm-up
+        if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+        for (int q = 0; q < sweeps && e == cudaSuccess; ++q) e = launch_fused_all(b, 0, 2, 0);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) {
+          rc = bcuda(e, "batch autotune sweep");
+          break;
+        }
+        best.candidates += 1;
+        if (ms / sweeps < best.ms_per_sweep) {
+          best.ms_per_sweep = ms / sweeps;
+          best.tile_y = ty;
+          best.kchunk = kc;
+          best.split_sources = split;
+        }
       }
     }
     if (rc != FDTD_OK) break;
@@ -431,9 +435,17 @@ int fdtd_batch_autotune(fdtd_batch* b, int sweeps, fdtd_tune_result* out) {
   if (rc != FDTD_OK) return rc;
   b->cfg.tile_y = best.tile_y;
   b->cfg.kchunk = best.kchunk;
+  b->cfg.split_sources = best.split_sources != 0;
   b->use_graphs = graphs;
   b->dirty = true;
   if (out) *out = best;
+  return FDTD_OK;
+}
+
+int fdtd_batch_set_split_sources(fdtd_batch* b, int on) {
+  if (int rc = check_batch(b)) return rc;
+  b->cfg.split_sources = on != 0;
+  b->dirty = true;
   return FDTD_OK;
 }
 

@@ -29,6 +29,9 @@ struct FusedConfig {
   int tile_y = 14;
   int kchunk = 48;  // planes per tile (the autotuner picks from 16 to 96)
   int cells_per_thread = 1;  // 1: 32-wide tiles (kernels_fused1.cu); 2: 64-wide, packed float2
+  // Batched sweep only: compile the plane loop with and without source
+  // evaluation and run the source-free copy on tiles no source reaches.
+  bool split_sources = false;
 };
 
 // A box of cells [i0,i1) x [j0,j1) x [k0,k1) (the ranges the reference's

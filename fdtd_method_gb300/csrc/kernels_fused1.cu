@@ -504,8 +504,8 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
 //
 // kSplit: compile the plane loop twice and run the source-free copy on tiles
 // that no source reaches (fewer live registers there).  The batched kernel
-// uses one copy: its tiles alternate between the two cases, and two hot copies
-// of the loop ran about 30 % slower there.
+// takes either: where its tiles alternate between the two cases, two hot
+// copies of the loop ran slower than one (its autotuner picks).
 template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSplit>
 __device__ __forceinline__ void fused1_tile(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                                             const CoefSet& cs, int bx, int by, int bz, int kchunk,
@@ -571,7 +571,7 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
 // bz) from the tile table in order, through an atomic counter, until none
 // are left.  `parity` selects which of each domain's two copies is read.  The
 // last CTA to finish resets the counters for the next launch.
-template <class S, class A, int RY, int kApps>
+template <class S, class A, int RY, int kApps, bool kSplit>
 __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
     fused1_batch(const BatchDomain<S>* __restrict__ doms, const StepMaps* __restrict__ maps,
                  const int4* __restrict__ tiles, int n_tiles, int parity, int kchunk,
@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
       if (Plan1<S, RY>::kLo || (q < 6 || (q >= 12 && q < 18))) prefetch_tensormap(tm);
     }
     __syncthreads();
-    fused1_tile<S, A, RY, kApps, false, false>(dom.L, dom.s[parity], dom.s[parity ^ 1], maps[2 * w.x + parity], dom.cs,
+    fused1_tile<S, A, RY, kApps, false, kSplit>(dom.L, dom.s[parity], dom.s[parity ^ 1], maps[2 * w.x + parity], dom.cs,
                                                w.y, w.z, w.w, kchunk, nullptr, nullptr, nullptr, dom.ss, step, err, smem,
                                                ring);
     __syncthreads();
@@ -665,12 +665,12 @@ cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const
   return launch1_ry<S, 14>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
 }
 
-template <class S, int RY, int APPS>
+template <class S, int RY, int APPS, bool SPLIT>
 static cudaError_t launch1_batch_one(const BatchDomain<S>* doms, const StepMaps* maps, const int4* tiles,
                                      int n_tiles, int parity, int kchunk, const int64_t* step_base, int step_off,
                                      int* counters, int* err, cudaStream_t stream) {
   using A = typename ArithOf1<S>::type;
-  auto kern = fused1_batch<S, A, RY, APPS>;
+  auto kern = fused1_batch<S, A, RY, APPS, SPLIT>;
   const int bytes = Plan1<S, RY>::kTotal;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
@@ -691,16 +691,23 @@ cudaError_t launch_fused1_batch(const void* doms, const StepMaps* maps, const in
                                 int* counters, int* err, cudaStream_t stream) {
   const BatchDomain<S>* d = static_cast<const BatchDomain<S>*>(doms);
   const int kc = cfg.kchunk;
-#define FDTD_B(RY)                                                                                                  \
+#define FDTD_B1(RY, SPLIT)                                                                                          \
   return applications == 2                                                                                       \
-             ? launch1_batch_one<S, RY, 2>(d, maps, tiles, n_tiles, parity, kc, step_base, step_off, counters, err, \
-                                           stream)                                                               \
-             : launch1_batch_one<S, RY, 1>(d, maps, tiles, n_tiles, parity, kc, step_base, step_off, counters, err, \
-                                           stream)
+             ? launch1_batch_one<S, RY, 2, SPLIT>(d, maps, tiles, n_tiles, parity, kc, step_base, step_off, counters, \
+                                                  err, stream)                                                   \
+             : launch1_batch_one<S, RY, 1, SPLIT>(d, maps, tiles, n_tiles, parity, kc, step_base, step_off, counters, \
+                                                  err, stream)
+#define FDTD_B(RY)                  \
+  {                                 \
+    if (cfg.split_sources)          \
+      FDTD_B1(RY, true);            \
+    FDTD_B1(RY, false);             \
+  }
   if (cfg.tile_y == 6) FDTD_B(6);
   if (cfg.tile_y == 30) FDTD_B(30);
   FDTD_B(14);
 #undef FDTD_B
+#undef FDTD_B1
 }
 
 template <class S>

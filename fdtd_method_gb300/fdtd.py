@@ -469,16 +469,22 @@ class FDTDBatch:
     def set_config(self, tile_y=0, kchunk=0, graphs=True):
         _lib.check(self._lib.fdtd_batch_set_config(self._handle(), int(tile_y), int(kchunk), 1 if graphs else 0))
 
+    def set_split_sources(self, on):
+        """Compile the sweep's plane loop twice and run the source-free copy on
+        tiles no source reaches (see fdtd_batch_set_split_sources)."""
+        _lib.check(self._lib.fdtd_batch_set_split_sources(self._handle(), 1 if on else 0))
+
     def step(self, n):
         _lib.check(self._lib.fdtd_batch_step(self._handle(), int(n)))
 
     def autotune(self, sweeps=5):
-        """Times the persistent fused sweep for every candidate tile shape
-        (the state is only read) and keeps the fastest."""
+        """Times the persistent fused sweep for every candidate tile shape,
+        with the plane loop compiled once or split (the state is only read),
+        and keeps the fastest."""
         r = _lib.TuneResult()
         _lib.check(self._lib.fdtd_batch_autotune(self._handle(), int(sweeps), ctypes.byref(r)))
         return {"tile_y": r.tile_y, "kchunk": r.kchunk, "ms_per_sweep": r.ms_per_sweep,
-                "candidates": r.candidates}
+                "candidates": r.candidates, "split_sources": bool(r.split_sources)}
 
     def synchronize(self):
         _lib.check(self._lib.fdtd_batch_synchronize(self._handle()))

@@ -230,6 +230,7 @@ typedef struct fdtd_tune_result {
     double ms_per_sweep;  /* of the chosen shape */
     int candidates;       /* shapes timed */
     int cached;           /* 1 if taken from the cache */
+    int split_sources;    /* batched sweep: 1 if the chosen sweep runs the split plane loop */
 } fdtd_tune_result;
 int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out);
 
@@ -269,9 +270,14 @@ int fdtd_batch_get_step(fdtd_batch* b, int64_t* step);
 int fdtd_batch_tiles(fdtd_batch* b, int64_t* tiles);
 int fdtd_batch_set_stream(fdtd_batch* b, void* stream);
 /* Autotuner of the batch: times `sweeps` (0 = 5) persistent fused sweeps of
- * every domain for tile_y 6, 14 and 30 with kchunk 16, 24, 32, 48 and 64, and
- * keeps the fastest; the state does not change.  Synchronous. */
+ * every domain for tile_y 6, 14 and 30 with kchunk 16, 24, 32, 48 and 64,
+ * each with the plane loop compiled once or split (below), and keeps the
+ * fastest; the state does not change.  Synchronous. */
 int fdtd_batch_autotune(fdtd_batch* b, int sweeps, fdtd_tune_result* out);
+/* Split plane loop (on != 0): the sweep carries a source-free copy of its
+ * plane loop for tiles no source reaches.  Faster where most tiles have no
+ * source; slower where tiles of both kinds alternate.  Same results. */
+int fdtd_batch_set_split_sources(fdtd_batch* b, int on);
 int fdtd_batch_synchronize(fdtd_batch* b);
 
 /* No counterpart in the reference.  The ten field sums of fdtd_field_sums,

@@ -48,9 +48,10 @@ def _single(p, prec, vals, srcs, groups, exps=None):
     return out, sums
 
 
-def _batch(doms, prec, groups, tile_y=0, kchunk=0, graphs=True, exps=None):
+def _batch(doms, prec, groups, tile_y=0, kchunk=0, graphs=True, exps=None, split=False):
     b = FDTDBatch([d[0] for d in doms], COURANT_DT, prec)
     b.set_config(tile_y, kchunk, graphs)
+    b.set_split_sources(split)
     for q, (p, vals, srcs) in enumerate(doms):
         if exps is not None:
             b.set_fp16_exponents(q, exps)
@@ -68,11 +69,14 @@ def _batch(doms, prec, groups, tile_y=0, kchunk=0, graphs=True, exps=None):
     return out, sums
 
 
+@pytest.mark.parametrize("split", [False, True])
 @pytest.mark.parametrize("prec", [Precision.FP32, Precision.FP32_COMP, Precision.FP16_SCALED])
-def test_batch_equals_single_domains(prec):
+def test_batch_equals_single_domains(prec, split):
+    """Every domain equals a single handle, with the sweep's plane loop
+    compiled once or split into source and source-free copies."""
     doms = _domains(SHAPES, 3)
     exps = [4] * 6 if prec == Precision.FP16_SCALED else None
-    got, sums = _batch(doms, prec, [5], exps=exps)
+    got, sums = _batch(doms, prec, [5], exps=exps, split=split)
     for q, (p, vals, srcs) in enumerate(doms):
         want, wsums = _single(p, prec, vals, srcs, [5], exps=exps)
         for c in range(6):
