@@ -116,6 +116,12 @@ SIGNATURES = {
     "fdtd_batch_set_stream": [_H, ctypes.c_void_p],
     "fdtd_batch_synchronize": [_H],
     "fdtd_batch_set_split_sources": [_H, ctypes.c_int],
+    # compact forms
+    "fdtd_energy": [_H, _D],
+    "fdtd_set_sources": [_H, ctypes.POINTER(Source), ctypes.c_int],
+    "fdtd_field_device_ptr": [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)],
+    "fdtd_copy_field": [_H, ctypes.c_int, ctypes.c_void_p, ctypes.c_int],
+    "fdtd_sync": [_H],
     # z slabs
     "fdtd_slab_create": [ctypes.POINTER(Params), ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                          ctypes.POINTER(_H)],

@@ -1027,6 +1027,57 @@ int fdtd_set_fp16_exponents(fdtd_handle* h, const int exponents[6]) {
 
 
 // ---------------------------------------------------------------------------
+// Compact forms of the entry points above.
+
+int fdtd_energy(fdtd_handle* h, double out[3]) {
+  if (!out) return fail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  double sums[FDTD_DIAG_COUNT];
+  if (int rc = fdtd_field_sums(h, sums)) return rc;
+  const double dv8pi = h->p.dx * h->p.dy * h->p.dz / (8.0 * kPi);
+  out[0] = (sums[FDTD_DIAG_EX2] + sums[FDTD_DIAG_EY2] + sums[FDTD_DIAG_EZ2]) * dv8pi;
+  out[1] = (sums[FDTD_DIAG_BX2] + sums[FDTD_DIAG_BY2] + sums[FDTD_DIAG_BZ2]) * dv8pi;
+  out[2] = out[0] + out[1];
+  return FDTD_OK;
+}
+
+int fdtd_set_sources(fdtd_handle* h, const fdtd_source* src, int n) {
+  if (int rc = check_handle(h)) return rc;
+  if (n < 0 || (n > 0 && !src)) return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid source list");
+  const std::vector<HostSource> keep = h->sources;
+  const int calls = h->source_calls;
+  if (int rc = fdtd_clear_sources(h)) return rc;
+  for (int q = 0; q < n; ++q) {
+    if (int rc = fdtd_add_source(h, &src[q], nullptr)) {
+      // leave the previous list in place
+      const std::string msg = fdtd_last_error();
+      DeviceGuard dg(h->device);
+      h->sources = keep;
+      h->source_calls = calls;
+      upload_sources(h);
+      return fail(rc, msg);
+    }
+  }
+  return FDTD_OK;
+}
+
+int fdtd_field_device_ptr(fdtd_handle* h, int comp, void** device_ptr) {
+  if (!device_ptr) return fail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
+  double* p = nullptr;
+  if (int rc = fdtd_get_field(h, comp, &p)) return rc;
+  *device_ptr = p;
+  return FDTD_OK;
+}
+
+int fdtd_copy_field(fdtd_handle* h, int comp, double* host, int dir) {
+  if (int rc = check_handle(h)) return rc;
+  if (dir != FDTD_TO_HOST && dir != FDTD_FROM_HOST) return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid direction");
+  const size_t n = (size_t)h->g.cells;
+  return dir == FDTD_TO_HOST ? fdtd_copy_field_to_host(h, comp, host, n) : fdtd_copy_field_from_host(h, comp, host, n);
+}
+
+int fdtd_sync(fdtd_handle* h) { return fdtd_synchronize(h); }
+
+// ---------------------------------------------------------------------------
 // z slabs: the decomposition of the reference's coarray program
 // (coarray/fdtd.F90:90-98), where image s owns a range of z planes and reads
 // the neighbours' boundary planes of E (for B at k+1, kokkos_functors.h:141)

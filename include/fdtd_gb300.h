@@ -295,6 +295,24 @@ int fdtd_batch_synchronize(fdtd_batch* b);
 int fdtd_field_sums_noalloc(const double* const fields[6], int64_t cells, double* out_device, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Compact forms of the entry points above. */
+/* Field energy in Gaussian units, from fdtd_field_sums: out[0] electric
+ * (sum E^2) dV/(8 pi), out[1] magnetic (sum B^2) dV/(8 pi), out[2] their sum,
+ * dV = dx dy dz.  Synchronous. */
+int fdtd_energy(fdtd_handle* h, double out[3]);
+/* Replaces the handle's source list by src[0..n-1] (fdtd_clear_sources, then
+ * fdtd_add_source for each).  On an error the previous list stays. */
+int fdtd_set_sources(fdtd_handle* h, const fdtd_source* src, int n);
+/* fdtd_get_field as an untyped device pointer (FP64 form). */
+int fdtd_field_device_ptr(fdtd_handle* h, int comp, void** device_ptr);
+/* fdtd_copy_field_to_host (dir FDTD_TO_HOST) or _from_host (FDTD_FROM_HOST)
+ * of all Ni*Nj*Nk values. */
+enum fdtd_direction { FDTD_TO_HOST = 0, FDTD_FROM_HOST = 1 };
+int fdtd_copy_field(fdtd_handle* h, int comp, double* host, int dir);
+/* fdtd_synchronize. */
+int fdtd_sync(fdtd_handle* h);
+
+/* ------------------------------------------------------------------------
  * z slabs: the domain decomposition of the reference's coarray program
  * (coarray/fdtd.F90:90-98, 149-164).  A slab handle owns planes
  * [k_begin, k_end) of the grid `params` plus one halo plane below and one
