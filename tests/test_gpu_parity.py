@@ -17,7 +17,8 @@ from golden_inputs import CASES, case_inputs, case_params
 from oracle import Oracle
 from refcases import CONVERGENCE_CASES, run_convergence
 
-from fdtd_method_gb300 import FDTD, Component, CurrentParameters, InvalidArgument, LogicError, Parameters, build, sources
+from fdtd_method_gb300 import (FDTD, Component, CurrentParameters, InvalidArgument, LogicError, Parameters, Precision,
+                               build, sources)
 from fdtd_method_gb300.sources import COURANT_DT, normalised_parameters
 
 pytestmark = pytest.mark.gpu
@@ -275,3 +276,26 @@ def test_step_counter_drives_source_tables():
     b.step(15)
     for c in range(6):
         np.testing.assert_array_equal(a.get_field(c).numpy(), b.get_field(c).numpy())
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("prec,tol", [(Precision.FP64, 1e-13), (Precision.FP32_COMP, 1e-6),
+                                      (Precision.FP32, 1e-4)])
+def test_engine_follows_the_exact_discrete_plane_wave(axis, prec, tol):
+    """The Yee scheme's exact solution for one periodic mode (discrete
+    dispersion relation and eigenvectors, tests/discrete_wave.py) after 1000
+    steps: FP64 to rounding, the FP32 forms within the bound written here."""
+    import discrete_wave as dw
+    shape = [8, 8, 8]
+    shape[axis] = 64
+    p = normalised_parameters(*shape)
+    e0, b0 = dw.initial(p, axis)
+    ce, cb = dw.PAIRS[axis]
+    s = FDTD(p, COURANT_DT, prec)
+    s.copy_from_host(ce, e0)
+    s.copy_from_host(cb, b0)
+    s.step(1000)
+    e, b = dw.exact(p, axis, COURANT_DT, 1000)
+    assert np.abs(dw.line(s.copy_to_host(ce), p, axis) - e).max() < tol
+    assert np.abs(dw.line(s.copy_to_host(cb), p, axis) - b).max() < tol
+    s.close()

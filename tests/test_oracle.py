@@ -199,3 +199,24 @@ def test_oracle_pml_bitwise_equal_to_reference_build(shape, pct):
     for c in range(6):
         np.testing.assert_array_equal(o.get(c), r.get(c))
     r.close()
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_oracle_follows_the_exact_discrete_plane_wave(axis):
+    """The Yee scheme's exact solution for one periodic mode (its discrete
+    dispersion relation and eigenvectors, tests/discrete_wave.py): the
+    oracle follows it to FP64 rounding over 1000 steps along every axis."""
+    import discrete_wave as dw
+    from fdtd_method_gb300.sources import COURANT_DT, normalised_parameters
+    shape = [4, 4, 4]
+    shape[axis] = 64
+    p = normalised_parameters(*shape)
+    e0, b0 = dw.initial(p, axis)
+    ce, cb = dw.PAIRS[axis]
+    o = Oracle(p, COURANT_DT)
+    o.set(ce, e0)
+    o.set(cb, b0)
+    o.step(1000)
+    e, b = dw.exact(p, axis, COURANT_DT, 1000)
+    assert np.abs(dw.line(o.get(ce), p, axis) - e).max() < 1e-13
+    assert np.abs(dw.line(o.get(cb), p, axis) - b).max() < 1e-13
