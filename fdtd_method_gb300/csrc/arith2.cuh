@@ -106,13 +106,11 @@ template <>
 struct Codec2<StoreF16> {
   using HiT = __half;
   using Raw = __half2;
-  __device__ __forceinline__ static P2 decode(const StoreF16& s, int c, __half2 h, uint32_t) {
-    const float2 f = __half22float2(h);
-    return P2{mul2(f, make_float2(s.inv_scale[c], s.inv_scale[c])), make_float2(0.f, 0.f)};
+  // stored values, as StoreF16 (the scales travel in the coefficients)
+  __device__ __forceinline__ static P2 decode(const StoreF16&, int, __half2 h, uint32_t) {
+    return P2{__half22float2(h), make_float2(0.f, 0.f)};
   }
-  __device__ __forceinline__ static __half2 encode(const StoreF16& s, int c, P2 p) {
-    return __float22half2_rn(mul2(p.hi, make_float2(s.scale[c], s.scale[c])));
-  }
+  __device__ __forceinline__ static __half2 encode(const StoreF16&, int, P2 p) { return __float22half2_rn(p.hi); }
   __device__ __forceinline__ static P2 quantize(const StoreF16& s, int c, P2 p) {
     return decode(s, c, encode(s, c, p), 0);
   }

@@ -57,6 +57,7 @@ Coef split_coef(double c) {
 namespace fdtd {
 // Lets other translation units of the library report through fdtd_last_error().
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
 }  // namespace fdtd
 
 namespace {
@@ -1004,7 +1005,8 @@ int fdtd_set_fp16_exponents(fdtd_handle* h, const int exponents[6]) {
   if (!exponents) return fail(FDTD_ERR_INVALID_ARGUMENT, "null exponents");
   if (h->form != Form::F16) return fail(FDTD_ERR_UNSUPPORTED, "exponents apply to the FP16_SCALED form only");
   for (int c = 0; c < 6; ++c)
-    if (exponents[c] < -100 || exponents[c] > 100) return fail(FDTD_ERR_INVALID_ARGUMENT, "exponent out of range");
+    // |e| <= 60 keeps every coefficient times 2^(e_dst - e_src) a finite float
+    if (exponents[c] < -60 || exponents[c] > 60) return fail(FDTD_ERR_INVALID_ARGUMENT, "exponent out of range [-60, 60]");
   // Rescale stored values so the fields they represent are unchanged.
   DeviceGuard dg(h->device);
   if (int rc = ensure_staging(h)) return rc;

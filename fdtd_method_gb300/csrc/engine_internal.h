@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "common.cuh"
 #include "layout.cuh"
@@ -22,6 +23,40 @@ struct CoefSet {
   Coef cj;      // -4 pi dt
   double cj64;  // -4 pi dt in FP64 (current term of the compensated form)
 };
+
+// The axis and the source component of term t of component c's update
+// (kokkos_functors.h:64-90 for E, :128-151 for B):
+//   Ex: cy (Bz - Bz[j-1]) - cz (By - By[k-1])     Bx: cz (Ey[k+1] - Ey) - cy (Ez[j+1] - Ez)
+//   Ey: cz (Bx - Bx[k-1]) - cx (Bz - Bz[i-1])     By: cx (Ez[i+1] - Ez) - cz (Ex[k+1] - Ex)
+//   Ez: cx (By - By[i-1]) - cy (Bx - Bx[j-1])     Bz: cy (Ex[j+1] - Ex) - cx (Ey[i+1] - Ey)
+__host__ __device__ constexpr int term_axis(int c, int t) {
+  return c == 0 ? (t == 0 ? 1 : 2) : c == 1 ? (t == 0 ? 2 : 0) : (t == 0 ? 0 : 1);
+}
+__host__ __device__ constexpr int e_term_src(int c, int t) {  // a B component
+  return c == 0 ? (t == 0 ? 5 : 4) : c == 1 ? (t == 0 ? 3 : 5) : (t == 0 ? 4 : 3);
+}
+__host__ __device__ constexpr int b_term_src(int c, int t) { return term_axis(c, t); }  // an E component
+
+// The coefficient a kernel of storage form S multiplies term t of component
+// c's update by: the per-axis set of CoefSet, except in the FP16 form, whose
+// kernels compute on stored (scaled) values with the per-term coefficients
+// its store carries (StoreF16::te, tb, tj).
+template <class S>
+__device__ __forceinline__ Coef ecoef(const CoefSet& cs, const S& st, int c, int t) {
+  if constexpr (std::is_same<S, StoreF16>::value) return Coef{st.te[2 * c + t], 0.f};
+  else return cs.ce[term_axis(c, t)];
+}
+template <class S>
+__device__ __forceinline__ Coef bcoef(const CoefSet& cs, const S& st, int c, int t) {
+  if constexpr (std::is_same<S, StoreF16>::value) return Coef{st.tb[2 * c + t], 0.f};
+  else return cs.cb[term_axis(c, t)];
+}
+template <class S>
+__device__ __forceinline__ Coef jcoef(const CoefSet& cs, const S& st, int c) {
+  if constexpr (std::is_same<S, StoreF16>::value) return Coef{st.tj[c], 0.f};
+  else return cs.cj;
+}
+
 
 // Launch shape of the fused step kernel: interior tile rows (14 or 6) and
 // planes per tile.

@@ -151,6 +151,16 @@ struct fdtd_handle {
       v.s16.scale[c] = std::ldexp(1.0f, fp16_exp[c]);
       v.s16.inv_scale[c] = std::ldexp(1.0f, -fp16_exp[c]);
     }
+    // FP16 kernels compute on stored values: each coefficient carries the
+    // power of two between its term's source and destination scales.
+    const int* e = fp16_exp;
+    for (int c = 0; c < 3; ++c) {
+      for (int t = 0; t < 2; ++t) {
+        v.s16.te[2 * c + t] = std::ldexp(cs.ce[term_axis(c, t)].hi, e[c] - e[e_term_src(c, t)]);
+        v.s16.tb[2 * c + t] = std::ldexp(cs.cb[term_axis(c, t)].hi, e[3 + c] - e[b_term_src(c, t)]);
+      }
+      v.s16.tj[c] = std::ldexp(cs.cj.hi, e[c]);
+    }
     return v;
   }
   StateView view() const { return make_view(field, lo); }

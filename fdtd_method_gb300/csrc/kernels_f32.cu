@@ -20,7 +20,6 @@ __device__ __forceinline__ void b_column(const PLayout& L, const S& st, const Co
                                          int kchunk, int kend) {
   if (i >= L.Ni || j >= L.Nj || k0 >= kend) return;
   const int k1 = min(k0 + kchunk, kend);
-  const Coef cx = cs.cb[0], cy = cs.cb[1], cz = cs.cb[2];
   const int64_t col = L.at(i, j, 0), col_in = L.at(i + 1, j, 0), col_jn = L.at(i, j + 1, 0);
 
   Pair ex = st.load(0, col + (int64_t)k0 * L.pplane);
@@ -31,9 +30,9 @@ __device__ __forceinline__ void b_column(const PLayout& L, const S& st, const Co
     const Pair ex_kn = st.load(0, col + nbase);
     const Pair ey_kn = st.load(1, col + nbase);
     const Pair ez = st.load(2, col + base);
-    Pair tx = A::curl(cz, ey_kn, ey, cy, st.load(2, col_jn + base), ez);
-    Pair ty = A::curl(cx, st.load(2, col_in + base), ez, cz, ex_kn, ex);
-    Pair tz = A::curl(cy, st.load(0, col_jn + base), ex, cx, st.load(1, col_in + base), ey);
+    Pair tx = A::curl(bcoef<S>(cs, st, 0, 0), ey_kn, ey, bcoef<S>(cs, st, 0, 1), st.load(2, col_jn + base), ez);
+    Pair ty = A::curl(bcoef<S>(cs, st, 1, 0), st.load(2, col_in + base), ez, bcoef<S>(cs, st, 1, 1), ex_kn, ex);
+    Pair tz = A::curl(bcoef<S>(cs, st, 2, 0), st.load(0, col_jn + base), ex, bcoef<S>(cs, st, 2, 1), st.load(1, col_in + base), ey);
     if (kApplications == 2) {
       tx = A::twice(tx);
       ty = A::twice(ty);
@@ -84,7 +83,6 @@ __global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __r
   const int k0 = kbeg + blockIdx.z * kchunk;
   if (i >= L.Ni || j >= L.Nj || k0 >= kend) return;
   const int k1 = min(k0 + kchunk, kend);
-  const Coef cx = cs.ce[0], cy = cs.ce[1], cz = cs.ce[2];
   const int64_t col = L.at(i, j, 0), col_ip = L.at(i - 1, j, 0), col_jp = L.at(i, j - 1, 0);
   const int64_t dcol = i + (int64_t)j * L.Ni;  // dense current index
   const int64_t dplane = (int64_t)L.Ni * L.Nj;
@@ -97,9 +95,9 @@ __global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __r
     const Pair bx = st.load(3, col + base);
     const Pair by = st.load(4, col + base);
     const Pair bz = st.load(5, col + base);
-    Pair tx = A::curl(cy, bz, st.load(5, col_jp + base), cz, by, by_kp);
-    Pair ty = A::curl(cz, bx, bx_kp, cx, bz, st.load(5, col_ip + base));
-    Pair tz = A::curl(cx, by, st.load(4, col_ip + base), cy, bx, st.load(3, col_jp + base));
+    Pair tx = A::curl(ecoef<S>(cs, st, 0, 0), bz, st.load(5, col_jp + base), ecoef<S>(cs, st, 0, 1), by, by_kp);
+    Pair ty = A::curl(ecoef<S>(cs, st, 1, 0), bx, bx_kp, ecoef<S>(cs, st, 1, 1), bz, st.load(5, col_ip + base));
+    Pair tz = A::curl(ecoef<S>(cs, st, 2, 0), by, st.load(4, col_ip + base), ecoef<S>(cs, st, 2, 1), bx, st.load(3, col_jp + base));
     T jv[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
     unsigned has = 0;  // J components that carry current here
     if (kDenseJ) {
@@ -110,9 +108,9 @@ __global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __r
       has = 7u;
     }
     if (kSources) has |= source_sum<A>(ss, step, i, j, k, L, jv);
-    if (has & 1u) tx = A::add(tx, A::cur_term(cs.cj, jv[0]));
-    if (has & 2u) ty = A::add(ty, A::cur_term(cs.cj, jv[1]));
-    if (has & 4u) tz = A::add(tz, A::cur_term(cs.cj, jv[2]));
+    if (has & 1u) tx = A::add(tx, A::cur_term(jcoef<S>(cs, st, 0), jv[0]));
+    if (has & 2u) ty = A::add(ty, A::cur_term(jcoef<S>(cs, st, 1), jv[1]));
+    if (has & 4u) tz = A::add(tz, A::cur_term(jcoef<S>(cs, st, 2), jv[2]));
     store_with_ghosts(st, L, 0, i, j, k, A::acc(st.load(0, col + base), tx));
     store_with_ghosts(st, L, 1, i, j, k, A::acc(st.load(1, col + base), ty));
     store_with_ghosts(st, L, 2, i, j, k, A::acc(st.load(2, col + base), tz));

@@ -160,8 +160,6 @@ __global__ void __launch_bounds__(32 * (RY + 2))
     if (e1) src1.init(ss, xl1, yl, step, L);
   }
 
-  const Coef2 ce0 = bcast(cs.ce[0]), ce1 = bcast(cs.ce[1]), ce2 = bcast(cs.ce[2]);
-  const Coef2 cb0 = bcast(cs.cb[0]), cb1 = bcast(cs.cb[1]), cb2 = bcast(cs.cb[2]);
   const P2 zero{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
   P2 pbx = zero, pby = zero, pbz = zero, pex = zero, pey = zero, pez = zero;
   {
@@ -221,9 +219,9 @@ __global__ void __launch_bounds__(32 * (RY + 2))
       const P2 bz_jp = ld2(5, r - 1, c0), bx_jp = ld2(3, r - 1, c0);
       const P2 bz_ip = make_p2(ld1(5, r, c0 - 1), lane0(bz));
       const P2 by_ip = make_p2(ld1(4, r, c0 - 1), lane0(by));
-      P2 qx = A2::curl(ce1, bz, bz_jp, ce2, by, pby);
-      P2 qy = A2::curl(ce2, bx, pbx, ce0, bz, bz_ip);
-      P2 qz = A2::curl(ce0, by, by_ip, ce1, bx, bx_jp);
+      P2 qx = A2::curl(bcast(ecoef<S>(cs, st, 0, 0)), bz, bz_jp, bcast(ecoef<S>(cs, st, 0, 1)), by, pby);
+      P2 qy = A2::curl(bcast(ecoef<S>(cs, st, 1, 0)), bx, pbx, bcast(ecoef<S>(cs, st, 1, 1)), bz, bz_ip);
+      P2 qz = A2::curl(bcast(ecoef<S>(cs, st, 2, 0)), by, by_ip, bcast(ecoef<S>(cs, st, 2, 1)), bx, bx_jp);
       if (kDenseJ || kSrc != 0) {
         T j0[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
         T j1[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
@@ -256,7 +254,7 @@ __global__ void __launch_bounds__(32 * (RY + 2))
           P2* q[3] = {&qx, &qy, &qz};
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            const Pair t0 = A::cur_term(cs.cj, j0[c]), t1 = A::cur_term(cs.cj, j1[c]);
+            const Pair t0 = A::cur_term(jcoef<S>(cs, st, c), j0[c]), t1 = A::cur_term(jcoef<S>(cs, st, c), j1[c]);
             const P2 s = A2::add(*q[c], make_p2(t0, t1));
             if (h0 >> c & 1u) {
               q[c]->hi.x = s.hi.x;
@@ -279,9 +277,9 @@ __global__ void __launch_bounds__(32 * (RY + 2))
         const P2 ez_jn = se_get2(prv, 2, r + 1, c0), ex_jn = se_get2(prv, 0, r + 1, c0);
         const P2 ez_in = make_p2(lane1(pez), se_get1(prv, 2, r, c0 + 2));
         const P2 ey_in = make_p2(lane1(pey), se_get1(prv, 1, r, c0 + 2));
-        P2 ux = A2::curl(cb2, ney, pey, cb1, ez_jn, pez);
-        P2 uy = A2::curl(cb0, ez_in, pez, cb2, nex, pex);
-        P2 uz = A2::curl(cb1, ex_jn, pex, cb0, ey_in, pey);
+        P2 ux = A2::curl(bcast(bcoef<S>(cs, st, 0, 0)), ney, pey, bcast(bcoef<S>(cs, st, 0, 1)), ez_jn, pez);
+        P2 uy = A2::curl(bcast(bcoef<S>(cs, st, 1, 0)), ez_in, pez, bcast(bcoef<S>(cs, st, 1, 1)), nex, pex);
+        P2 uz = A2::curl(bcast(bcoef<S>(cs, st, 2, 0)), ex_jn, pex, bcast(bcoef<S>(cs, st, 2, 1)), ey_in, pey);
         if (kApps == 2) {
           ux = A2::twice(ux);
           uy = A2::twice(uy);

@@ -315,9 +315,9 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
 
     // 1. E'(t)
     const Pair bx = V(Comp<3>{}, 0, 0), by = V(Comp<4>{}, 0, 0), bz = V(Comp<5>{}, 0, 0);
-    Pair qx = A::curl(cs.ce[1], bz, V(Comp<5>{}, -1, 0), cs.ce[2], by, pby);
-    Pair qy = A::curl(cs.ce[2], bx, pbx, cs.ce[0], bz, V(Comp<5>{}, 0, -1));
-    Pair qz = A::curl(cs.ce[0], by, V(Comp<4>{}, 0, -1), cs.ce[1], bx, V(Comp<3>{}, -1, 0));
+    Pair qx = A::curl(ecoef<S>(cs, st, 0, 0), bz, V(Comp<5>{}, -1, 0), ecoef<S>(cs, st, 0, 1), by, pby);
+    Pair qy = A::curl(ecoef<S>(cs, st, 1, 0), bx, pbx, ecoef<S>(cs, st, 1, 1), bz, V(Comp<5>{}, 0, -1));
+    Pair qz = A::curl(ecoef<S>(cs, st, 2, 0), by, V(Comp<4>{}, 0, -1), ecoef<S>(cs, st, 2, 1), bx, V(Comp<3>{}, -1, 0));
     if (kDenseJ || kSrc) {
       // Current, accumulated per J component in registration order; only the
       // components that received current get the current term.
@@ -356,9 +356,9 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
           has |= (unsigned)d.comp_mask;
         }
       }
-      if (has & 1u) qx = A::add(qx, A::cur_term(cs.cj, jv[0]));
-      if (has & 2u) qy = A::add(qy, A::cur_term(cs.cj, jv[1]));
-      if (has & 4u) qz = A::add(qz, A::cur_term(cs.cj, jv[2]));
+      if (has & 1u) qx = A::add(qx, A::cur_term(jcoef<S>(cs, st, 0), jv[0]));
+      if (has & 2u) qy = A::add(qy, A::cur_term(jcoef<S>(cs, st, 1), jv[1]));
+      if (has & 4u) qz = A::add(qz, A::cur_term(jcoef<S>(cs, st, 2), jv[2]));
     }
     const Pair ax = A::acc(V(Comp<0>{}, 0, 0), qx), ay = A::acc(V(Comp<1>{}, 0, 0), qy), az = A::acc(V(Comp<2>{}, 0, 0), qz);
     // E' in its stored words; the B update uses the value they hold.
@@ -390,9 +390,9 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
       auto E = [&](int c, int off) -> Pair {
         return st.decode(c, ph[c * P::kXComp + off], P::kLo ? pq[c * P::kXComp + off] : LoT(0));
       };
-      Pair ux = A::curl(cs.cb[2], ney, pey, cs.cb[1], E(2, xo_up), pez);
-      Pair uy = A::curl(cs.cb[0], E(2, xo_right), pez, cs.cb[2], nex, pex);
-      Pair uz = A::curl(cs.cb[1], E(0, xo_up), pex, cs.cb[0], E(1, xo_right), pey);
+      Pair ux = A::curl(bcoef<S>(cs, st, 0, 0), ney, pey, bcoef<S>(cs, st, 0, 1), E(2, xo_up), pez);
+      Pair uy = A::curl(bcoef<S>(cs, st, 1, 0), E(2, xo_right), pez, bcoef<S>(cs, st, 1, 1), nex, pex);
+      Pair uz = A::curl(bcoef<S>(cs, st, 2, 0), E(0, xo_up), pex, bcoef<S>(cs, st, 2, 1), E(1, xo_right), pey);
       if (kApps == 2) {
         ux = A::twice(ux);
         uy = A::twice(uy);

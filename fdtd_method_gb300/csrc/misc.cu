@@ -51,7 +51,7 @@ template <class S>
 __global__ void import_kernel(PLayout L, S st, int c, const double* __restrict__ src, int64_t off, int64_t n) {
   for_cells_by_row(L, off, n, [&](int x, int y, int z, int64_t t) {
     const Pair p = S::kComp ? split_f64(src[t]) : Pair{__double2float_rn(src[t]), 0.f};
-    store_with_ghosts(st, L, c, x, y, z, p);
+    store_with_ghosts(st, L, c, x, y, z, st.to_stored(c, p));
   });
 }
 

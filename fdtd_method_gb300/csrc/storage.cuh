@@ -36,6 +36,7 @@ struct StoreF32 {
   // Stores already encoded words (enc_hi / enc_lo).
   __device__ __forceinline__ void store_words(int c, int64_t idx, float h, uint16_t) const { v[c][idx] = h; }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const { return (double)v[c][idx]; }
+  __device__ __forceinline__ Pair to_stored(int, Pair p) const { return p; }
   // The value a store followed by a load returns.
   __device__ __forceinline__ Pair quantize(int, Pair p) const { return Pair{p.hi, 0.f}; }
   // The stored words of a value (quantize(c, p) == decode(c, enc_hi(c, p), enc_lo(p))).
@@ -44,27 +45,31 @@ struct StoreF32 {
 };
 
 // FP16 storage with a power-of-two scale per component: stored = field * 2^e.
+// The kernels compute on stored values (the scale travels in the per-term
+// coefficients, CoefSet::te/tb/tj), so decode and encode are conversions
+// only; load_f64 and to_stored convert from and to field values.
 struct StoreF16 {
   static constexpr bool kComp = false;
   using HiT = __half;
   __half* v[6];
   float scale[6];      // 2^e
   float inv_scale[6];  // 2^-e
-  __device__ __forceinline__ Pair decode(int c, __half h, uint16_t) const {
-    return Pair{__fmul_rn(__half2float(h), inv_scale[c]), 0.f};
-  }
+  // The update coefficients in stored units: te[2c+t] multiplies the t-th curl
+  // difference of E component c, tb[2c+t] that of B component c, tj[c] the
+  // current of E component c; each is the FP64 form's coefficient times the
+  // exact power of two 2^(e_dst - e_src) between the two components' scales.
+  float te[6], tb[6], tj[3];
+  __device__ __forceinline__ Pair decode(int, __half h, uint16_t) const { return Pair{__half2float(h), 0.f}; }
   __device__ __forceinline__ Pair load(int c, int64_t idx) const { return decode(c, v[c][idx], 0); }
-  __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const {
-    v[c][idx] = __float2half_rn(__fmul_rn(p.hi, scale[c]));
-  }
+  __device__ __forceinline__ void store(int c, int64_t idx, Pair p) const { v[c][idx] = __float2half_rn(p.hi); }
+  // A field value in the units the kernels compute in.
+  __device__ __forceinline__ Pair to_stored(int c, Pair p) const { return Pair{__fmul_rn(p.hi, scale[c]), 0.f}; }
   __device__ __forceinline__ void store_words(int c, int64_t idx, __half h, uint16_t) const { v[c][idx] = h; }
   __device__ __forceinline__ double load_f64(int c, int64_t idx) const {
     return (double)__half2float(v[c][idx]) * (double)inv_scale[c];
   }
-  __device__ __forceinline__ Pair quantize(int c, Pair p) const {
-    return Pair{__fmul_rn(__half2float(__float2half_rn(__fmul_rn(p.hi, scale[c]))), inv_scale[c]), 0.f};
-  }
-  __device__ __forceinline__ __half enc_hi(int c, Pair p) const { return __float2half_rn(__fmul_rn(p.hi, scale[c])); }
+  __device__ __forceinline__ Pair quantize(int, Pair p) const { return Pair{__half2float(__float2half_rn(p.hi)), 0.f}; }
+  __device__ __forceinline__ __half enc_hi(int, Pair p) const { return __float2half_rn(p.hi); }
   __device__ __forceinline__ uint16_t enc_lo(Pair) const { return 0; }
 };
 
@@ -104,6 +109,7 @@ struct StoreF32C {
     const Pair p = load(c, idx);
     return (double)p.hi + (double)p.lo;
   }
+  __device__ __forceinline__ Pair to_stored(int, Pair p) const { return p; }
 };
 
 }  // namespace fdtd

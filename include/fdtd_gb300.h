@@ -187,7 +187,7 @@ int fdtd_set_stream(fdtd_handle* h, void* stream);
 int fdtd_synchronize(fdtd_handle* h);
 
 /* Per-component power-of-two scales of the FP16_SCALED form: stored value =
- * field * 2^exponent.  `exponents` has 6 entries (Ex..Bz). */
+ * field * 2^exponent.  `exponents` has 6 entries (Ex..Bz), each in [-60, 60]. */
 int fdtd_set_fp16_exponents(fdtd_handle* h, const int exponents[6]);
 
 /* Kernel timing (new; for roofline accounting).  While enabled, every kernel
