@@ -112,3 +112,28 @@ def test_slice_csv_matches_the_plotting_script_format(tmp_path):
     assert lines[0].split(";") == ["0", "1", "2", "3", "4"]
     table = np.array([[float(x.replace(",", ".")) for x in ln.split(";")] for ln in lines[1:]])
     np.testing.assert_array_equal(table, values.reshape(3, 4, 5)[1])
+
+
+def test_slab_and_compact_arguments_checked_before_gpu_work(lib):
+    p = Parameters(8, 8, 12, 0, 1, 0, 1, 0, 1, 0.25, 0.25, 0.25).to_c()
+    h = ctypes.c_void_p()
+    # plane range outside the grid, or empty
+    for k0, k1 in ((0, 13), (5, 5), (-1, 4)):
+        assert lib.fdtd_slab_create(ctypes.byref(p), 1e-12, 0, k0, k1, ctypes.byref(h)) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert b"k_begin" in lib.fdtd_last_error()
+    bad = _lib.Params(0, 8, 8, 0, 1, 0, 1, 0, 1, 0.25, 0.25, 0.25)
+    assert lib.fdtd_slab_create(ctypes.byref(bad), 1e-12, 0, 0, 4, ctypes.byref(h)) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_last_error() == b"ERROR: invalid parameters"
+    # exchange: no slabs, a null slab, a bad halo kind
+    assert lib.fdtd_slab_exchange(None, 0, 0) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    arr = (ctypes.c_void_p * 1)(None)
+    assert lib.fdtd_slab_exchange(arr, 1, 0) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_slab_exchange(arr, 1, 5) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    # compact forms and the batch loop switch on null handles
+    out = (ctypes.c_double * 3)()
+    assert lib.fdtd_energy(None, out) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_set_sources(None, None, 0) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_copy_field(None, 0, None, 0) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_sync(None) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_slab_sweep(None, 0) == _lib.FDTD_ERR_INVALID_ARGUMENT
+    assert lib.fdtd_batch_set_split_sources(None, 1) == _lib.FDTD_ERR_INVALID_ARGUMENT
