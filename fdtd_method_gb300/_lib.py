@@ -93,6 +93,8 @@ SIGNATURES = {
     "fdtd_set_stream": [_H, ctypes.c_void_p],
     "fdtd_synchronize": [_H],
     "fdtd_set_fp16_exponents": [_H, ctypes.POINTER(ctypes.c_int)],
+    "fdtd_set_fp64_arith": [_H, ctypes.c_int],
+    "fdtd_measure_fp64_rate": [_D, _D],
     "fdtd_set_kernel_timing": [_H, ctypes.c_int],
     "fdtd_kernel_times": [_H, _D, ctypes.POINTER(ctypes.c_int64)],
     "fdtd_set_pipeline": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],

@@ -194,7 +194,7 @@ int run_b(fdtd_handle* h, int apps) {
   if (h->form == Form::F64) {
     Fp64Fields F;
     for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c] - h->halo_elems();
-    e = launch_b_fp64(v.g, box, F, &h->coef[3], apps, h->stream);
+    e = launch_b_fp64(v.g, box, F, &h->coef[3], apps, h->fp64_fma, h->stream);
   } else {
     switch (h->form) {
       case Form::F32: e = launch_b_f32(v.L, v.s32, h->cs, apps, box.k0, box.k1, h->stream); break;
@@ -218,7 +218,7 @@ int run_e(fdtd_handle* h, int64_t step) {
   if (h->form == Form::F64) {
     Fp64Fields F;
     for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c] - h->halo_elems();
-    e = launch_e_fp64(v.g, box, F, &h->coef[0], h->coef[6], h->dense_j, ss, step, h->stream);
+    e = launch_e_fp64(v.g, box, F, &h->coef[0], h->coef[6], h->dense_j, ss, step, h->fp64_fma, h->stream);
   } else {
     // dense FP32 currents: the dense layout, with the same halo planes
     const int64_t dj0 = h->zhalo * h->g.plane;
@@ -997,6 +997,15 @@ int fdtd_synchronize(fdtd_handle* h) {
     cudaMemset(h->d_err, 0, sizeof(int));
     return fail(FDTD_ERR_TIMEOUT, "a bounded wait in a step kernel gave up; results of that step are invalid");
   }
+  return FDTD_OK;
+}
+
+int fdtd_set_fp64_arith(fdtd_handle* h, int arith) {
+  if (int rc = check_handle(h)) return rc;
+  if (arith != FDTD_FP64_BITWISE && arith != FDTD_FP64_CONTRACTED)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid FP64 arithmetic mode");
+  if (h->form != Form::F64) return fail(FDTD_ERR_UNSUPPORTED, "the arithmetic mode applies to the FP64 form only");
+  h->fp64_fma = arith == FDTD_FP64_CONTRACTED;
   return FDTD_OK;
 }
 

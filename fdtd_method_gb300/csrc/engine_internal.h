@@ -77,11 +77,12 @@ struct Box {
   static Box whole(const Grid& g) { return Box{0, g.Ni, 0, g.Nj, 0, g.Nk}; }
 };
 
-// kernels_fp64.cu: the FP64 sweeps over a box.
+// kernels_fp64.cu: the FP64 sweeps over a box; fma selects the contracted
+// arithmetic (otherwise the reference's, bit for bit).
 cudaError_t launch_b_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const double cb[3],
-                          int applications, cudaStream_t st);
+                          int applications, bool fma, cudaStream_t st);
 cudaError_t launch_e_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const double ce[3], double cJ,
-                          bool dense_j, const SourceSet& ss, int64_t step, cudaStream_t st);
+                          bool dense_j, const SourceSet& ss, int64_t step, bool fma, cudaStream_t st);
 
 // kernels_pml.cu: the split-field layer updates (FP64) over a box.  split =
 // Exy, Exz, Eyx, Eyz, Ezx, Ezy, Bxy, Bxz, Byx, Byz, Bzx, Bzy; decay[a][n] =

@@ -61,6 +61,7 @@ struct fdtd_handle {
   LoT* alt_lo[6] = {nullptr};
   float* jf[3] = {nullptr};
   bool dense_j = false;  // the E update reads the dense J arrays
+  bool fp64_fma = false;  // FP64 form: contracted arithmetic (fdtd_set_fp64_arith)
   int fp16_exp[6] = {0, 0, 0, 0, 0, 0};
 
   // Sources.

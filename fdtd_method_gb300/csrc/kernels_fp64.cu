@@ -13,6 +13,14 @@
 // FP64 pipe: one thread per (i, j) column marching along z with the z
 // neighbour carried in registers, all index arithmetic in 32-bit integers
 // plus one 64-bit plane offset per z step.
+//
+// Contracted variant (kFma, fdtd_set_fp64_arith): the same sweeps with each
+// curl term accumulated by DFMA into the field, B += (apps cB) d1 - (apps cB) d2
+// as two DFMAs after the two differences (apps cB is exact: apps is 1 or 2),
+// E likewise, with cJ J as one more DFMA.  A B double half step then costs 12
+// FP64 instructions per cell and E 12 (15 with current), against 21 and 18:
+// the results are no longer the reference's bit for bit but stay within a
+// few ulps per step (the drop-in contract is 1e-12 of the field amplitude).
 #include "engine_internal.h"
 
 namespace fdtd {
@@ -25,7 +33,7 @@ namespace fdtd {
 // followed by the first half step of the next, which see the same E and
 // therefore the same t — the two additions stay separate, so the result is
 // the reference's bit for bit).  kernels: kokkos_functors.h:128-151.
-template <int kApplications>
+template <int kApplications, bool kFma>
 __global__ void __launch_bounds__(256) b_update_fp64(Grid g, Box b, const double* __restrict__ Ex,
                                                      const double* __restrict__ Ey,
                                                      const double* __restrict__ Ez,
@@ -54,6 +62,17 @@ __global__ void __launch_bounds__(256) b_update_fp64(Grid g, Box b, const double
     const double ey_in = Ey[col_in + base];
     const double ex_jn = Ex[col_jn + base];
 
+    if (kFma) {
+      // c' = apps * c (exact); B + c' d1 - c' d2 as two DFMAs
+      const double ax = kApplications * cx, ay = kApplications * cy, az = kApplications * cz;
+      Bx[col + base] = __fma_rn(az, DSUB(ey_kn, ey), __fma_rn(-ay, DSUB(ez_jn, ez), Bx[col + base]));
+      By[col + base] = __fma_rn(ax, DSUB(ez_in, ez), __fma_rn(-az, DSUB(ex_kn, ex), By[col + base]));
+      Bz[col + base] = __fma_rn(ay, DSUB(ex_jn, ex), __fma_rn(-ax, DSUB(ey_in, ey), Bz[col + base]));
+      ex = ex_kn;
+      ey = ey_kn;
+      base = nbase;
+      continue;
+    }
     const double tx = DSUB(DMUL(cz, DSUB(ey_kn, ey)), DMUL(cy, DSUB(ez_jn, ez)));
     const double ty = DSUB(DMUL(cx, DSUB(ez_in, ez)), DMUL(cz, DSUB(ex_kn, ex)));
     const double tz = DSUB(DMUL(cy, DSUB(ex_jn, ex)), DMUL(cx, DSUB(ey_in, ey)));
@@ -79,7 +98,7 @@ __global__ void __launch_bounds__(256) b_update_fp64(Grid g, Box b, const double
 // E += cJ*J + c*curl(B), kokkos_functors.h:64-90.  Cells with no current skip
 // the cJ*J term: cJ < 0, so cJ*0 = -0 and x + (-0) = x for every x, which
 // leaves the result bit-identical.
-template <bool kDenseJ, bool kSources>
+template <bool kDenseJ, bool kSources, bool kFma>
 __global__ void __launch_bounds__(256) e_update_fp64(Grid g, Box b, const double* __restrict__ Bx,
                                                      const double* __restrict__ By,
                                                      const double* __restrict__ Bz,
@@ -112,10 +131,6 @@ __global__ void __launch_bounds__(256) e_update_fp64(Grid g, Box b, const double
     const double by_ip = By[col_ip + base];
     const double bx_jp = Bx[col_jp + base];
 
-    double tx = DSUB(DMUL(cy, DSUB(bz, bz_jp)), DMUL(cz, DSUB(by, by_kp)));
-    double ty = DSUB(DMUL(cz, DSUB(bx, bx_kp)), DMUL(cx, DSUB(bz, bz_ip)));
-    double tz = DSUB(DMUL(cx, DSUB(by, by_ip)), DMUL(cy, DSUB(bx, bx_jp)));
-
     bool has_j = false;
     double jx = 0.0, jy = 0.0, jz = 0.0;
     if (kDenseJ) {
@@ -125,6 +140,25 @@ __global__ void __launch_bounds__(256) e_update_fp64(Grid g, Box b, const double
       has_j = true;
     }
     if (kSources) has_j |= source_current(ss, s, i, j, k, g, jx, jy, jz);
+    if (kFma) {
+      // E + cJ J + c1 d1 - c2 d2 as DFMAs into E
+      double ex = Ex[col + base], ey = Ey[col + base], ez = Ez[col + base];
+      if (has_j) {
+        ex = __fma_rn(cJ, jx, ex);
+        ey = __fma_rn(cJ, jy, ey);
+        ez = __fma_rn(cJ, jz, ez);
+      }
+      Ex[col + base] = __fma_rn(cy, DSUB(bz, bz_jp), __fma_rn(-cz, DSUB(by, by_kp), ex));
+      Ey[col + base] = __fma_rn(cz, DSUB(bx, bx_kp), __fma_rn(-cx, DSUB(bz, bz_ip), ey));
+      Ez[col + base] = __fma_rn(cx, DSUB(by, by_ip), __fma_rn(-cy, DSUB(bx, bx_jp), ez));
+      bx_kp = bx;
+      by_kp = by;
+      base += g.plane;
+      continue;
+    }
+    double tx = DSUB(DMUL(cy, DSUB(bz, bz_jp)), DMUL(cz, DSUB(by, by_kp)));
+    double ty = DSUB(DMUL(cz, DSUB(bx, bx_kp)), DMUL(cx, DSUB(bz, bz_ip)));
+    double tz = DSUB(DMUL(cx, DSUB(by, by_ip)), DMUL(cy, DSUB(bx, bx_jp)));
     if (has_j) {
       // (cJ*J + c1*d1) - c2*d2, the reference's association.
       tx = DSUB(DADD(DMUL(cJ, jx), DMUL(cy, DSUB(bz, bz_jp))), DMUL(cz, DSUB(by, by_kp)));
@@ -149,34 +183,47 @@ static dim3 fp64_grid(const Box& b, int kchunk) {
 }
 
 cudaError_t launch_b_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const double cb[3],
-                          int applications, cudaStream_t st) {
+                          int applications, bool fma, cudaStream_t st) {
   if (box.empty()) return cudaSuccess;
   const int kchunk = 16;
   dim3 block(32, 8), grid = fp64_grid(box, kchunk);
-  if (applications == 2)
-    b_update_fp64<2><<<grid, block, 0, st>>>(g, box, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5],
-                                             cb[0], cb[1], cb[2], kchunk);
-  else
-    b_update_fp64<1><<<grid, block, 0, st>>>(g, box, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5],
-                                             cb[0], cb[1], cb[2], kchunk);
+#define FDTD_B64(APPS, FMA)                                                                              \
+  b_update_fp64<APPS, FMA><<<grid, block, 0, st>>>(g, box, F.f[0], F.f[1], F.f[2], F.f[3], F.f[4], F.f[5], \
+                                                   cb[0], cb[1], cb[2], kchunk)
+  if (applications == 2) {
+    if (fma) FDTD_B64(2, true);
+    else FDTD_B64(2, false);
+  } else {
+    if (fma) FDTD_B64(1, true);
+    else FDTD_B64(1, false);
+  }
+#undef FDTD_B64
   return cudaGetLastError();
 }
 
-cudaError_t launch_e_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const double ce[3], double cJ,
-                          bool dense_j, const SourceSet& ss, int64_t step, cudaStream_t st) {
-  if (box.empty()) return cudaSuccess;
-  const int kchunk = 16;
-  dim3 block(32, 8), grid = fp64_grid(box, kchunk);
+template <bool FMA>
+static void launch_e_fp64_arith(dim3 grid, dim3 block, const Grid& g, const Box& box, const Fp64Fields& F,
+                                const double ce[3], double cJ, bool dense_j, const SourceSet& ss, int64_t step,
+                                int kchunk, cudaStream_t st) {
   const bool src = ss.count > 0;
-#define FDTD_E64(DJ, SRC)                                                                     \
-  e_update_fp64<DJ, SRC><<<grid, block, 0, st>>>(g, box, F.f[3], F.f[4], F.f[5], F.f[6], F.f[7], \
-                                                 F.f[8], F.f[0], F.f[1], F.f[2], cJ, ce[0],   \
-                                                 ce[1], ce[2], kchunk, ss, step)
+#define FDTD_E64(DJ, SRC)                                                                          \
+  e_update_fp64<DJ, SRC, FMA><<<grid, block, 0, st>>>(g, box, F.f[3], F.f[4], F.f[5], F.f[6], F.f[7], \
+                                                      F.f[8], F.f[0], F.f[1], F.f[2], cJ, ce[0],   \
+                                                      ce[1], ce[2], kchunk, ss, step)
   if (dense_j && src) FDTD_E64(true, true);
   else if (dense_j) FDTD_E64(true, false);
   else if (src) FDTD_E64(false, true);
   else FDTD_E64(false, false);
 #undef FDTD_E64
+}
+
+cudaError_t launch_e_fp64(const Grid& g, const Box& box, const Fp64Fields& F, const double ce[3], double cJ,
+                          bool dense_j, const SourceSet& ss, int64_t step, bool fma, cudaStream_t st) {
+  if (box.empty()) return cudaSuccess;
+  const int kchunk = 16;
+  dim3 block(32, 8), grid = fp64_grid(box, kchunk);
+  if (fma) launch_e_fp64_arith<true>(grid, block, g, box, F, ce, cJ, dense_j, ss, step, kchunk, st);
+  else launch_e_fp64_arith<false>(grid, block, g, box, F, ce, cJ, dense_j, ss, step, kchunk, st);
   return cudaGetLastError();
 }
 

@@ -305,6 +305,12 @@ class FDTD:
         arr = (ctypes.c_int * 6)(*[int(e) for e in exps])
         _lib.check(self._lib.fdtd_set_fp16_exponents(self._handle(), arr))
 
+    def set_fp64_arith(self, contracted):
+        """FP64 form: False keeps the reference's arithmetic bit for bit (the
+        default); True accumulates each curl and current term with DFMA
+        (fewer FP64 instructions; within a few ulps per step)."""
+        _lib.check(self._lib.fdtd_set_fp64_arith(self._handle(), 1 if contracted else 0))
+
     KERNEL_KINDS = ("e_update", "b_half", "b_double", "fused_step")
     PIPELINES = {"auto": 0, "split": 1, "fused": 2}
 
@@ -346,6 +352,15 @@ class FDTD:
         return {"coef_E": (cdt / p.dx, cdt / p.dy, cdt / p.dz),
                 "coef_B": (cdt / (2.0 * p.dx), cdt / (2.0 * p.dy), cdt / (2.0 * p.dz)),
                 "current_coef": -4.0 * Const.PI * dt}
+
+
+def measure_fp64_rate():
+    """Issue rate of the current GPU's FP64 pipe (DMUL/DADD instructions per
+    second) and the probe's duration in ms (fdtd_measure_fp64_rate)."""
+    lib = _lib.load()
+    rate, ms = ctypes.c_double(), ctypes.c_double()
+    _lib.check(lib.fdtd_measure_fp64_rate(ctypes.byref(rate), ctypes.byref(ms)))
+    return rate.value, ms.value
 
 
 class FDTD_PML(FDTD):

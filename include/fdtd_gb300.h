@@ -186,6 +186,21 @@ int fdtd_get_params(fdtd_handle* h, fdtd_params* params, double* dt, int* precis
 int fdtd_set_stream(fdtd_handle* h, void* stream);
 int fdtd_synchronize(fdtd_handle* h);
 
+/* Arithmetic of the FP64 form (new).  BITWISE (the default) evaluates the
+ * reference's expressions (kokkos_functors.h:64-90, :128-151) in its
+ * operation order with no fused multiply-add: bit-identical to the
+ * reference.  CONTRACTED accumulates each curl and current term into the
+ * field with DFMA (24 FP64 instructions per cell-step against 39; the FP64
+ * pipe bounds these sweeps on GB300): within a few ulps of the reference per
+ * step.  Other storage forms give FDTD_ERR_UNSUPPORTED. */
+enum fdtd_fp64_arith { FDTD_FP64_BITWISE = 0, FDTD_FP64_CONTRACTED = 1 };
+int fdtd_set_fp64_arith(fdtd_handle* h, int arith);
+
+/* Measured issue rate of the FP64 pipe of the current device (new; the
+ * roofline of the FP64 sweeps): independent DMUL/DADD chains on every SM,
+ * timed with CUDA events.  Synchronous; about 50 ms. */
+int fdtd_measure_fp64_rate(double* dp_instr_per_s, double* ms);
+
 /* Per-component power-of-two scales of the FP16_SCALED form: stored value =
  * field * 2^exponent.  `exponents` has 6 entries (Ex..Bz), each in [-60, 60]. */
 int fdtd_set_fp16_exponents(fdtd_handle* h, const int exponents[6]);

@@ -177,6 +177,11 @@ class FDTD {
     return idx;
   }
   void field_sums(double out[FDTD_DIAG_COUNT]) { check(fdtd_field_sums(h_, out)); }
+  // FP64 form: DFMA-contracted sweeps (true) or the reference's arithmetic
+  // bit for bit (false, the default).
+  void set_fp64_arith(bool contracted) {
+    check(fdtd_set_fp64_arith(h_, contracted ? FDTD_FP64_CONTRACTED : FDTD_FP64_BITWISE));
+  }
   const Parameters& parameters() const { return parameters_; }
   FP dt() const { return dt_; }
   fdtd_handle* handle() const { return h_; }

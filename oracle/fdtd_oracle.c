@@ -18,6 +18,7 @@
  *   parameter validation      src/FDTD_kokkos/FDTD_kokkos.cpp:7-12
  *   update_fields = B/2,E,B/2 src/FDTD_kokkos/FDTD_kokkos.cpp:91-104
  *   current box source        perf-tests/kokkos_sample/kokkos_sample.cpp:88-129
+ *   OpenMP solver twin        src/FDTD/FDTD.cpp:63-157 (timed CPU path only)
  *   PML (split-field layer)   src/FDTD_kokkos/FDTD_PML_kokkos.cpp:22-189,
  *                             include/FDTD_kokkos/kokkos_functors.h:154-415
  *
@@ -260,6 +261,83 @@ void oracle_run_driver(long Ni, long Nj, long Nk, double* f[9], const double coe
         oracle_update_E(Ni, Nj, Nk, f[3], f[4], f[5], J[0], J[1], J[2], f[0], f[1], f[2],
                         coef[6], coef[0], coef[1], coef[2]);
         oracle_update_B(Ni, Nj, Nk, f[0], f[1], f[2], f[3], f[4], f[5], coef[3], coef[4], coef[5]);
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * The reference's OpenMP solver twin, FDTD_openmp::FDTD
+ * (src/FDTD/FDTD.cpp:63-157): the second timed CPU path of the benchmark.
+ *
+ * Its loops differ from the Kokkos path's: OpenMP over k, the plane and row
+ * offsets and the wrapped neighbour rows computed once per k and per j, and
+ * an `omp simd` loop over i (FDTD.cpp:64-97 E, :99-130 B).  Its E update adds
+ * cur_coef * Jx to all three components (FDTD.cpp:82-90), so it is the
+ * Kokkos path only at J = 0; this restatement keeps that line, so it gives
+ * the twin's results and streams the twin's bytes (Jx read, Jy and Jz not).
+ * f = the nine arrays in component order (f[6] must exist). */
+static void twin_update_E(long Ni, long Nj, long Nk, double* f[9], const double coef[7]) {
+    const double* Bx = f[3];
+    const double* By = f[4];
+    const double* Bz = f[5];
+    const double* Jx = f[6];
+    double* Ex = f[0];
+    double* Ey = f[1];
+    double* Ez = f[2];
+    const double cJ = coef[6], cx = coef[0], cy = coef[1], cz = coef[2];
+    const long plane = Ni * Nj;
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < Nk; ++k) {
+        const long zk = k * plane, zp = wrap(k - 1, Nk) * plane;
+        for (long j = 0; j < Nj; ++j) {
+            const long row = zk + j * Ni;           /* (., j, k) */
+            const long row_jp = zk + wrap(j - 1, Nj) * Ni;  /* (., j-1, k) */
+            const long row_kp = zp + j * Ni;        /* (., j, k-1) */
+#pragma omp simd
+            for (long i = 0; i < Ni; ++i) {
+                const long c = row + i, ip = row + wrap(i - 1, Ni);
+                const long jp = row_jp + i, kp = row_kp + i;
+                Ex[c] += cJ * Jx[c] + cy * (Bz[c] - Bz[jp]) - cz * (By[c] - By[kp]);
+                Ey[c] += cJ * Jx[c] + cz * (Bx[c] - Bx[kp]) - cx * (Bz[c] - Bz[ip]);
+                Ez[c] += cJ * Jx[c] + cx * (By[c] - By[ip]) - cy * (Bx[c] - Bx[jp]);
+            }
+        }
+    }
+}
+
+static void twin_update_B(long Ni, long Nj, long Nk, double* f[9], const double coef[7]) {
+    const double* Ex = f[0];
+    const double* Ey = f[1];
+    const double* Ez = f[2];
+    double* Bx = f[3];
+    double* By = f[4];
+    double* Bz = f[5];
+    const double cx = coef[3], cy = coef[4], cz = coef[5];
+    const long plane = Ni * Nj;
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < Nk; ++k) {
+        const long zk = k * plane, zn = wrap(k + 1, Nk) * plane;
+        for (long j = 0; j < Nj; ++j) {
+            const long row = zk + j * Ni;           /* (., j, k) */
+            const long row_jn = zk + wrap(j + 1, Nj) * Ni;  /* (., j+1, k) */
+            const long row_kn = zn + j * Ni;        /* (., j, k+1) */
+#pragma omp simd
+            for (long i = 0; i < Ni; ++i) {
+                const long c = row + i, in = row + wrap(i + 1, Ni);
+                const long jn = row_jn + i, kn = row_kn + i;
+                Bx[c] += cz * (Ey[kn] - Ey[c]) - cy * (Ez[jn] - Ez[c]);
+                By[c] += cx * (Ez[in] - Ez[c]) - cz * (Ex[kn] - Ex[c]);
+                Bz[c] += cy * (Ex[jn] - Ex[c]) - cx * (Ey[in] - Ey[c]);
+            }
+        }
+    }
+}
+
+/* FDTD_openmp::FDTD::update_fields (src/FDTD/FDTD.cpp:153-157) `steps` times. */
+void oracle_twin_run(long Ni, long Nj, long Nk, double* f[9], const double coef[7], int steps) {
+    for (int s = 0; s < steps; ++s) {
+        twin_update_B(Ni, Nj, Nk, f, coef);
+        twin_update_E(Ni, Nj, Nk, f, coef);
+        twin_update_B(Ni, Nj, Nk, f, coef);
     }
 }
 

@@ -63,6 +63,9 @@ def oracle_lib():
         lib.oracle_run_driver.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.POINTER(_D), _D,
                                           ctypes.POINTER(OracleSource), ctypes.c_int, ctypes.c_long, ctypes.c_int]
         lib.oracle_run_driver.restype = None
+        lib.oracle_twin_run.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.POINTER(_D), _D,
+                                        ctypes.c_int]
+        lib.oracle_twin_run.restype = None
         lib.oracle_pml_sizes.argtypes = [ctypes.POINTER(OracleParams), ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
         lib.oracle_pml_sizes.restype = None
         lib.oracle_pml_sigma.argtypes = [ctypes.POINTER(OracleParams), ctypes.c_double, _D, _D, _D]
@@ -159,6 +162,18 @@ class Oracle:
         csrc, keep = self._csources()
         oracle_lib().oracle_run_driver(p.Ni, p.Nj, p.Nk, ptrs, _ptr(self.coef), csrc, len(self.sources),
                                        self.step_index, int(n))
+        self.step_index += int(n)
+
+    def step_twin(self, n=1):
+        """n update_fields of the reference's OpenMP twin (oracle_twin_run):
+        the Kokkos path's results at J = 0; with current it keeps the twin's
+        Jx line (src/FDTD/FDTD.cpp:82-90).  Sources are not evaluated."""
+        p = self.params
+        for c in range(6, 9):
+            if self.f[c] is None:
+                self.f[c] = np.zeros_like(self.f[0])
+        ptrs = (_D * 9)(*[_ptr(a) for a in self.f])
+        oracle_lib().oracle_twin_run(p.Ni, p.Nj, p.Nk, ptrs, _ptr(self.coef), int(n))
         self.step_index += int(n)
 
     def step(self, n=1):

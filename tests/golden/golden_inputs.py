@@ -15,6 +15,16 @@ CASES = {
 }
 
 
+# Runs of the reference's OpenMP twin (FDTD_openmp::FDTD, src/FDTD/FDTD.cpp);
+# with J != 0 they record its Jx line (:82-90), with J = 0 the Kokkos path
+TWIN_CASES = {
+    "twin_random_12x10x7": {"n": (12, 10, 7), "steps": 5, "seed": 31, "comps": range(9)},
+    "twin_noJ_9x6x5": {"n": (9, 6, 5), "steps": 7, "seed": 32, "comps": range(6)},
+    "twin_odd_7x3x5": {"n": (7, 3, 5), "steps": 6, "seed": 33, "comps": range(9)},
+    "twin_tiny_1x1x1": {"n": (1, 1, 1), "steps": 4, "seed": 34, "comps": range(9)},
+}
+
+
 # PML cases (FDTD_PML(Parameters, dt, pml_percent)); same domain and inputs
 PML_CASES = {
     "pml_random_20x16x12_p20": {"n": (20, 16, 12), "steps": 6, "seed": 21, "comps": range(9), "pml": 0.2},

@@ -13,8 +13,11 @@ unmodified against the host Kokkos stand-in.  Outputs:
                              program (perf-tests/kokkos_sample/kokkos_sample.cpp)
   reference_pml_cases.npz    final E and B of small runs of FDTD_kokkos::FDTD_PML
                              (src/FDTD_kokkos/FDTD_PML_kokkos.cpp) on seeded inputs
+  reference_twin_cases.npz   final fields of small runs of the reference's
+                             OpenMP twin FDTD_openmp::FDTD (src/FDTD/FDTD.cpp)
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py twin pml   # the named ones only
 """
 import json
 import os
@@ -27,29 +30,33 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from golden_inputs import CASES, PML_CASES, case_inputs, case_params  # noqa: E402
+from golden_inputs import CASES, PML_CASES, TWIN_CASES, case_inputs, case_params  # noqa: E402
 from oracle import RefKokkos, run_reference_unit_tests  # noqa: E402
 from oracle.oracle import REF_DIR  # noqa: E402
 
 
-def main():
+def unit_tests():
     tests = run_reference_unit_tests()
     with open(os.path.join(HERE, "reference_unit_tests.json"), "w") as f:
         json.dump({k: {"value": v[0], "expected": v[1], "tol": v[2], "passed": v[3]}
                    for k, v in sorted(tests.items())}, f, indent=1)
 
+
+def runs(cases, kind, path):
     out = {}
-    for name, spec in CASES.items():
+    for name, spec in cases.items():
         params, dt = case_params(spec)
-        ref = RefKokkos(params, dt)
+        ref = RefKokkos(params, dt, kind=kind)
         for comp, values in case_inputs(spec).items():
             ref.set(comp, values)
         ref.update_fields(spec["steps"])
         for comp in range(9):
             out["%s/%d" % (name, comp)] = ref.get(comp)
         ref.close()
-    np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **out)
+    np.savez_compressed(os.path.join(HERE, path), **out)
 
+
+def pml():
     out = {}
     for name, spec in PML_CASES.items():
         params, dt = case_params(spec)
@@ -62,6 +69,8 @@ def main():
         ref.close()
     np.savez_compressed(os.path.join(HERE, "reference_pml_cases.npz"), **out)
 
+
+def sample():
     sample = {}
     for n, it in ((16, 60), (32, 100), (20, 30)):
         r = subprocess.run([os.path.join(REF_DIR, "kokkos_sample"), str(n), str(it)],
@@ -71,8 +80,22 @@ def main():
         sample["%d_%d" % (n, it)] = rows
     with open(os.path.join(HERE, "reference_sample.json"), "w") as f:
         json.dump(sample, f, indent=1)
+
+
+FIXTURES = {
+    "unit": unit_tests,
+    "cases": lambda: runs(CASES, "kokkos", "reference_cases.npz"),
+    "pml": pml,
+    "sample": sample,
+    "twin": lambda: runs(TWIN_CASES, "openmp", "reference_twin_cases.npz"),
+}
+
+
+def main(names):
+    for name in names or sorted(FIXTURES):
+        FIXTURES[name]()
     print("wrote", sorted(os.listdir(HERE)))
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from golden_inputs import CASES, PML_CASES, case_inputs, case_params
+from golden_inputs import CASES, PML_CASES, TWIN_CASES, case_inputs, case_params
 from oracle import Oracle, OraclePML, RefKokkos, coefficients, field_sums, ref_available
 from refcases import CONVERGENCE_CASES, run_convergence
 
@@ -61,6 +61,56 @@ def test_oracle_matches_reference_golden_cases(name):
     o.step(spec["steps"])
     for c in range(9):
         np.testing.assert_array_equal(o.get(c), golden["%s/%d" % (name, c)], err_msg="component %d" % c)
+
+
+@pytest.mark.parametrize("name", sorted(TWIN_CASES))
+def test_twin_restatement_matches_reference_twin_runs(name):
+    """oracle_twin_run (the timed second CPU path) is the reference's OpenMP
+    twin (src/FDTD/FDTD.cpp) bit for bit, its Jx line included."""
+    golden = np.load(os.path.join(GOLDEN, "reference_twin_cases.npz"))
+    spec = TWIN_CASES[name]
+    p, dt = case_params(spec)
+    o = Oracle(p, dt)
+    for c, v in case_inputs(spec).items():
+        o.set(c, v)
+    o.step_twin(spec["steps"])
+    for c in range(9):
+        np.testing.assert_array_equal(o.get(c), golden["%s/%d" % (name, c)], err_msg="component %d" % c)
+
+
+@pytest.mark.parametrize("shape", [(12, 10, 7), (1, 1, 1), (5, 1, 3), (16, 8, 4)])
+def test_twin_equals_the_kokkos_path_without_current(shape):
+    """At J = 0 the twin and the Kokkos path give the same bits (the twin's
+    only arithmetic difference is its current line)."""
+    Ni, Nj, Nk = shape
+    p = Parameters(Ni, Nj, Nk, 0, 1, 0, 2, 0, 3, 1.0 / Ni, 2.0 / Nj, 3.0 / Nk)
+    dt = 0.3 * min(p.dx, p.dy, p.dz) / 3e10
+    rng = np.random.default_rng(Ni * 100 + Nj * 10 + Nk)
+    a, b = Oracle(p, dt), Oracle(p, dt)
+    for c in range(6):
+        v = rng.standard_normal(p.cells)
+        a.set(c, v)
+        b.set(c, v)
+    a.step(5)
+    b.step_twin(5)
+    for c in range(6):
+        np.testing.assert_array_equal(a.get(c), b.get(c))
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference build (oracle/_ref) not present on this host")
+def test_twin_restatement_bitwise_equal_to_reference_twin_build():
+    p = Parameters(11, 6, 9, 0, 1, 0, 2, 0, 3, 1.0 / 11, 2.0 / 6, 3.0 / 9)
+    dt = 0.3 * min(p.dx, p.dy, p.dz) / 3e10
+    rng = np.random.default_rng(5)
+    o, r = Oracle(p, dt), RefKokkos(p, dt, kind="openmp")
+    for c in range(9):
+        v = rng.standard_normal(p.cells)
+        o.set(c, v)
+        r.set(c, v)
+    o.step_twin(6)
+    r.update_fields(6)
+    for c in range(9):
+        np.testing.assert_array_equal(o.get(c), r.get(c))
 
 
 @pytest.mark.parametrize("name,field,sel,grid", CONVERGENCE_CASES)
