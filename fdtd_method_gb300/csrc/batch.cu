@@ -4,10 +4,16 @@
 // batch adds device tables that describe every domain to one persistent
 // fused-step kernel, and runs a step group as one CUDA graph:
 //
-//   leading B half step of every domain      (one launch, kernels_f32.cu)
-//   n fused sweeps of every domain           (n persistent launches over the
+//   n B-first sweeps of every domain         (n persistent launches over the
 //                                             tile table, kernels_fused1.cu)
 //   step counter += n                        (one thread)
+//
+// As for a single handle, the last step's trailing B half is left pending
+// and the next group's first sweep applies it with its own leading half;
+// readers of a domain see it applied (the domain handle's read path), and
+// before anything writes a domain's E or B the batch applies it to every
+// domain in one launch (kernels_f32.cu b_sweep_batch), so all domains stay
+// at the same point of the step.
 //
 // The per-domain tile table lists (domain, bx, by, bz) for every tile of every
 // domain, domain by domain; the persistent CTAs take tiles from it in order.
@@ -18,6 +24,7 @@
 #include <algorithm>
 #include <map>
 #include <string>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -58,6 +65,7 @@ struct fdtd_batch {
   int parity = 0;     // which copy of the tables' two is current
   int64_t step = 0;   // completed steps
   bool dirty = true;  // device tables out of date
+  bool pending = false;  // every domain's trailing B half step is pending
   // device tables
   void* d_doms = nullptr;        // BatchDomain<S>[n]
   StepMaps* d_maps = nullptr;    // [2 n]
@@ -68,7 +76,7 @@ struct fdtd_batch {
   int* d_counters = nullptr;     // 2 ints, zero between launches
   int64_t* d_step = nullptr;
   int* d_err = nullptr;
-  std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
+  std::map<std::tuple<int64_t, int, int>, cudaGraphExec_t> graphs;  // (steps, parity, first sweep's apps)
 };
 
 namespace {
@@ -129,9 +137,9 @@ int build_tables(fdtd_batch* b) {
     fdtd_handle* h = b->doms[d];
     h->fused_cfg = b->cfg;
     if (int rc = ensure_alt(h)) return rc;
-    maps[2 * d].ld = h->maps_cur;
+    maps[2 * d].ld = h->bmaps_cur;
     maps[2 * d].st = h->smaps_alt;
-    maps[2 * d + 1].ld = h->maps_alt;
+    maps[2 * d + 1].ld = h->bmaps_alt;
     maps[2 * d + 1].st = h->smaps_cur;
     const int tx = (h->g.Ni + 31) / 32, ty = (h->g.Nj + b->cfg.tile_y - 1) / b->cfg.tile_y;
     const int tz = (h->g.Nk + b->cfg.kchunk - 1) / b->cfg.kchunk;
@@ -169,16 +177,17 @@ int build_tables(fdtd_batch* b) {
 }
 
 cudaError_t launch_fused_all(fdtd_batch* b, int parity, int apps, int step_off) {
+  const WaitCtl wc{b->d_err, kMaxBarrierPolls, 0};
   switch (b->form) {
     case Form::F32:
       return launch_fused1_batch<StoreF32>(b->d_doms, b->d_maps, b->d_tiles, b->n_tiles, parity, apps, b->cfg,
-                                           b->d_step, step_off, b->d_counters, b->d_err, b->stream);
+                                           b->d_step, step_off, b->d_counters, wc, b->stream);
     case Form::F32C:
       return launch_fused1_batch<StoreF32C>(b->d_doms, b->d_maps, b->d_tiles, b->n_tiles, parity, apps, b->cfg,
-                                            b->d_step, step_off, b->d_counters, b->d_err, b->stream);
+                                            b->d_step, step_off, b->d_counters, wc, b->stream);
     case Form::F16:
       return launch_fused1_batch<StoreF16>(b->d_doms, b->d_maps, b->d_tiles, b->n_tiles, parity, apps, b->cfg,
-                                           b->d_step, step_off, b->d_counters, b->d_err, b->stream);
+                                           b->d_step, step_off, b->d_counters, wc, b->stream);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -193,16 +202,32 @@ cudaError_t launch_b_all(fdtd_batch* b, int parity) {
   }
 }
 
-// The launches of `n` steps from copy `parity`.
-cudaError_t enqueue_steps(fdtd_batch* b, int64_t n, int parity) {
-  cudaError_t e = launch_b_all(b, parity);
+// The launches of `n` steps from copy `parity`; the first sweep applies
+// `first_apps` B half steps (2: the pending one and its own leading one).
+cudaError_t enqueue_steps(fdtd_batch* b, int64_t n, int parity, int first_apps) {
+  cudaError_t e = cudaSuccess;
   for (int64_t s = 0; s < n && e == cudaSuccess; ++s)
-    e = launch_fused_all(b, parity ^ (int)(s & 1), s + 1 < n ? 2 : 1, (int)s);
+    e = launch_fused_all(b, parity ^ (int)(s & 1), s == 0 ? first_apps : 2, (int)s);
   if (e == cudaSuccess) {
     advance_step<<<1, 1, 0, b->stream>>>(b->d_step, n);
     e = cudaGetLastError();
   }
   return e;
+}
+
+// Applies the pending B half step of every domain (one launch) before
+// anything writes a domain's E or B.
+int resolve_batch(fdtd_batch* b) {
+  if (!b->pending) return FDTD_OK;
+  if (b->dirty)
+    if (int rc = build_tables(b)) return rc;
+  FDTD_BCUDA(launch_b_all(b, b->parity), "pending B half step of the batch");
+  b->pending = false;
+  for (fdtd_handle* h : b->doms) {
+    h->b_pending = false;
+    h->b_side = false;
+  }
+  return FDTD_OK;
 }
 
 int check_batch(fdtd_batch* b) {
@@ -304,6 +329,7 @@ int fdtd_batch_copy_field_from_host(fdtd_batch* b, int d, int comp, const double
   if (comp < FDTD_EX || comp > FDTD_BZ)
     return bfail(FDTD_ERR_LOGIC, "ERROR: Invalid field component");
   DeviceGuard dg(b->device);
+  if (int rc = resolve_batch(b)) return rc;
   return fdtd_copy_field_from_host(b->doms[d], comp, host, n);
 }
 
@@ -315,6 +341,10 @@ int fdtd_batch_field_sums(fdtd_batch* b, int d, double out[FDTD_DIAG_COUNT]) {
 
 int fdtd_batch_set_fp16_exponents(fdtd_batch* b, int d, const int exponents[6]) {
   if (int rc = check_domain(b, d)) return rc;
+  {
+    DeviceGuard dg(b->device);
+    if (int rc = resolve_batch(b)) return rc;
+  }
   const int rc = fdtd_set_fp16_exponents(b->doms[d], exponents);
   if (rc == FDTD_OK) b->dirty = true;
   return rc;
@@ -349,14 +379,15 @@ int fdtd_batch_step(fdtd_batch* b, int64_t n) {
   DeviceGuard dg(b->device);
   if (b->dirty)
     if (int rc = build_tables(b)) return rc;
+  const int first_apps = b->pending ? 2 : 1;
   if (b->use_graphs) {
-    const auto key = std::make_pair(n, b->parity);
+    const auto key = std::make_tuple(n, b->parity, first_apps);
     auto it = b->graphs.find(key);
     if (it == b->graphs.end()) {
       cudaGraph_t g = nullptr;
       cudaGraphExec_t ge = nullptr;
       FDTD_BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed), "graph capture");
-      cudaError_t e = enqueue_steps(b, n, b->parity);
+      cudaError_t e = enqueue_steps(b, n, b->parity, first_apps);
       cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
       if (e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -370,14 +401,19 @@ int fdtd_batch_step(fdtd_batch* b, int64_t n) {
     }
     FDTD_BCUDA(cudaGraphLaunch(it->second, b->stream), "batch step graph launch");
   } else {
-    FDTD_BCUDA(enqueue_steps(b, n, b->parity), "batch step launch");
+    FDTD_BCUDA(enqueue_steps(b, n, b->parity, first_apps), "batch step launch");
   }
   if (n & 1) {
     b->parity ^= 1;
     for (fdtd_handle* h : b->doms) swap_copies(h);
   }
   b->step += n;
-  for (fdtd_handle* h : b->doms) h->host_step = b->step;
+  b->pending = true;
+  for (fdtd_handle* h : b->doms) {
+    h->host_step = b->step;
+    h->b_pending = true;
+    h->b_side = false;
+  }
   return FDTD_OK;
 }
 
@@ -432,6 +468,7 @@ int fdtd_batch_autotune(fdtd_batch* b, int sweeps, fdtd_tune_result* out) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  for (fdtd_handle* h : b->doms) h->b_side = false;  // the timed sweeps wrote the second copies
   if (rc != FDTD_OK) return rc;
   b->cfg.tile_y = best.tile_y;
   b->cfg.kchunk = best.kchunk;

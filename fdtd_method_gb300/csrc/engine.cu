@@ -236,10 +236,14 @@ int run_e(fdtd_handle* h, int64_t step) {
   return FDTD_OK;
 }
 
-// E step `step` followed by `apps` B half steps, in one sweep from the
-// current copy into the second one, which then becomes current.
-// One fused sweep from the current copy into the second one, without the
-// swap (the autotuner repeats it to time a tile shape: the state is only read).
+// Whether the handle's fused sweeps run B-first (one cell per thread) or
+// E-first (the two-cell kernel).
+bool b_first(const fdtd_handle* h) { return h->fused_cfg.cells_per_thread == 1; }
+
+// One fused sweep of step `step` from the current copy into the second one,
+// without the swap (the autotuner repeats it to time a tile shape: the state
+// is only read).  B-first: `apps` B half steps, then E; E-first: E, then
+// `apps` B half steps.
 cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps) {
   SourceSet ss = h->source_set();
   StateView v = h->view();
@@ -247,24 +251,28 @@ cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps) {
   const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
   const bool dj = h->dense_j && h->jf[0];
   const FusedConfig& cf = h->fused_cfg;
+  const bool bf = b_first(h);
+  const WaitCtl wc = h->wait_ctl();
   StepMaps sm;
-  sm.ld = h->maps_cur;
+  sm.ld = bf ? h->bmaps_cur : h->maps_cur;
   sm.st = h->smaps_alt;
-  const void* m = cf.cells_per_thread == 2 ? static_cast<const void*>(&h->maps_cur) : static_cast<const void*>(&sm);
   cudaError_t e = cudaSuccess;
-#define FDTD_FUSED_LAUNCH(FN)                                                                                  \
-  switch (h->form) {                                                                                         \
-    case Form::F32: e = FN(h->L, v.s32, w.s32, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;    \
-    case Form::F32C: e = FN(h->L, v.s32c, w.s32c, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break; \
-    case Form::F16: e = FN(h->L, v.s16, w.s16, m, J, dj, h->cs, ss, step, apps, cf, h->d_err, h->stream); break;    \
-    default: e = cudaErrorInvalidValue; break;                                                               \
-  }
   if (cf.cells_per_thread == 2) {
-    FDTD_FUSED_LAUNCH(launch_fused_f32)
-  } else {
-    FDTD_FUSED_LAUNCH(launch_fused1_f32)
+    const void* m = &h->maps_cur;
+    switch (h->form) {
+      case Form::F32: e = launch_fused_f32(h->L, v.s32, w.s32, m, J, dj, h->cs, ss, step, apps, cf, wc, h->stream); break;
+      case Form::F32C: e = launch_fused_f32(h->L, v.s32c, w.s32c, m, J, dj, h->cs, ss, step, apps, cf, wc, h->stream); break;
+      case Form::F16: e = launch_fused_f32(h->L, v.s16, w.s16, m, J, dj, h->cs, ss, step, apps, cf, wc, h->stream); break;
+      default: e = cudaErrorInvalidValue; break;
+    }
+    return e;
   }
-#undef FDTD_FUSED_LAUNCH
+  switch (h->form) {
+    case Form::F32: e = launch_fused1_f32(h->L, v.s32, w.s32, &sm, J, dj, h->cs, ss, step, apps, cf, bf, wc, h->stream); break;
+    case Form::F32C: e = launch_fused1_f32(h->L, v.s32c, w.s32c, &sm, J, dj, h->cs, ss, step, apps, cf, bf, wc, h->stream); break;
+    case Form::F16: e = launch_fused1_f32(h->L, v.s16, w.s16, &sm, J, dj, h->cs, ss, step, apps, cf, bf, wc, h->stream); break;
+    default: e = cudaErrorInvalidValue; break;
+  }
   return e;
 }
 
@@ -372,8 +380,13 @@ int ensure_alt(fdtd_handle* h) {
     const int lbw = two ? fused_lo_box_width() : fused1_lo_box_width();
     LoT* const* lo_cur = h->form == Form::F32C ? h->lo : nullptr;
     LoT* const* lo_alt = h->form == Form::F32C ? h->alt_lo : nullptr;
-    if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, lbw, h->fused_cfg.tile_y, !two) != cudaSuccess ||
-        build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, h->fused_cfg.tile_y, !two) != cudaSuccess)
+    const int ty = h->fused_cfg.tile_y;
+    const BoxTrim trim = two ? BoxTrim::None : BoxTrim::EFirst;
+    if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, lbw, ty, trim) != cudaSuccess ||
+        build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, ty, trim) != cudaSuccess)
+      return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
+    if (!two && (build_tma_maps(&h->bmaps_cur, h->L, ht, h->field, lo_cur, bw, lbw, ty, BoxTrim::BFirst) != cudaSuccess ||
+                 build_tma_maps(&h->bmaps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, ty, BoxTrim::BFirst) != cudaSuccess))
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
     if (!two && (build_tma_store_maps(&h->smaps_cur, h->L, ht, h->field, lo_cur, h->fused_cfg.tile_y) != cudaSuccess ||
                  build_tma_store_maps(&h->smaps_alt, h->L, ht, h->alt_field, lo_alt, h->fused_cfg.tile_y) != cudaSuccess))
@@ -390,6 +403,53 @@ void swap_copies(fdtd_handle* h) {
   }
   std::swap(h->maps_cur, h->maps_alt);
   std::swap(h->smaps_cur, h->smaps_alt);
+  std::swap(h->bmaps_cur, h->bmaps_alt);
+}
+
+int read_view(fdtd_handle* h, StateView* v) {
+  if (!h->b_pending) {
+    *v = h->view();
+    return FDTD_OK;
+  }
+  if (!h->b_side) {
+    // B with the pending half step, into the second copy's B arrays (the next
+    // sweep overwrites that copy anyway); a z slab uses side arrays, and its
+    // halo plane above holds the neighbour's E from the last exchange.
+    if (h->zhalo && !h->side_b[0]) {
+      const int64_t n = h->L.elems() + 2 * h->halo_elems();
+      for (int c = 0; c < 3; ++c) {
+        void* base = nullptr;
+        FDTD_CUDA(dev_alloc(h, &base, elem_bytes(h->form) * n), "pending B half step arrays");
+        h->side_b[c] = static_cast<unsigned char*>(base) + elem_bytes(h->form) * h->halo_elems();
+        if (h->form == Form::F32C) {
+          LoT* lb = nullptr;
+          FDTD_CUDA(dev_alloc(h, (void**)&lb, sizeof(LoT) * n), "pending B half step arrays");
+          h->side_lo[c] = lb + h->halo_elems();
+        }
+      }
+    }
+    const StateView cur = h->sweep_view(), side = h->with_halo(h->view_side());
+    const Box box = h->sweep_box();
+    cudaError_t e = cudaSuccess;
+    switch (h->form) {
+      case Form::F32: e = launch_b_f32_into(cur.L, cur.s32, side.s32, h->cs, box.k0, box.k1, h->stream); break;
+      case Form::F32C: e = launch_b_f32_into(cur.L, cur.s32c, side.s32c, h->cs, box.k0, box.k1, h->stream); break;
+      case Form::F16: e = launch_b_f32_into(cur.L, cur.s16, side.s16, h->cs, box.k0, box.k1, h->stream); break;
+      default: e = cudaErrorInvalidValue; break;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "pending B half step");
+    h->b_side = true;
+  }
+  *v = h->view_side();
+  return FDTD_OK;
+}
+
+int resolve_pending(fdtd_handle* h) {
+  if (!h->b_pending) return FDTD_OK;
+  if (int rc = run_b(h, 1)) return rc;
+  h->b_pending = false;
+  h->b_side = false;
+  return FDTD_OK;
 }
 
 }  // namespace fdtd
@@ -623,6 +683,100 @@ int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t laun
   return FDTD_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// n steps without FP16 rescans.  src/FDTD_kokkos/FDTD_kokkos.cpp:91-104
+// repeated n times; the trailing B half step of one step and the leading one
+// of the next share one sweep.
+int step_sweeps(fdtd_handle* h, int64_t n) {
+  if (h->form == Form::F64) {
+    // FP64: every call ends at the step boundary (get_field hands out the
+    // storage itself, so no half step may be left pending); B + t + t keeps
+    // the two additions, so the merged sweeps are the reference's bits.
+    if (int rc = run_b(h, 1)) return rc;
+    for (int64_t s = 0; s < n; ++s) {
+      const int apps = s + 1 < n ? 2 : 1;
+      if (h->pml) {
+        // FDTD_PML::update_fields (FDTD_PML_kokkos.cpp:162-189): B/2 inside,
+        // B on the six layer slabs, E inside, E on the slabs, B/2 inside.
+        if (int rc = run_pml(h, false)) return rc;
+        if (int rc = run_e(h, h->host_step + s)) return rc;
+        if (int rc = run_pml(h, true)) return rc;
+        if (int rc = run_b(h, apps)) return rc;
+      } else {
+        if (int rc = run_e(h, h->host_step + s)) return rc;
+        if (int rc = run_b(h, apps)) return rc;
+      }
+    }
+    return FDTD_OK;
+  }
+  // FP32-arithmetic forms: the last step's trailing B half is left pending
+  // and applied with the next step's leading half (or by the reader of B).
+  const bool fused = h->pipeline != FDTD_PIPELINE_SPLIT;
+  if (fused && b_first(h)) {
+    // B-first sweeps: sweep s applies the B half steps that meet before step
+    // s, then E.
+    for (int64_t s = 0; s < n; ++s) {
+      if (int rc = run_fused(h, h->host_step + s, h->b_pending ? 2 : 1)) return rc;
+      h->b_pending = true;
+      h->b_side = false;
+    }
+    return FDTD_OK;
+  }
+  // E-first sweeps (two cells per thread) or split sweeps: the leading half
+  // (with a pending one: both halves), then per step E and the two halves
+  // that follow it, except the last step's trailing one.
+  if (int rc = run_b(h, h->b_pending ? 2 : 1)) return rc;
+  h->b_pending = false;
+  h->b_side = false;
+  for (int64_t s = 0; s < n; ++s) {
+    const bool last = s + 1 == n;
+    if (fused && !last) {
+      if (int rc = run_fused(h, h->host_step + s, 2)) return rc;
+    } else {
+      if (int rc = run_e(h, h->host_step + s)) return rc;
+      if (!last)
+        if (int rc = run_b(h, 2)) return rc;
+    }
+  }
+  h->b_pending = true;
+  return FDTD_OK;
+}
+
+// FP16 range check (fdtd_set_fp16_autoscale): re-encodes every component
+// whose stored peak left [2^(target-4), 2^(target+2)] so that it sits in
+// (2^(target-1), 2^target]; `force` re-encodes every component with a
+// nonzero, finite peak.  Synchronous (reads six maxima).
+int fp16_rescan(fdtd_handle* h, int target, bool force, int out[6]) {
+  unsigned* d_max = reinterpret_cast<unsigned*>(h->d_diag_out);
+  FDTD_CUDA(launch_f16_absmax(h->L, h->view().s16, d_max, h->stream), "FP16 peak scan");
+  unsigned bits[6];
+  FDTD_CUDA(cudaMemcpyAsync(bits, d_max, sizeof(bits), cudaMemcpyDeviceToHost, h->stream), "FP16 peak scan");
+  FDTD_CUDA(cudaStreamSynchronize(h->stream), "FP16 peak scan");
+  for (int c = 0; c < 6; ++c) {
+    float m;
+    std::memcpy(&m, &bits[c], sizeof(m));
+    if (out) out[c] = h->fp16_exp[c];
+    if (!(m > 0.f) || !std::isfinite(m)) continue;
+    const int k = (int)std::ceil(std::log2((double)m));  // stored peak <= 2^k
+    if (!force && k >= target - 4 && k <= target + 2) continue;
+    const int e_new = std::max(-60, std::min(60, h->fp16_exp[c] + target - k));
+    const int shift = e_new - h->fp16_exp[c];
+    if (shift == 0) continue;
+    FDTD_CUDA(launch_f16_rescale(static_cast<__half*>(h->field[c]), h->L.elems(), shift, h->stream), "FP16 rescale");
+    h->fp16_exp[c] = e_new;
+    h->b_side = false;
+    if (out) out[c] = e_new;
+  }
+  return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int fdtd_step(fdtd_handle* h, int64_t n) {
   if (int rc = check_handle(h)) return rc;
   if (n < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "negative step count");
@@ -630,27 +784,17 @@ int fdtd_step(fdtd_handle* h, int64_t n) {
     return fail(FDTD_ERR_UNSUPPORTED, "a z slab steps through fdtd_slab_sweep and fdtd_slab_exchange");
   if (n == 0) return FDTD_OK;
   DeviceGuard dg(h->device);
-  // src/FDTD_kokkos/FDTD_kokkos.cpp:91-104 repeated n times; the trailing B
-  // half step of one step and the leading one of the next share one sweep.
-  const bool fused = h->form != Form::F64 && h->pipeline != FDTD_PIPELINE_SPLIT;
-  if (int rc = run_b(h, 1)) return rc;
-  for (int64_t s = 0; s < n; ++s) {
-    const int apps = s + 1 < n ? 2 : 1;
-    if (h->pml) {
-      // FDTD_PML::update_fields (FDTD_PML_kokkos.cpp:162-189): B/2 inside,
-      // B on the six layer slabs, E inside, E on the slabs, B/2 inside.
-      if (int rc = run_pml(h, false)) return rc;
-      if (int rc = run_e(h, h->host_step + s)) return rc;
-      if (int rc = run_pml(h, true)) return rc;
-      if (int rc = run_b(h, apps)) return rc;
-    } else if (fused) {
-      if (int rc = run_fused(h, h->host_step + s, apps)) return rc;
-    } else {
-      if (int rc = run_e(h, h->host_step + s)) return rc;
-      if (int rc = run_b(h, apps)) return rc;
+  const int every = h->form == Form::F16 ? h->fp16_autoscale_every : 0;
+  while (n > 0) {
+    const int64_t m = every > 0 ? std::min<int64_t>(n, every - h->fp16_autoscale_count) : n;
+    if (int rc = step_sweeps(h, m)) return rc;
+    h->host_step += m;
+    n -= m;
+    if (every > 0 && (h->fp16_autoscale_count += (int)m) >= every) {
+      h->fp16_autoscale_count = 0;
+      if (int rc = fp16_rescan(h, h->fp16_autoscale_target, false, nullptr)) return rc;
     }
   }
-  h->host_step += n;
   return FDTD_OK;
 }
 
@@ -699,7 +843,8 @@ int fdtd_copy_field_to_host(fdtd_handle* h, int comp, double* host, size_t n) {
     std::memset(host, 0, sizeof(double) * n);
     return FDTD_OK;
   }
-  StateView v = h->view();
+  StateView v;
+  if (int rc = read_view(h, &v)) return rc;
   if (comp < FDTD_JX) {
     if (double* dev = device_alias(host)) {
       // pinned host memory the device addresses: convert in one pass
@@ -737,7 +882,9 @@ int fdtd_export_field(fdtd_handle* h, int comp, int64_t offset, int64_t count, d
   if (!device_dst || offset < 0 || count < 0 || offset + count > h->g.cells)
     return fail(FDTD_ERR_INVALID_ARGUMENT, "export range outside the grid");
   DeviceGuard dg(h->device);
-  FDTD_CUDA(launch_export(h->view(), comp, device_dst, offset, count, h->stream), "export field");
+  StateView v;
+  if (int rc = read_view(h, &v)) return rc;
+  FDTD_CUDA(launch_export(v, comp, device_dst, offset, count, h->stream), "export field");
   return FDTD_OK;
 }
 
@@ -746,6 +893,8 @@ int fdtd_copy_field_from_host(fdtd_handle* h, int comp, const double* host, size
   if (comp < FDTD_EX || comp > FDTD_JZ) return fail(FDTD_ERR_LOGIC, "ERROR: Invalid field component");
   if (!host || (int64_t)n != h->g.cells) return fail(FDTD_ERR_INVALID_ARGUMENT, "host buffer size mismatch");
   DeviceGuard dg(h->device);
+  if (comp < FDTD_JX)
+    if (int rc = resolve_pending(h)) return rc;  // the pending half reads the E and B being replaced
   if (h->form == Form::F64) {
     FDTD_CUDA(cudaMemcpyAsync(h->field[comp], host, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream),
               "copy field from host");
@@ -943,6 +1092,7 @@ int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out) 
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    h->b_side = false;  // the timed sweeps wrote the second copy
     if (rc != FDTD_OK) return rc;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune_cache[key] = best;
@@ -963,7 +1113,9 @@ int fdtd_field_sums(fdtd_handle* h, double out[FDTD_DIAG_COUNT]) {
   if (!out) return fail(FDTD_ERR_INVALID_ARGUMENT, "null output pointer");
   DeviceGuard dg(h->device);
   const int nb = diag_blocks_for(h->g.cells, kMaxDiagBlocks);
-  FDTD_CUDA(launch_field_sums(h->view(), h->d_partials, nb, h->d_diag_out, h->stream), "field sums");
+  StateView v;
+  if (int rc = read_view(h, &v)) return rc;
+  FDTD_CUDA(launch_field_sums(v, h->d_partials, nb, h->d_diag_out, h->stream), "field sums");
   FDTD_CUDA(cudaMemcpyAsync(out, h->d_diag_out, sizeof(double) * kDiagValues, cudaMemcpyDeviceToHost,
                             h->stream),
             "field sums readback");
@@ -995,8 +1147,48 @@ int fdtd_synchronize(fdtd_handle* h) {
   FDTD_CUDA(cudaMemcpy(&status, h->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read device status");
   if (status != 0) {
     cudaMemset(h->d_err, 0, sizeof(int));
-    return fail(FDTD_ERR_TIMEOUT, "a bounded wait in a step kernel gave up; results of that step are invalid");
+    return fail(FDTD_ERR_TIMEOUT, (status & 2) ? "a bounded wait in a step kernel gave up, and so did the wait for its "
+                                                 "copies in flight; results of that step are invalid"
+                                               : "a bounded wait in a step kernel gave up; results of that step are "
+                                                 "invalid");
   }
+  return FDTD_OK;
+}
+
+int fdtd_fp16_autoscale(fdtd_handle* h, int target_log2, int exponents[6]) {
+  if (int rc = check_handle(h)) return rc;
+  if (h->form != Form::F16) return fail(FDTD_ERR_UNSUPPORTED, "scales apply to the FP16_SCALED form only");
+  if (target_log2 < 0 || target_log2 > 15) return fail(FDTD_ERR_INVALID_ARGUMENT, "target_log2 must be in [0, 15]");
+  DeviceGuard dg(h->device);
+  if (int rc = fp16_rescan(h, target_log2, true, exponents)) return rc;
+  FDTD_CUDA(cudaStreamSynchronize(h->stream), "FP16 rescale");
+  return FDTD_OK;
+}
+
+int fdtd_set_fp16_autoscale(fdtd_handle* h, int every_steps, int target_log2) {
+  if (int rc = check_handle(h)) return rc;
+  if (h->form != Form::F16) return fail(FDTD_ERR_UNSUPPORTED, "scales apply to the FP16_SCALED form only");
+  if (every_steps < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "every_steps must be >= 0");
+  if (target_log2 < 0 || target_log2 > 15) return fail(FDTD_ERR_INVALID_ARGUMENT, "target_log2 must be in [0, 15]");
+  h->fp16_autoscale_every = every_steps;
+  h->fp16_autoscale_target = target_log2;
+  h->fp16_autoscale_count = 0;
+  return FDTD_OK;
+}
+
+int fdtd_get_fp16_exponents(fdtd_handle* h, int exponents[6]) {
+  if (int rc = check_handle(h)) return rc;
+  if (!exponents) return fail(FDTD_ERR_INVALID_ARGUMENT, "null exponents");
+  for (int c = 0; c < 6; ++c) exponents[c] = h->fp16_exp[c];
+  return FDTD_OK;
+}
+
+int fdtd_set_wait_limit(fdtd_handle* h, int64_t polls, int withhold_loads) {
+  if (int rc = check_handle(h)) return rc;
+  if (polls < 0 || polls > (int64_t)kMaxBarrierPolls)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "polls must be in [0, 2^24] (0: the default)");
+  h->wait_polls = polls ? (uint32_t)polls : kMaxBarrierPolls;
+  h->withhold_loads = withhold_loads ? 1 : 0;
   return FDTD_OK;
 }
 
@@ -1018,6 +1210,7 @@ int fdtd_set_fp16_exponents(fdtd_handle* h, const int exponents[6]) {
     if (exponents[c] < -60 || exponents[c] > 60) return fail(FDTD_ERR_INVALID_ARGUMENT, "exponent out of range [-60, 60]");
   // Rescale stored values so the fields they represent are unchanged.
   DeviceGuard dg(h->device);
+  if (int rc = resolve_pending(h)) return rc;
   if (int rc = ensure_staging(h)) return rc;
   for (int c = 0; c < 6; ++c) {
     if (exponents[c] == h->fp16_exp[c]) continue;
@@ -1127,14 +1320,29 @@ int fdtd_slab_info(fdtd_handle* h, int* k_begin, int* k_end, int* nk_global) {
 int fdtd_slab_sweep(fdtd_handle* h, int sweep) {
   if (int rc = check_handle(h)) return rc;
   if (h->pml) return fail(FDTD_ERR_UNSUPPORTED, "the PML form steps through fdtd_step");
-  if (sweep < FDTD_SWEEP_B_HALF || sweep > FDTD_SWEEP_E) return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid sweep");
+  if (sweep < FDTD_SWEEP_B_HALF || sweep > FDTD_SWEEP_B_DEFER) return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid sweep");
   DeviceGuard dg(h->device);
-  if (sweep == FDTD_SWEEP_E) {
-    if (int rc = run_e(h, h->host_step)) return rc;
-    ++h->host_step;
-    return FDTD_OK;
+  switch (sweep) {
+    case FDTD_SWEEP_E:
+      if (int rc = resolve_pending(h)) return rc;
+      if (int rc = run_e(h, h->host_step)) return rc;
+      ++h->host_step;
+      return FDTD_OK;
+    case FDTD_SWEEP_B_DEFER:
+      // the FP64 form hands out its storage (fdtd_get_field): nothing may be
+      // left pending there
+      if (h->form == Form::F64) return fail(FDTD_ERR_UNSUPPORTED, "the FP64 form applies every half step");
+      if (h->b_pending) return fail(FDTD_ERR_LOGIC, "a B half step is already pending");
+      h->b_pending = true;
+      h->b_side = false;
+      return FDTD_OK;
+    default:
+      // with a half step pending, it is the first of the half steps applied
+      if (int rc = run_b(h, sweep == FDTD_SWEEP_B_DOUBLE ? 2 : 1)) return rc;
+      h->b_pending = false;
+      h->b_side = false;
+      return FDTD_OK;
   }
-  return run_b(h, sweep == FDTD_SWEEP_B_DOUBLE ? 2 : 1);
 }
 
 }  // extern "C"
@@ -1169,6 +1377,12 @@ int fdtd_slab_plane(fdtd_handle* h, int comp, int plane, int part, void** device
     return fail(FDTD_ERR_INVALID_ARGUMENT, "only a z slab has halo planes");
   if (part != 0 && !(part == 1 && h->form == Form::F32C))
     return fail(FDTD_ERR_INVALID_ARGUMENT, "part 1 (compensation words) exists in the FP32_COMP form only");
+  if (comp >= FDTD_BX) {
+    // the caller addresses stored B planes: they must hold the whole step (E
+    // planes do not depend on a pending half step)
+    DeviceGuard dg(h->device);
+    if (int rc = resolve_pending(h)) return rc;
+  }
   *device_ptr = slab_plane(h, comp, plane, part, bytes);
   return FDTD_OK;
 }

@@ -10,6 +10,7 @@
 #include "common.cuh"
 #include "layout.cuh"
 #include "storage.cuh"
+#include "tma.cuh"
 
 namespace fdtd {
 
@@ -102,6 +103,11 @@ cudaError_t launch_b_pml_fp64(const Grid& g, const Box& box, const Fp64Fields& F
 template <class S>
 cudaError_t launch_b_f32(const PLayout& L, const S& st, const CoefSet& cs, int applications, int kbeg, int kend,
                          cudaStream_t stream);
+// One B half step of planes [kbeg, kend) from the state `st` (E and B) into
+// the B arrays of `out`, which must not alias st's.
+template <class S>
+cudaError_t launch_b_f32_into(const PLayout& L, const S& st, const S& out, const CoefSet& cs, int kbeg, int kend,
+                              cudaStream_t stream);
 template <class S>
 cudaError_t launch_e_f32(const PLayout& L, const S& st, const float* const J[3], bool dense_j,
                          const CoefSet& cs, const SourceSet& ss, int64_t step, int kbeg, int kend,
@@ -112,17 +118,19 @@ template <class S>
 cudaError_t launch_fused_f32(const PLayout& L, const S& st, const S& out, const void* maps,
                              const float* const J[3], bool dense_j, const CoefSet& cs,
                              const SourceSet& ss, int64_t step, int applications,
-                             const FusedConfig& cfg, int* err, cudaStream_t stream);
+                             const FusedConfig& cfg, const WaitCtl& wc, cudaStream_t stream);
 template <class S>
 int fused_box_width();
 int fused_lo_box_width();
 // kernels_fused1.cu: the same sweep with one cell per thread (32-wide tiles);
-// `maps` is a StepMaps: load maps of `st`'s arrays, store maps of `out`'s.
+// `maps` is a StepMaps: load maps of `st`'s arrays (built with the trim of
+// the sweep order), store maps of `out`'s.  b_first: the B-first sweep (B
+// half steps, then E), otherwise the E-first one (E, then B half steps).
 template <class S>
 cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const void* maps,
                               const float* const J[3], bool dense_j, const CoefSet& cs,
                               const SourceSet& ss, int64_t step, int applications,
-                              const FusedConfig& cfg, int* err, cudaStream_t stream);
+                              const FusedConfig& cfg, bool b_first, const WaitCtl& wc, cudaStream_t stream);
 template <class S>
 int fused1_box_width();
 int fused1_lo_box_width();
@@ -147,7 +155,7 @@ struct BatchDomain {
 template <class S>
 cudaError_t launch_fused1_batch(const void* doms, const StepMaps* maps, const int4* tiles, int n_tiles, int parity,
                                 int applications, const FusedConfig& cfg, const int64_t* step_base, int step_off,
-                                int* counters, int* err, cudaStream_t stream);
+                                int* counters, const WaitCtl& wc, cudaStream_t stream);
 
 // kernels_f32.cu: the leading B half step of every domain in place on copy
 // `parity`, as one launch of 32 x 8 blocks marching kBatchBChunk planes;
@@ -164,10 +172,14 @@ enum class HiType { F32, F16 };
 // margins (x coordinate kPadX + x is cell x), box 32 x tile_y.
 cudaError_t build_tma_store_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], LoT* const lo[6],
                                  int tile_y);
-// trimmed (the one-cell-per-thread kernel): boxes of components other than
-// Bx and Bz are one row shorter (they start at the tile's first row).
+// Box heights of the load maps: None (the two-cell kernel) gives every
+// component tile_y + 2 rows; the one-cell kernel's E-first sweep gives Bx and
+// Bz tile_y + 2 rows (the rows below and above the tile) and the others
+// tile_y + 1 (the row above); its B-first sweep gives Ex and Ez tile_y + 2
+// and the others tile_y + 1 (the row below).
+enum class BoxTrim { None, EFirst, BFirst };
 cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6],
-                           LoT* const lo[6], int box_w, int lo_box_w, int tile_y, bool trimmed);
+                           LoT* const lo[6], int box_w, int lo_box_w, int tile_y, BoxTrim trim);
 
 // misc.cu — conversions, diagnostics, small helpers.
 enum class Form { F64 = 0, F32 = 1, F32C = 2, F16 = 3 };
@@ -189,6 +201,11 @@ cudaError_t launch_import(const StateView& v, int c, const double* src, int64_t 
 // Reads component c (0..5) of the state as FP64 into `dst` (logical cells).
 cudaError_t launch_export(const StateView& v, int c, double* dst, int64_t off, int64_t n,
                           cudaStream_t st);
+// Largest |stored value| of each FP16 component (grid cells), as FP32 bit
+// patterns in out_dev[6] (device memory; zeroed here first).
+cudaError_t launch_f16_absmax(const PLayout& L, const StoreF16& st, unsigned* out_dev, cudaStream_t stream);
+// Multiplies n stored FP16 words (n even) by 2^shift, in place.
+cudaError_t launch_f16_rescale(__half* v, int64_t n, int shift, cudaStream_t stream);
 // FP64 -> FP32 conversion of n values.
 cudaError_t launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
 // FP64 -> FP32 hi + FP32 lo (hi + lo carries the FP64 value to ~2^-48).

@@ -63,6 +63,11 @@ struct fdtd_handle {
   bool dense_j = false;  // the E update reads the dense J arrays
   bool fp64_fma = false;  // FP64 form: contracted arithmetic (fdtd_set_fp64_arith)
   int fp16_exp[6] = {0, 0, 0, 0, 0, 0};
+  // FP16 range checks (fdtd_set_fp16_autoscale): every n steps (0: off) the
+  // stored peaks are scanned and components re-encoded around 2^target.
+  int fp16_autoscale_every = 0;
+  int fp16_autoscale_target = 12;
+  int fp16_autoscale_count = 0;  // steps since the last check
 
   // Sources.
   std::vector<HostSource> sources;
@@ -119,8 +124,29 @@ struct fdtd_handle {
   // fused kernel.
   TmaMaps smaps_cur;
   TmaMaps smaps_alt;
+  // Load maps of the B-first sweep (its boxes hold other halo rows).
+  TmaMaps bmaps_cur;
+  TmaMaps bmaps_alt;
   int maps_tile_y = 0;
   int* d_err = nullptr;  // device status word (bounded waits that gave up)
+  // Bounded waits of the fused sweeps: polls before a wait gives up, and the
+  // test hook that issues no tile loads (fdtd_set_wait_limit).
+  uint32_t wait_polls = kMaxBarrierPolls;
+  int withhold_loads = 0;
+  WaitCtl wait_ctl() const { return WaitCtl{d_err, wait_polls, withhold_loads}; }
+
+  // Pending B half step (FP32-arithmetic forms, B-first fused sweeps): the
+  // stored B lacks the trailing half step of the last update_fields; the next
+  // step applies it together with its leading half (one sweep), and every
+  // reader of B sees it applied (read_view).  b_side: the second copy's B
+  // arrays hold the stored B with the pending half applied (valid until the
+  // next sweep writes that copy).
+  bool b_pending = false;
+  bool b_side = false;
+  // A z slab has no second copy: its side B arrays (allocated on first use,
+  // halo planes included) take the pending half for readers.
+  void* side_b[3] = {nullptr, nullptr, nullptr};
+  LoT* side_lo[3] = {nullptr, nullptr, nullptr};
 
   // Scratch.
   double* d_staging = nullptr;
@@ -166,9 +192,18 @@ struct fdtd_handle {
   }
   StateView view() const { return make_view(field, lo); }
   StateView view_alt() const { return make_view(alt_field, alt_lo); }
+  // E from the current copy, B from the second copy (a z slab: its side
+  // arrays) with the pending half applied.
+  StateView view_side() const {
+    void* const* sb = zhalo ? side_b : alt_field + 3;
+    LoT* const* sl = zhalo ? side_lo : alt_lo + 3;
+    void* f[6] = {field[0], field[1], field[2], sb[0], sb[1], sb[2]};
+    LoT* l[6] = {lo[0], lo[1], lo[2], sl[0], sl[1], sl[2]};
+    return make_view(f, l);
+  }
   // The storage the sweeps index: the owned planes and the halo planes.
-  StateView sweep_view() const {
-    StateView v = view();
+  StateView sweep_view() const { return with_halo(view()); }
+  StateView with_halo(StateView v) const {
     if (zhalo == 0) return v;
     v.g.Nk += 2 * zhalo;
     v.g.cells = v.g.plane * v.g.Nk;
@@ -201,4 +236,10 @@ namespace fdtd {
 int ensure_alt(fdtd_handle* h);
 // Swaps the current and the second copy (after a fused sweep).
 void swap_copies(fdtd_handle* h);
+// The state as readers see it: the stored state, or with a pending B half
+// step applied (computed into the second copy's B arrays on first use).
+int read_view(fdtd_handle* h, StateView* v);
+// Applies a pending B half step to the stored state (before anything writes
+// E or B, or runs a sweep that expects B at the step boundary).
+int resolve_pending(fdtd_handle* h);
 }  // namespace fdtd

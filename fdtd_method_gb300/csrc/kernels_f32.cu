@@ -14,10 +14,11 @@
 
 namespace fdtd {
 
-// B update of column (i, j), planes k0 .. min(k0+kchunk, kend)-1.
+// B update of column (i, j), planes k0 .. min(k0+kchunk, kend)-1: reads E
+// and B from `st`, writes B to `out` (the same storage for the in-place sweeps).
 template <class S, class A, int kApplications>
-__device__ __forceinline__ void b_column(const PLayout& L, const S& st, const CoefSet& cs, int i, int j, int k0,
-                                         int kchunk, int kend) {
+__device__ __forceinline__ void b_column(const PLayout& L, const S& st, const S& out, const CoefSet& cs, int i, int j,
+                                         int k0, int kchunk, int kend) {
   if (i >= L.Ni || j >= L.Nj || k0 >= kend) return;
   const int k1 = min(k0 + kchunk, kend);
   const int64_t col = L.at(i, j, 0), col_in = L.at(i + 1, j, 0), col_jn = L.at(i, j + 1, 0);
@@ -38,17 +39,17 @@ __device__ __forceinline__ void b_column(const PLayout& L, const S& st, const Co
       ty = A::twice(ty);
       tz = A::twice(tz);
     }
-    store_with_ghosts(st, L, 3, i, j, k, A::acc(st.load(3, col + base), tx));
-    store_with_ghosts(st, L, 4, i, j, k, A::acc(st.load(4, col + base), ty));
-    store_with_ghosts(st, L, 5, i, j, k, A::acc(st.load(5, col + base), tz));
+    store_with_ghosts(out, L, 3, i, j, k, A::acc(st.load(3, col + base), tx));
+    store_with_ghosts(out, L, 4, i, j, k, A::acc(st.load(4, col + base), ty));
+    store_with_ghosts(out, L, 5, i, j, k, A::acc(st.load(5, col + base), tz));
     ex = ex_kn;
     ey = ey_kn;
   }
 }
 
 template <class S, class A, int kApplications>
-__global__ void __launch_bounds__(256) b_sweep(PLayout L, S st, CoefSet cs, int kchunk, int kbeg, int kend) {
-  b_column<S, A, kApplications>(L, st, cs, blockIdx.x * blockDim.x + threadIdx.x,
+__global__ void __launch_bounds__(256) b_sweep(PLayout L, S st, S out, CoefSet cs, int kchunk, int kbeg, int kend) {
+  b_column<S, A, kApplications>(L, st, out, cs, blockIdx.x * blockDim.x + threadIdx.x,
                                 blockIdx.y * blockDim.y + threadIdx.y, kbeg + blockIdx.z * kchunk, kchunk, kend);
 }
 
@@ -68,8 +69,8 @@ __global__ void __launch_bounds__(256) b_sweep_batch(const BatchDomain<S>* __res
   const int64_t local = b - block_start[lo];
   const int nbx = (d.L.Ni + 31) / 32, nby = (d.L.Nj + 7) / 8;
   const int bx = (int)(local % nbx), by = (int)((local / nbx) % nby), bz = (int)(local / ((int64_t)nbx * nby));
-  b_column<S, A, 1>(d.L, d.s[parity], d.cs, bx * 32 + threadIdx.x, by * 8 + threadIdx.y, bz * kBatchBChunk,
-                    kBatchBChunk, d.L.Nk);
+  b_column<S, A, 1>(d.L, d.s[parity], d.s[parity], d.cs, bx * 32 + threadIdx.x, by * 8 + threadIdx.y,
+                    bz * kBatchBChunk, kBatchBChunk, d.L.Nk);
 }
 
 template <class S, class A, bool kDenseJ, bool kSources>
@@ -137,8 +138,20 @@ cudaError_t launch_b_f32(const PLayout& L, const S& st, const CoefSet& cs, int a
   if (kend <= kbeg) return cudaSuccess;
   const int kchunk = 16;
   dim3 block(32, 8), grid = sweep_grid(L, kbeg, kend, kchunk);
-  if (applications == 2) b_sweep<S, A, 2><<<grid, block, 0, stream>>>(L, st, cs, kchunk, kbeg, kend);
-  else b_sweep<S, A, 1><<<grid, block, 0, stream>>>(L, st, cs, kchunk, kbeg, kend);
+  if (applications == 2) b_sweep<S, A, 2><<<grid, block, 0, stream>>>(L, st, st, cs, kchunk, kbeg, kend);
+  else b_sweep<S, A, 1><<<grid, block, 0, stream>>>(L, st, st, cs, kchunk, kbeg, kend);
+  return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t launch_b_f32_into(const PLayout& L, const S& st, const S& out, const CoefSet& cs, int kbeg, int kend,
+                              cudaStream_t stream) {
+  using A = typename ArithOf<S>::type;
+  if (kbeg < 0 || kend > L.Nk) return cudaErrorInvalidValue;
+  if (kend <= kbeg) return cudaSuccess;
+  const int kchunk = 16;
+  dim3 block(32, 8), grid = sweep_grid(L, kbeg, kend, kchunk);
+  b_sweep<S, A, 1><<<grid, block, 0, stream>>>(L, st, out, cs, kchunk, kbeg, kend);
   return cudaGetLastError();
 }
 
@@ -175,6 +188,8 @@ cudaError_t launch_b_f32_batch(const void* doms, const int64_t* block_start, int
 
 #define FDTD_INSTANTIATE(S)                                                                            \
   template cudaError_t launch_b_f32<S>(const PLayout&, const S&, const CoefSet&, int, int, int, cudaStream_t); \
+  template cudaError_t launch_b_f32_into<S>(const PLayout&, const S&, const S&, const CoefSet&, int, int,      \
+                                            cudaStream_t);                                                    \
   template cudaError_t launch_b_f32_batch<S>(const void*, const int64_t*, int, int64_t, int, cudaStream_t); \
   template cudaError_t launch_e_f32<S>(const PLayout&, const S&, const float* const[3], bool,         \
                                        const CoefSet&, const SourceSet&, int64_t, int, int, cudaStream_t);

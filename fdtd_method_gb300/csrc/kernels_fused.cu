@@ -101,7 +101,7 @@ template <class S, class A, int RY, int kApps, bool kDenseJ, int kSrc>
 __global__ void __launch_bounds__(32 * (RY + 2))
     fused2(PLayout L, S st, S out, const __grid_constant__ TmaMaps maps, CoefSet cs, int kchunk,
            const float* __restrict__ Jx, const float* __restrict__ Jy, const float* __restrict__ Jz,
-           SourceSet ss, int64_t step, int* err) {
+           SourceSet ss, int64_t step, WaitCtl wc) {
   using SP = SmemPlan<S, RY>;
   using C2 = Codec2<S>;
   using A2 = Arith2<A>;
@@ -133,7 +133,10 @@ __global__ void __launch_bounds__(32 * (RY + 2))
   const int k1 = min(k0 + kchunk, L.Nk);
   const bool producer = (w == 0 && lane == 0);
 
+  int issued = 0;  // fills issued (the producer's count)
   auto issue = [&](int t) {
+    if (wc.withhold) return;
+    ++issued;
     const int slot = (t - k0) % kStages;
     const int kk = (t == L.Nk) ? 0 : t;
     unsigned char* base = smem + slot * SP::kStageBytes;
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(32 * (RY + 2))
   for (int t = k0; t <= k1; ++t) {
     const int slot = (t - k0) % kStages;
     const int cur = t & 1;
-    mbar_wait_bounded(&bar[slot], ((t - k0) / kStages) & 1, err);
+    const bool timed_out = !mbar_wait_bounded(&bar[slot], ((t - k0) / kStages) & 1, wc);
     const HiT* H = reinterpret_cast<const HiT*>(smem + slot * SP::kStageBytes);
     const LoT* Lo = reinterpret_cast<const LoT*>(smem + slot * SP::kStageBytes + SP::kHiBytes);
     auto ld2 = [&](int c, int row, int col) -> P2 {  // cells col, col+1 (col even)
@@ -307,7 +310,13 @@ __global__ void __launch_bounds__(32 * (RY + 2))
     pex = nex;
     pey = ney;
     pez = nez;
-    __syncthreads();
+    if (__syncthreads_or(timed_out)) {
+      // a wait gave up: stop, after the producer has waited (bounded) for the
+      // fills still in flight
+      if (producer)
+        for (int f = t - k0; f < issued; ++f) mbar_wait_bounded(&bar[f % kStages], (f / kStages) & 1, wc, 2);
+      return;
+    }
     if (producer && t + kStages <= k1) issue(t + kStages);
   }
 }
@@ -315,25 +324,25 @@ __global__ void __launch_bounds__(32 * (RY + 2))
 template <class S, int RY, int APPS, bool DJ, int SRC>
 cudaError_t launch_one(dim3 grid, const PLayout& L, const S& st, const S& out, const TmaMaps& maps,
                        const CoefSet& cs, int kchunk, const float* const J[3], const SourceSet& ss,
-                       int64_t step, int* err, cudaStream_t stream) {
+                       int64_t step, const WaitCtl& wc, cudaStream_t stream) {
   using A = typename ArithFor<S>::type;
   auto kern = fused2<S, A, RY, APPS, DJ, SRC>;
   const int bytes = SmemPlan<S, RY>::kTotal;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
   kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(L, st, out, maps, cs, kchunk, J[0], J[1], J[2], ss, step,
-                                                  err);
+                                                  wc);
   return cudaGetLastError();
 }
 
 template <class S, int RY>
 cudaError_t launch_ry(const PLayout& L, const S& st, const S& out, const TmaMaps& maps,
                       const float* const J[3], bool dense_j, const CoefSet& cs, const SourceSet& ss,
-                      int64_t step, int applications, int kchunk, int* err, cudaStream_t stream) {
+                      int64_t step, int applications, int kchunk, const WaitCtl& wc, cudaStream_t stream) {
   dim3 grid((L.Ni + kTileX - 1) / kTileX, (L.Nj + RY - 1) / RY, (L.Nk + kchunk - 1) / kchunk);
   const int src = ss.count == 0 ? 0 : (ss.count <= kFastSources ? 1 : 2);
 #define FDTD_F(APPS, DJ, SRC) \
-  return launch_one<S, RY, APPS, DJ, SRC>(grid, L, st, out, maps, cs, kchunk, J, ss, step, err, stream)
+  return launch_one<S, RY, APPS, DJ, SRC>(grid, L, st, out, maps, cs, kchunk, J, ss, step, wc, stream)
 #define FDTD_FS(APPS, DJ)            \
   if (src == 0) FDTD_F(APPS, DJ, 0); \
   if (src == 1) FDTD_F(APPS, DJ, 1); \
@@ -353,12 +362,12 @@ template <class S>
 cudaError_t launch_fused_f32(const PLayout& L, const S& st, const S& out, const void* maps,
                              const float* const J[3], bool dense_j, const CoefSet& cs,
                              const SourceSet& ss, int64_t step, int applications,
-                             const FusedConfig& cfg, int* err, cudaStream_t stream) {
+                             const FusedConfig& cfg, const WaitCtl& wc, cudaStream_t stream) {
   const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 32;
   const TmaMaps& m = *static_cast<const TmaMaps*>(maps);
   if (cfg.tile_y == 6)
-    return launch_ry<S, 6>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
-  return launch_ry<S, 14>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
+    return launch_ry<S, 6>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, wc, stream);
+  return launch_ry<S, 14>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, wc, stream);
 }
 
 template <class S>
@@ -368,7 +377,8 @@ int fused_lo_box_width() { return BoxOf<StoreF32C>::kLoW; }
 #define FDTD_INSTANTIATE(S)                                                                          \
   template cudaError_t launch_fused_f32<S>(const PLayout&, const S&, const S&, const void*,         \
                                            const float* const[3], bool, const CoefSet&,             \
-                                           const SourceSet&, int64_t, int, const FusedConfig&, int*, \
+                                           const SourceSet&, int64_t, int, const FusedConfig&,      \
+                                           const WaitCtl&,                                          \
                                            cudaStream_t);                                           \
   template int fused_box_width<S>();
 FDTD_INSTANTIATE(StoreF32)

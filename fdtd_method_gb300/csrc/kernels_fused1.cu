@@ -1,38 +1,59 @@
-// Fused step kernel, one cell per thread: the default step of the
-// FP32-arithmetic forms.  One sweep advances one update_fields step (the E
-// step and the B half steps around it); the arithmetic is that of the split
-// sweeps (kernels_f32.cu, the reference's functors kokkos_functors.h:64-90 E
-// and :128-151 B), reproduced bit for bit.
+// Fused step kernels, one cell per thread: the default step of the
+// FP32-arithmetic forms.  One sweep advances one update_fields step; the
+// arithmetic is that of the split sweeps (kernels_f32.cu, the reference's
+// functors kokkos_functors.h:64-90 E and :128-151 B), reproduced bit for bit.
+// A sweep comes in two orders:
+//
+//   E-first (fused1)    E step, then `apps` B half steps (the trailing half of
+//                       this step, and with apps = 2 the leading half of the
+//                       next), marching z upward.  A run of n steps is a
+//                       leading B half sweep and n of these.
+//   B-first (fused1b)   `apps` B half steps (the trailing half of the
+//                       previous step, which was left pending, and the leading
+//                       half of this one), then the E step, marching z
+//                       downward.  A run of n steps is n of these with the
+//                       last trailing half left pending; every reader of B
+//                       applies it (engine.cu), so n update_fields calls cost
+//                       n sweeps.
+//
+// Both orders add the same terms in the same order, so they agree bit for bit
+// with each other and with the split sweeps.
 //
 // A CTA owns a tile of 32 x RY cells at (x0, y0) (RY = 6, 14 or 30) and
-// marches the planes k0..k1 of its z chunk.  Warps 0..RY are the box rows
-// 1..RY+1 (the last computes E' only, for the B update of the row below it);
-// warp RY+1 computes E' on the x halo column for rows 1..RY.
+// marches the planes of its z chunk.  Warps 0..RY-1 are the tile rows; warps
+// RY and RY+1 compute the first half-sweep's field on the tile's halo row and
+// halo column (E-first: E' on the row above and the column right of the tile,
+// which the B update reads at j+1 and i+1; B-first: B' on the row below and
+// the column left of it, which the E update reads at j-1 and i-1).
 //
 // Data movement, per plane:
 //   in   one 3-D TMA box per stored array (hi words: columns x0-4 .. x0+35,
-//        BF16 lo and FP16 words: x0-8 .. x0+39; rows y0-1 .. y0+RY), NS
-//        planes ahead through an mbarrier ring;
-//   out  E'(t) and B'(t-1) are written to shared staging boxes of 32 x RY in
-//        their stored encoding; one thread stores them with TMA through
+//        BF16 lo and FP16 words: x0-8 .. x0+39; each component's rows are the
+//        ones its stencil reads), NS planes ahead through an mbarrier ring;
+//   out  both updated fields are written to shared staging boxes of 32 x RY
+//        in their stored encoding; one thread stores them with TMA through
 //        tensor maps of the grid rows (the copy engine clips rows past the
 //        grid; a tile narrower than 32 columns stores with plain stores).
 //        The first and last tile columns store the same boxes into the x
 //        margins as well, which fills the ghost columns with bulk copies
 //        where the alignment allows; the remaining ghost copies (ghost
 //        rows, corners, unaligned columns) are plain stores.
-// The E' staging box doubles as the exchange plane from which the next
-// iteration reads E'(t-1) at i+1 and j+1; it has two extra rows, holding the
-// halo row's and the halo column's E'.
+// The first half-sweep's staging box doubles as the exchange plane from which
+// the next iteration reads that field at the tile's neighbouring cells; it
+// has two extra rows, holding the halo row's and the halo column's values.
 //
-// In iteration t every thread
-//   1. computes E'(t) = E + c curl B of its cell (B at i-1, j-1 from the box,
+// E-first, iteration t (planes k0 .. k1):
+//   1. E'(t) = E + c curl B of the thread's cell (B at i-1, j-1 from the box,
 //      B(t-1) carried in registers);
-//   2. on interior cells (t > k0), computes B'(t-1) = B(t-1) + apps (c/2) curl E'
-//      (E'(t-1) at i+1, j+1 from the exchange plane, E'(t) in registers);
-//   3. writes both to staging, and the CTA synchronises once; lane 0 of the
-//      halo-column warp then stores the staged boxes and refills the freed
-//      ring slot.
+//   2. on interior cells (t > k0), B'(t-1) = B(t-1) + apps (c/2) curl E'
+//      (E'(t-1) at i+1, j+1 from the exchange plane, E'(t) in registers).
+// B-first, iteration t (planes k1-1 down to k0-1):
+//   1. B'(t) = B + apps (c/2) curl E of the thread's cell (E at i+1, j+1 from
+//      the box, E(t+1) carried in registers);
+//   2. on interior cells (t < k1-1), E'(t+1) = E(t+1) + c curl B' + J
+//      (B'(t+1) at i-1, j-1 from the exchange plane, B'(t) in registers).
+// Each iteration ends with one CTA barrier; lane 0 of the halo-column warp
+// then stores the staged boxes and refills the freed ring slot.
 // The sweep reads the state from `st` and writes the new state to `out`:
 // neighbouring tiles read what a tile writes, so an in-place update would race.
 #include "arith.cuh"
@@ -86,16 +107,26 @@ struct BoxTable {
   int stage;           // stage size, 128-byte multiple
 };
 
-constexpr BoxTable box_table(int RY, int W, int LW, int HS, int LS, bool lo, int off, int lo_off) {
+constexpr BoxTable box_table(int RY, int W, int LW, int HS, int LS, bool lo, int off, int lo_off, bool bfirst) {
   BoxTable b{};
   int at = 0;
   unsigned tx = 0;
   for (int c = 0; c < 6; ++c) {
-    const bool below = (c == 3 || c == 5), left = (c == 4 || c == 5);
-    b.rows[c] = below ? RY + 2 : RY + 1;
-    b.row0[c] = below ? 0 : 1;
-    b.xoff[c] = left ? off : 0;
-    b.lxoff[c] = left ? lo_off : 0;
+    if (bfirst) {
+      // every box starts at the row below and the column left of the tile
+      // (the halo warps' cells); Ex and Ez also hold the row above (B'z and
+      // B'x read them at j+1).  Box row 0 is y0-1.
+      b.rows[c] = (c == 0 || c == 2) ? RY + 2 : RY + 1;
+      b.row0[c] = 0;
+      b.xoff[c] = off;
+      b.lxoff[c] = lo_off;
+    } else {
+      const bool below = (c == 3 || c == 5), left = (c == 4 || c == 5);
+      b.rows[c] = below ? RY + 2 : RY + 1;
+      b.row0[c] = below ? 0 : 1;
+      b.xoff[c] = left ? off : 0;
+      b.lxoff[c] = left ? lo_off : 0;
+    }
   }
   for (int c = 0; c < 6; ++c) {
     b.hi[c] = at;
@@ -116,8 +147,9 @@ constexpr BoxTable box_table(int RY, int W, int LW, int HS, int LS, bool lo, int
   return b;
 }
 
-// Shared-memory plan (byte offsets).
-template <class S, int RY>
+// Shared-memory plan (byte offsets) of the E-first (BF false) or B-first
+// (BF true) sweep.
+template <class S, int RY, bool BF = false>
 struct Plan1 {
   using HiT = typename S::HiT;
   static constexpr bool kLo = S::kComp;
@@ -125,30 +157,32 @@ struct Plan1 {
   static constexpr int W = Box1<S>::kW, LW = Box1<S>::kLoW, OFF = Box1<S>::kOff;
   static constexpr int HS = (int)sizeof(HiT), LS = (int)sizeof(LoT);
   // Ring stage: 6 hi boxes, then 6 lo boxes.  Each component's box holds
-  // only the halos its stencil reads: the column left of the tile for By and
-  // Bz (E update, i-1), the row below for Bx and Bz (E update, j-1); every
-  // box holds the column right of the tile and the row above, where the
-  // halo warps compute E'.  Box row 0 is y0-1 for Bx, Bz and y0 otherwise
-  // (box row of thread row r: r - row0).  Every box starts on a 128-byte
-  // boundary, as tensor copies require.
+  // only the halos its stencil reads.  E-first: the column left of the tile
+  // for By and Bz (E update, i-1), the row below for Bx and Bz (E update,
+  // j-1); every box holds the column right of the tile and the row above,
+  // where the halo warps compute E'.  Box row 0 is y0-1 for Bx, Bz and y0
+  // otherwise (box row of thread row r: r - row0).  B-first: see box_table.
+  // Every box starts on a 128-byte boundary, as tensor copies require.
   // Per-component scalars of the table (device code may use scalar
   // constants, not the table object).
-  static constexpr BoxTable box() { return box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1); }
-  template <int c> static constexpr int kHiAt = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).hi[c];
-  template <int c> static constexpr int kLoAt = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).lo[c];
-  template <int c> static constexpr int kRow0 = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).row0[c];
-  template <int c> static constexpr int kXOff = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).xoff[c];
-  template <int c> static constexpr int kLXOff = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).lxoff[c];
-  static constexpr uint32_t kTx = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).tx;
-  static constexpr int kStage = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1).stage;
-  // E' exchange / staging buffer: per component RY+2 rows of 32 (rows 0..RY-1
-  // the tile, row RY the halo row, row RY+1 the halo column by row), hi words
-  // then lo words.
+  static constexpr BoxTable box() { return box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF); }
+  template <int c> static constexpr int kHiAt = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).hi[c];
+  template <int c> static constexpr int kLoAt = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).lo[c];
+  template <int c> static constexpr int kRow0 = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).row0[c];
+  template <int c> static constexpr int kXOff = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).xoff[c];
+  template <int c> static constexpr int kLXOff = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).lxoff[c];
+  static constexpr uint32_t kTx = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).tx;
+  static constexpr int kStage = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).stage;
+  // Exchange / staging buffer of the first half-sweep's field (E' in the
+  // E-first sweep, B' in the B-first one): per component RY+2 rows of 32
+  // (rows 0..RY-1 the tile, row RY the halo row, row RY+1 the halo column by
+  // row), hi words then lo words.
   static constexpr int kXComp = (RY + 2) * 32;  // elements per component
   static constexpr int kXHi = 0;
   static constexpr int kXLo = round128(3 * kXComp * HS);
   static constexpr int kXBytes = kXLo + (kLo ? round128(3 * kXComp * LS) : 0);
-  // B' staging buffer: per component RY rows of 32, hi words then lo words.
+  // Staging buffer of the second field (B' in the E-first sweep, E' in the
+  // B-first one): per component RY rows of 32, hi words then lo words.
   static constexpr int kBComp = RY * 32;
   static constexpr int kBLo = round128(3 * kBComp * HS);
   static constexpr int kBBytes = kBLo + (kLo ? round128(3 * kBComp * LS) : 0);
@@ -158,6 +192,9 @@ struct Plan1 {
   static constexpr int kBar = kBst + 2 * kBBytes;
   static constexpr int kList = kBar + kStages1 * 8;
   static constexpr int kTotal = kList + 4 * (kMaxSources + 1);
+  // The box the B-first sweep's halo column reads starts one column left of
+  // the tile, inside every box's left offset.
+  static_assert(!BF || (OFF >= 1 && (!kLo || kLoOff1 >= 1)), "B-first boxes need the left halo column");
   static_assert(box().hi[1] % 128 == 0 && box().hi[5] % 128 == 0 && box().lo[0] % 128 == 0 &&
                     box().lo[5] % 128 == 0,
                 "ring boxes must start on 128-byte boundaries");
@@ -183,12 +220,25 @@ __device__ __forceinline__ bool window_meets(int o, int n, int N, int a, int m) 
 //
 // fused1_tile lists the sources that can reach the tile, then runs the plane
 // loop, fused1_planes, compiled with (kSrc) or without source evaluation.
+// On a wait that gives up (any thread), every thread leaves the plane loop
+// after the iteration's barrier; the copy-engine leader then waits for the
+// tile's loads still in flight and its committed stores (drain_tile), and the
+// function returns false.
+template <int NS>
+__device__ __forceinline__ void drain_tile(uint64_t* bar, uint32_t ring, int first, int issued, const WaitCtl& wc) {
+  for (int f = first; f < issued; ++f) {
+    const uint32_t g = ring + (uint32_t)f;
+    mbar_wait_bounded(&bar[g % NS], (g / NS) & 1u, wc, 2);
+  }
+  bulk_wait_all();
+}
+
 template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSrc>
-__device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
+__device__ __forceinline__ bool fused1_planes(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                                               const CoefSet& cs, int bx, int by, int bz, int kchunk,
                                               const float* __restrict__ Jx, const float* __restrict__ Jy,
                                               const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
-                                              int* err, unsigned char* smem, uint32_t& ring, int nsrc) {
+                                              const WaitCtl& wc, unsigned char* smem, uint32_t& ring, int nsrc) {
   using P = Plan1<S, RY>;
   using HiT = typename S::HiT;
   using T = typename A::Cur;
@@ -248,7 +298,10 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
   const int hi_own = r * P::W + cx;  // ring box element offsets, before each component's shifts
   const int lo_own = r * P::LW + cx;
 
+  int issued = 0;  // ring fills of this tile issued so far (the leader's count)
   auto issue = [&](int t) {
+    if (wc.withhold) return;
+    ++issued;
     const int slot = (slot0 + t - k0) % NS;
     const int kk = (t == L.Nk) ? 0 : t;
     unsigned char* base = smem + P::kRing + slot * P::kStage;
@@ -299,7 +352,7 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
   for (int t = k0; t <= k1; ++t) {
     const int cur = t & 1;
     const int kk = (t == L.Nk) ? 0 : t;
-    mbar_wait_bounded(&bar[slot], phase, err);
+    const bool timed_out = !mbar_wait_bounded(&bar[slot], phase, wc);
     const unsigned char* stage = smem + P::kRing + slot * P::kStage;
     const HiT* H = reinterpret_cast<const HiT*>(stage) + hi_own;
     const LoT* Q = reinterpret_cast<const LoT*>(stage) + lo_own;
@@ -449,7 +502,10 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
     // The previous iteration's stores must have read their staging (written
     // again next iteration) before anyone passes this barrier.
     if (leader) bulk_wait_read_all();
-    __syncthreads();
+    if (__syncthreads_or(timed_out)) {
+      if (leader) drain_tile<NS>(bar, ring, t - k0, issued, wc);
+      return false;
+    }
     if (w == RY && lane < ny && (x0 == 0 || x0 + nx == L.Ni)) {
       // ghost columns the bulk copies do not write: x = Ni from column 0,
       // x = -1 from column nx-1, row y0+lane, copied as stored words
@@ -499,23 +555,335 @@ __device__ __forceinline__ void fused1_planes(const PLayout& L, const S& st, con
   }
   ring += (uint32_t)(k1 - k0 + 1);
   if (leader) bulk_wait_read_all();
+  return true;
+}
+
+// The B-first sweep of one tile (see the file comment): planes k1-1 down to
+// k0-1.  Same contract as fused1_planes.
+template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSrc>
+__device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
+                                               const CoefSet& cs, int bx, int by, int bz, int kchunk,
+                                               const float* __restrict__ Jx, const float* __restrict__ Jy,
+                                               const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
+                                               const WaitCtl& wc, unsigned char* smem, uint32_t& ring, int nsrc) {
+  using P = Plan1<S, RY, true>;
+  using HiT = typename S::HiT;
+  using T = typename A::Cur;
+  constexpr int NS = kStages1;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + P::kBar);
+  int* list = reinterpret_cast<int*>(smem + P::kList);
+
+  const int lane = threadIdx.x, w = threadIdx.y;
+  const int x0 = bx * 32, y0 = by * RY;
+  const int nx = min(32, L.Ni - x0), ny = min(RY, L.Nj - y0);
+  const bool hrow = (w == RY), hcol = (w == RY + 1);
+  // Box row (0: y0-1) and tile column (-1: x0-1) of the thread's cell.  Lanes
+  // of the halo-column warp past the tile's rows are clamped onto its last
+  // row: they compute but never publish.
+  const int r = hrow ? 0 : hcol ? min(lane, RY - 1) + 1 : w + 1;
+  const int cx = hcol ? -1 : lane;
+  const bool active = hrow ? (lane < nx) : hcol ? (lane < ny) : (w < ny && lane < nx);
+  const bool interior = !hrow && !hcol && w < ny && lane < nx;
+  // unwrapped coordinates (x = -1 and y = -1 are the ghost copies of Ni-1 and
+  // Nj-1); interior cells have 0 <= x < Ni, 0 <= y < Nj
+  const int xu = x0 + cx, yu = y0 + r - 1;
+  const int k0 = bz * kchunk;
+  const int k1 = min(k0 + kchunk, L.Nk);
+  const int n_it = k1 - k0 + 1;
+  const bool leader = (w == RY + 1 && lane == 0);
+  const int slot0 = (int)(ring % NS);
+  const uint32_t phase0 = (ring / NS) & 1u;
+  const bool tile_edge = x0 == 0 || x0 + nx == L.Ni || y0 == 0 || y0 + ny == L.Nj;
+  const bool tma_out = (nx == 32);
+  auto ghost_r = [&]() { return P::kLo && tma_out && x0 == 0 && L.Ni % 8 == 0; };
+  auto ghost_l = [&]() { return P::kLo && tma_out && x0 + 32 == L.Ni; };
+  const bool edge_cell = interior && (yu == 0 || yu == L.Nj - 1);
+
+  // Exchange offsets: where the thread publishes B', and (interior cells)
+  // where it finds B' at (i-1) and (j-1).
+  const int xo_own = hrow ? RY * 32 + lane : hcol ? (RY + 1) * 32 + (r - 1) : w * 32 + lane;
+  const int xo_left = (lane == 0) ? (RY + 1) * 32 + w : w * 32 + lane - 1;
+  const int xo_down = (w == 0) ? RY * 32 + lane : (w - 1) * 32 + lane;
+  const int bo_own = w * 32 + lane;
+  const int hi_own = r * P::W + cx;
+  const int lo_own = r * P::LW + cx;
+
+  // Iteration it handles plane t = k1-1-it (t = -1 is plane Nk-1) from ring
+  // fill `it` of the tile.
+  int issued = 0;
+  auto issue = [&](int it) {
+    if (wc.withhold) return;
+    ++issued;
+    const int t = k1 - 1 - it;
+    const int kk = t < 0 ? L.Nk - 1 : t;
+    const int slot = (slot0 + it) % NS;
+    unsigned char* base = smem + P::kRing + slot * P::kStage;
+    mbar_arrive_expect_tx(&bar[slot], P::kTx);
+    for_each_comp([&](auto cc) {
+      constexpr int c = decltype(cc)::value;
+      tma_load_3d(base + P::template kHiAt<c>, &maps.ld.hi[c], x0 + kPadX - P::template kXOff<c>, y0, kk,
+                  &bar[slot]);
+      if (P::kLo)
+        tma_load_3d(base + P::template kLoAt<c>, &maps.ld.lo[c], x0 + kPadX - P::template kLXOff<c>, y0, kk,
+                    &bar[slot]);
+    });
+  };
+  if (leader)
+    for (int it = 0; it < n_it && it < NS; ++it) issue(it);
+
+  // Per-column factor (amp gx) gy of the first kFastSources listed sources.
+  T sxy[kFastSources];
+  unsigned smask = 0;
+#pragma unroll
+  for (int q = 0; q < kFastSources; ++q) {
+    sxy[q] = A::cur_zero();
+    if (kSrc && q < nsrc) {
+      const DevSource& d = ss.src[list[q]];
+      const int di = box_offset(xu, d.i0, d.ni, L.Ni);
+      const int dj = box_offset(yu, d.j0, d.nj, L.Nj);
+      if (interior && di >= 0 && dj >= 0) {
+        sxy[q] = A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + step), A::cur_table(ss, d.gx_off + di)),
+                            A::cur_table(ss, d.gy_off + dj));
+        smask |= 1u << q;
+      }
+    }
+  }
+
+  // E(t+1) of the thread's cell (its z neighbour above), then B'(t+1).
+  Pair pex{0.f, 0.f}, pey{0.f, 0.f}, pez{0.f, 0.f};
+  Pair pbx{0.f, 0.f}, pby{0.f, 0.f}, pbz{0.f, 0.f};
+  if (active) {
+    const int64_t e0 = L.at(xu, yu, k1 == L.Nk ? 0 : k1);
+    pex = st.load(0, e0);
+    pey = st.load(1, e0);
+  }
+
+  int slot = slot0;
+  uint32_t phase = phase0;
+  for (int it = 0; it < n_it; ++it) {
+    const int t = k1 - 1 - it;
+    const int cur = it & 1;
+    const bool timed_out = !mbar_wait_bounded(&bar[slot], phase, wc);
+    const unsigned char* stage = smem + P::kRing + slot * P::kStage;
+    const HiT* H = reinterpret_cast<const HiT*>(stage) + hi_own;
+    const LoT* Q = reinterpret_cast<const LoT*>(stage) + lo_own;
+    auto V = [&](auto cc, int dr, int dc) -> Pair {
+      constexpr int c = decltype(cc)::value;
+      const HiT h = H[P::template kHiAt<c> / P::HS + (dr - P::template kRow0<c>) * P::W + P::template kXOff<c> + dc];
+      const LoT q = P::kLo ? Q[P::template kLoAt<c> / P::LS + (dr - P::template kRow0<c>) * P::LW +
+                               P::template kLXOff<c> + dc]
+                           : LoT(0);
+      return st.decode(c, h, q);
+    };
+
+    // 1. B'(t), in the operation order of the B sweep (kernels_f32.cu b_column)
+    const Pair ex = V(Comp<0>{}, 0, 0), ey = V(Comp<1>{}, 0, 0), ez = V(Comp<2>{}, 0, 0);
+    Pair ux = A::curl(bcoef<S>(cs, st, 0, 0), pey, ey, bcoef<S>(cs, st, 0, 1), V(Comp<2>{}, 1, 0), ez);
+    Pair uy = A::curl(bcoef<S>(cs, st, 1, 0), V(Comp<2>{}, 0, 1), ez, bcoef<S>(cs, st, 1, 1), pex, ex);
+    Pair uz = A::curl(bcoef<S>(cs, st, 2, 0), V(Comp<0>{}, 1, 0), ex, bcoef<S>(cs, st, 2, 1), V(Comp<1>{}, 0, 1), ey);
+    if (kApps == 2) {
+      ux = A::twice(ux);
+      uy = A::twice(uy);
+      uz = A::twice(uz);
+    }
+    const Pair ax = A::acc(V(Comp<3>{}, 0, 0), ux), ay = A::acc(V(Comp<4>{}, 0, 0), uy),
+               az = A::acc(V(Comp<5>{}, 0, 0), uz);
+    // B' in its stored words; the E update uses the value they hold.
+    const HiT bhx = st.enc_hi(3, ax), bhy = st.enc_hi(4, ay), bhz = st.enc_hi(5, az);
+    const LoT blx = st.enc_lo(ax), bly = st.enc_lo(ay), blz = st.enc_lo(az);
+    const Pair nbx = st.decode(3, bhx, blx), nby = st.decode(4, bhy, bly), nbz = st.decode(5, bhz, blz);
+
+    unsigned char* xb = smem + P::kExch + cur * P::kXBytes;
+    if (active) {
+      HiT* xh = reinterpret_cast<HiT*>(xb + P::kXHi) + xo_own;
+      xh[0] = bhx;
+      xh[P::kXComp] = bhy;
+      xh[2 * P::kXComp] = bhz;
+      if (P::kLo) {
+        LoT* xq = reinterpret_cast<LoT*>(xb + P::kXLo) + xo_own;
+        xq[0] = blx;
+        xq[P::kXComp] = bly;
+        xq[2 * P::kXComp] = blz;
+      }
+    }
+
+    // 2. E'(t+1), in the operation order of the E sweep (kernels_f32.cu e_sweep)
+    Pair nex{0.f, 0.f}, ney{0.f, 0.f}, nez{0.f, 0.f};
+    unsigned char* eb = smem + P::kBst + cur * P::kBBytes;
+    const bool e_step = it > 0;  // plane t+1 lies in the chunk
+    if (e_step && interior) {
+      const int ke = t + 1;  // < k1 <= Nk
+      const unsigned char* pb = smem + P::kExch + (cur ^ 1) * P::kXBytes;
+      const HiT* ph = reinterpret_cast<const HiT*>(pb + P::kXHi);
+      const LoT* pq = reinterpret_cast<const LoT*>(pb + P::kXLo);
+      auto Bn = [&](int c, int off) -> Pair {  // B'(t+1), component 3 + c
+        return st.decode(3 + c, ph[c * P::kXComp + off], P::kLo ? pq[c * P::kXComp + off] : LoT(0));
+      };
+      Pair qx = A::curl(ecoef<S>(cs, st, 0, 0), pbz, Bn(2, xo_down), ecoef<S>(cs, st, 0, 1), pby, nby);
+      Pair qy = A::curl(ecoef<S>(cs, st, 1, 0), pbx, nbx, ecoef<S>(cs, st, 1, 1), pbz, Bn(2, xo_left));
+      Pair qz = A::curl(ecoef<S>(cs, st, 2, 0), pby, Bn(1, xo_left), ecoef<S>(cs, st, 2, 1), pbx, Bn(0, xo_down));
+      if (kDenseJ || kSrc) {
+        T jv[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
+        unsigned has = 0;
+        if (kDenseJ) {
+          const int64_t d = xu + (int64_t)yu * L.Ni + (int64_t)ke * L.Ni * L.Nj;
+          jv[0] = A::cur_dense(Jx[d]);
+          jv[1] = A::cur_dense(Jy[d]);
+          jv[2] = A::cur_dense(Jz[d]);
+          has = 7u;
+        }
+#pragma unroll
+        for (int q = 0; q < kFastSources; ++q) {
+          if (kSrc && q < nsrc) {
+            const DevSource& d = ss.src[list[q]];
+            const int dk = box_offset(ke, d.k0, d.nk, L.Nk);  // the same for the whole tile
+            if (dk >= 0 && (smask >> q & 1u)) {
+              add_current<A>(jv, d.comp_mask, A::cur_mul(sxy[q], A::cur_table(ss, d.gz_off + dk)));
+              has |= (unsigned)d.comp_mask;
+            }
+          }
+        }
+        for (int i = kFastSources; kSrc && i < nsrc; ++i) {
+          const DevSource& d = ss.src[list[i]];
+          const int dk = box_offset(ke, d.k0, d.nk, L.Nk);
+          if (dk < 0) continue;
+          const int di = box_offset(xu, d.i0, d.ni, L.Ni);
+          const int dj = box_offset(yu, d.j0, d.nj, L.Nj);
+          if (di >= 0 && dj >= 0) {
+            add_current<A>(jv, d.comp_mask,
+                           A::cur_mul(A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + step),
+                                                            A::cur_table(ss, d.gx_off + di)),
+                                                 A::cur_table(ss, d.gy_off + dj)),
+                                      A::cur_table(ss, d.gz_off + dk)));
+            has |= (unsigned)d.comp_mask;
+          }
+        }
+        if (has & 1u) qx = A::add(qx, A::cur_term(jcoef<S>(cs, st, 0), jv[0]));
+        if (has & 2u) qy = A::add(qy, A::cur_term(jcoef<S>(cs, st, 1), jv[1]));
+        if (has & 4u) qz = A::add(qz, A::cur_term(jcoef<S>(cs, st, 2), jv[2]));
+      }
+      nex = A::acc(pex, qx);
+      ney = A::acc(pey, qy);
+      nez = A::acc(pez, qz);
+      HiT* eh = reinterpret_cast<HiT*>(eb) + bo_own;
+      eh[0] = st.enc_hi(0, nex);
+      eh[P::kBComp] = st.enc_hi(1, ney);
+      eh[2 * P::kBComp] = st.enc_hi(2, nez);
+      if (P::kLo) {
+        LoT* eq = reinterpret_cast<LoT*>(eb + P::kBLo) + bo_own;
+        eq[0] = st.enc_lo(nex);
+        eq[P::kBComp] = st.enc_lo(ney);
+        eq[2 * P::kBComp] = st.enc_lo(nez);
+      }
+    }
+    if (!tma_out && interior) {
+      const int64_t o = L.at(xu, yu, 0);
+      if (t >= k0) {
+        out.store(3, o + (int64_t)t * L.pplane, nbx);
+        out.store(4, o + (int64_t)t * L.pplane, nby);
+        out.store(5, o + (int64_t)t * L.pplane, nbz);
+      }
+      if (e_step) {
+        out.store(0, o + (int64_t)(t + 1) * L.pplane, nex);
+        out.store(1, o + (int64_t)(t + 1) * L.pplane, ney);
+        out.store(2, o + (int64_t)(t + 1) * L.pplane, nez);
+      }
+    }
+    // Ghost copies of edge cells (their tiles only).
+    if (tile_edge && edge_cell) {
+      if (t >= k0) {
+        store_ghost_rows(out, L, true, true, 3, xu, yu, t, nbx);
+        store_ghost_rows(out, L, true, true, 4, xu, yu, t, nby);
+        store_ghost_rows(out, L, true, true, 5, xu, yu, t, nbz);
+      }
+      if (e_step) {
+        store_ghost_rows(out, L, true, true, 0, xu, yu, t + 1, nex);
+        store_ghost_rows(out, L, true, true, 1, xu, yu, t + 1, ney);
+        store_ghost_rows(out, L, true, true, 2, xu, yu, t + 1, nez);
+      }
+    }
+
+    pex = ex;
+    pey = ey;
+    pez = ez;
+    pbx = nbx;
+    pby = nby;
+    pbz = nbz;
+    fence_async_smem();
+    if (leader) bulk_wait_read_all();
+    if (__syncthreads_or(timed_out)) {
+      if (leader) drain_tile<NS>(bar, ring, it, issued, wc);
+      return false;
+    }
+    if (w == RY && lane < ny && (x0 == 0 || x0 + nx == L.Ni)) {
+      // ghost columns the bulk copies do not write: x = Ni from column 0,
+      // x = -1 from column nx-1, row y0+lane, copied as stored words
+#pragma unroll 1
+      for (int side = 0; side < 2; ++side) {
+        const bool on = side == 0 ? (x0 == 0 && !ghost_r()) : (x0 + nx == L.Ni && !ghost_l());
+        if (!on) continue;
+        const int col = side == 0 ? 0 : nx - 1;
+        const int64_t g = L.at(side == 0 ? L.Ni : -1, y0 + lane, 0);
+        const HiT* bh = reinterpret_cast<const HiT*>(xb + P::kXHi) + lane * 32 + col;
+        const LoT* bq = reinterpret_cast<const LoT*>(xb + P::kXLo) + lane * 32 + col;
+        const HiT* eh = reinterpret_cast<const HiT*>(eb) + lane * 32 + col;
+        const LoT* eq = reinterpret_cast<const LoT*>(eb + P::kBLo) + lane * 32 + col;
+        if (t >= k0)
+          for (int c = 0; c < 3; ++c)
+            out.store_words(3 + c, g + (int64_t)t * L.pplane, bh[c * P::kXComp], P::kLo ? bq[c * P::kXComp] : LoT(0));
+        if (e_step)
+          for (int c = 0; c < 3; ++c)
+            out.store_words(c, g + (int64_t)(t + 1) * L.pplane, eh[c * P::kBComp],
+                            P::kLo ? eq[c * P::kBComp] : LoT(0));
+      }
+    }
+    if (leader) {
+      // the tile's boxes at its own columns, then the margins it fills
+#pragma unroll 1
+      for (int g = 0; g < 3 && tma_out; ++g) {
+        if ((g == 1 && !ghost_r()) || (g == 2 && !ghost_l())) continue;
+        const int xs = g == 0 ? x0 + kPadX : g == 1 ? L.Ni + kPadX : 0;
+        if (t >= k0)
+          for (int c = 0; c < 3; ++c) {
+            tma_store_3d(&maps.st.hi[3 + c], xb + P::kXHi + c * P::kXComp * P::HS, xs, y0, t);
+            if (P::kLo) tma_store_3d(&maps.st.lo[3 + c], xb + P::kXLo + c * P::kXComp * P::LS, xs, y0, t);
+          }
+        if (e_step)
+          for (int c = 0; c < 3; ++c) {
+            tma_store_3d(&maps.st.hi[c], eb + c * P::kBComp * P::HS, xs, y0, t + 1);
+            if (P::kLo) tma_store_3d(&maps.st.lo[c], eb + P::kBLo + c * P::kBComp * P::LS, xs, y0, t + 1);
+          }
+      }
+      bulk_commit();
+      if (it + NS < n_it) issue(it + NS);
+    }
+    if (++slot == NS) {
+      slot = 0;
+      phase ^= 1u;
+    }
+  }
+  ring += (uint32_t)n_it;
+  if (leader) bulk_wait_read_all();
+  return true;
 }
 
 //
 // kSplit: compile the plane loop twice and run the source-free copy on tiles
 // that no source reaches (fewer live registers there).  The batched kernel
 // takes either: where its tiles alternate between the two cases, two hot
-// copies of the loop ran slower than one (its autotuner picks).
-template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSplit>
-__device__ __forceinline__ void fused1_tile(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
+// copies of the loop ran slower than one (its autotuner picks).  kBF selects
+// the B-first sweep.  Returns false when a bounded wait gave up (uniform over
+// the CTA).
+template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSplit, bool kBF>
+__device__ __forceinline__ bool fused1_tile(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                                             const CoefSet& cs, int bx, int by, int bz, int kchunk,
                                             const float* __restrict__ Jx, const float* __restrict__ Jy,
                                             const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
-                                            int* err, unsigned char* smem, uint32_t& ring) {
-  using P = Plan1<S, RY>;
+                                            const WaitCtl& wc, unsigned char* smem, uint32_t& ring) {
+  using P = Plan1<S, RY, kBF>;
   int* list = reinterpret_cast<int*>(smem + P::kList);
-  // Sources that can touch this tile's cells (its E' halo included), in
-  // registration order; the exact per-cell test comes in the plane loop.
+  // Sources that can touch this tile's cells (with one cell of halo on each
+  // side), in registration order; the exact per-cell test comes in the plane loop.
   if (threadIdx.y == 0) {
     const int lane = threadIdx.x;
     const int x0 = bx * 32, y0 = by * RY;
@@ -537,12 +905,14 @@ __device__ __forceinline__ void fused1_tile(const PLayout& L, const S& st, const
   }
   __syncthreads();
   const int nsrc = list[kMaxSources];
-  if (!kSplit || nsrc > 0)
-    fused1_planes<S, A, RY, kApps, kDenseJ, true>(L, st, out, maps, cs, bx, by, bz, kchunk, Jx, Jy, Jz, ss, step, err,
-                                                  smem, ring, nsrc);
-  else
-    fused1_planes<S, A, RY, kApps, kDenseJ, false>(L, st, out, maps, cs, bx, by, bz, kchunk, Jx, Jy, Jz, ss, step,
-                                                   err, smem, ring, 0);
+#define FDTD_PLANES(SRC, NSRC)                                                                                   \
+  return kBF ? fused1b_planes<S, A, RY, kApps, kDenseJ, SRC>(L, st, out, maps, cs, bx, by, bz, kchunk, Jx, Jy, Jz, \
+                                                            ss, step, wc, smem, ring, NSRC)                      \
+             : fused1_planes<S, A, RY, kApps, kDenseJ, SRC>(L, st, out, maps, cs, bx, by, bz, kchunk, Jx, Jy, Jz,  \
+                                                           ss, step, wc, smem, ring, NSRC)
+  if (!kSplit || nsrc > 0) FDTD_PLANES(true, nsrc);
+  FDTD_PLANES(false, 0);
+#undef FDTD_PLANES
 }
 
 template <int NS>
@@ -554,32 +924,33 @@ __device__ __forceinline__ void init_ring(uint64_t* bar) {
   __syncthreads();
 }
 
-template <class S, class A, int RY, int kApps, bool kDenseJ>
+template <class S, class A, int RY, int kApps, bool kDenseJ, bool kBF>
 __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
     fused1(PLayout L, S st, S out, const __grid_constant__ StepMaps maps, CoefSet cs, int kchunk,
            const float* __restrict__ Jx, const float* __restrict__ Jy, const float* __restrict__ Jz,
-           SourceSet ss, int64_t step, int* err) {
+           SourceSet ss, int64_t step, WaitCtl wc) {
   extern __shared__ __align__(128) unsigned char smem[];
-  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
+  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY, kBF>::kBar));
   uint32_t ring = 0;
-  fused1_tile<S, A, RY, kApps, kDenseJ, true>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z, kchunk, Jx, Jy,
-                                              Jz, ss, step, err, smem, ring);
+  fused1_tile<S, A, RY, kApps, kDenseJ, true, kBF>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z, kchunk,
+                                                   Jx, Jy, Jz, ss, step, wc, smem, ring);
   if (threadIdx.x == 0 && threadIdx.y == RY + 1) bulk_wait_all();  // the copy-engine leader's stores
 }
 
-// Batched form: a persistent kernel; every CTA takes tiles (domain, bx, by,
-// bz) from the tile table in order, through an atomic counter, until none
-// are left.  `parity` selects which of each domain's two copies is read.  The
-// last CTA to finish resets the counters for the next launch.
+// Batched form: a persistent kernel of B-first sweeps; every CTA takes tiles
+// (domain, bx, by, bz) from the tile table in order, through an atomic
+// counter, until none are left.  `parity` selects which of each domain's two
+// copies is read.  The last CTA to finish resets the counters for the next
+// launch.
 template <class S, class A, int RY, int kApps, bool kSplit>
 __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
     fused1_batch(const BatchDomain<S>* __restrict__ doms, const StepMaps* __restrict__ maps,
                  const int4* __restrict__ tiles, int n_tiles, int parity, int kchunk,
-                 const int64_t* __restrict__ step_base, int step_off, int* counters, int* err) {
+                 const int64_t* __restrict__ step_base, int step_off, int* counters, WaitCtl wc) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ BatchDomain<S> dom;
   __shared__ int4 tile;
-  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
+  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY, true>::kBar));
   const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const int64_t step = *step_base + step_off;
@@ -602,12 +973,13 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
       const StepMaps& m = maps[2 * w.x + parity];
       const int q = threadIdx.x;
       const CUtensorMap* tm = q < 6 ? &m.ld.hi[q] : q < 12 ? &m.ld.lo[q - 6] : q < 18 ? &m.st.hi[q - 12] : &m.st.lo[q - 18];
-      if (Plan1<S, RY>::kLo || (q < 6 || (q >= 12 && q < 18))) prefetch_tensormap(tm);
+      if (Plan1<S, RY, true>::kLo || (q < 6 || (q >= 12 && q < 18))) prefetch_tensormap(tm);
     }
     __syncthreads();
-    fused1_tile<S, A, RY, kApps, false, kSplit>(dom.L, dom.s[parity], dom.s[parity ^ 1], maps[2 * w.x + parity], dom.cs,
-                                               w.y, w.z, w.w, kchunk, nullptr, nullptr, nullptr, dom.ss, step, err, smem,
-                                               ring);
+    const bool ok = fused1_tile<S, A, RY, kApps, false, kSplit, true>(
+        dom.L, dom.s[parity], dom.s[parity ^ 1], maps[2 * w.x + parity], dom.cs, w.y, w.z, w.w, kchunk, nullptr,
+        nullptr, nullptr, dom.ss, step, wc, smem, ring);
+    if (!ok) break;  // a wait gave up: this CTA takes no more tiles
     __syncthreads();
   }
   if (threadIdx.x == 0 && threadIdx.y == RY + 1) bulk_wait_all();  // the copy-engine leader's stores
@@ -622,26 +994,27 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
 
 // ---------------------------------------------------------------------------
 
-template <class S, int RY, int APPS, bool DJ>
+template <class S, int RY, int APPS, bool DJ, bool BF>
 static cudaError_t launch1_one(dim3 grid, const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                                const CoefSet& cs, int kchunk, const float* const J[3], const SourceSet& ss,
-                               int64_t step, int* err, cudaStream_t stream) {
+                               int64_t step, const WaitCtl& wc, cudaStream_t stream) {
   using A = typename ArithOf1<S>::type;
-  auto kern = fused1<S, A, RY, APPS, DJ>;
-  const int bytes = Plan1<S, RY>::kTotal;
+  auto kern = fused1<S, A, RY, APPS, DJ, BF>;
+  const int bytes = Plan1<S, RY, BF>::kTotal;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
-  kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(L, st, out, maps, cs, kchunk, J[0], J[1], J[2], ss, step, err);
+  kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(L, st, out, maps, cs, kchunk, J[0], J[1], J[2], ss, step, wc);
   return cudaGetLastError();
 }
 
-template <class S, int RY>
+template <class S, int RY, bool BF>
 static cudaError_t launch1_ry(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                               const float* const J[3], bool dense_j, const CoefSet& cs, const SourceSet& ss,
-                              int64_t step, int applications, int kchunk, int* err, cudaStream_t stream) {
+                              int64_t step, int applications, int kchunk, const WaitCtl& wc, cudaStream_t stream) {
   if (ss.count > kMaxSources) return cudaErrorInvalidValue;
   dim3 grid((L.Ni + 31) / 32, (L.Nj + RY - 1) / RY, (L.Nk + kchunk - 1) / kchunk);
-#define FDTD_F(APPS, DJ) return launch1_one<S, RY, APPS, DJ>(grid, L, st, out, maps, cs, kchunk, J, ss, step, err, stream)
+#define FDTD_F(APPS, DJ) \
+  return launch1_one<S, RY, APPS, DJ, BF>(grid, L, st, out, maps, cs, kchunk, J, ss, step, wc, stream)
   if (applications == 2) {
     if (dense_j) FDTD_F(2, true);
     FDTD_F(2, false);
@@ -654,24 +1027,26 @@ static cudaError_t launch1_ry(const PLayout& L, const S& st, const S& out, const
 template <class S>
 cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const void* maps,
                               const float* const J[3], bool dense_j, const CoefSet& cs, const SourceSet& ss,
-                              int64_t step, int applications, const FusedConfig& cfg, int* err,
-                              cudaStream_t stream) {
+                              int64_t step, int applications, const FusedConfig& cfg, bool b_first,
+                              const WaitCtl& wc, cudaStream_t stream) {
   const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 48;
   const StepMaps& m = *static_cast<const StepMaps*>(maps);
-  if (cfg.tile_y == 6)
-    return launch1_ry<S, 6>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
-  if (cfg.tile_y == 30)
-    return launch1_ry<S, 30>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
-  return launch1_ry<S, 14>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, err, stream);
+#define FDTD_RY(RY)                                                                                                 \
+  return b_first ? launch1_ry<S, RY, true>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, wc, stream) \
+                 : launch1_ry<S, RY, false>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, wc, stream)
+  if (cfg.tile_y == 6) FDTD_RY(6);
+  if (cfg.tile_y == 30) FDTD_RY(30);
+  FDTD_RY(14);
+#undef FDTD_RY
 }
 
 template <class S, int RY, int APPS, bool SPLIT>
 static cudaError_t launch1_batch_one(const BatchDomain<S>* doms, const StepMaps* maps, const int4* tiles,
                                      int n_tiles, int parity, int kchunk, const int64_t* step_base, int step_off,
-                                     int* counters, int* err, cudaStream_t stream) {
+                                     int* counters, const WaitCtl& wc, cudaStream_t stream) {
   using A = typename ArithOf1<S>::type;
   auto kern = fused1_batch<S, A, RY, APPS, SPLIT>;
-  const int bytes = Plan1<S, RY>::kTotal;
+  const int bytes = Plan1<S, RY, true>::kTotal;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
@@ -681,22 +1056,22 @@ static cudaError_t launch1_batch_one(const BatchDomain<S>* doms, const StepMaps*
     return e;
   const int grid = sms * (per_sm > 0 ? per_sm : 1);
   kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(doms, maps, tiles, n_tiles, parity, kchunk, step_base, step_off,
-                                                  counters, err);
+                                                  counters, wc);
   return cudaGetLastError();
 }
 
 template <class S>
 cudaError_t launch_fused1_batch(const void* doms, const StepMaps* maps, const int4* tiles, int n_tiles, int parity,
                                 int applications, const FusedConfig& cfg, const int64_t* step_base, int step_off,
-                                int* counters, int* err, cudaStream_t stream) {
+                                int* counters, const WaitCtl& wc, cudaStream_t stream) {
   const BatchDomain<S>* d = static_cast<const BatchDomain<S>*>(doms);
   const int kc = cfg.kchunk;
 #define FDTD_B1(RY, SPLIT)                                                                                          \
   return applications == 2                                                                                       \
              ? launch1_batch_one<S, RY, 2, SPLIT>(d, maps, tiles, n_tiles, parity, kc, step_base, step_off, counters, \
-                                                  err, stream)                                                   \
+                                                  wc, stream)                                                    \
              : launch1_batch_one<S, RY, 1, SPLIT>(d, maps, tiles, n_tiles, parity, kc, step_base, step_off, counters, \
-                                                  err, stream)
+                                                  wc, stream)
 #define FDTD_B(RY)                  \
   {                                 \
     if (cfg.split_sources)          \
@@ -717,9 +1092,10 @@ int fused1_lo_box_width() { return Box1<StoreF32C>::kLoW; }
 #define FDTD_INSTANTIATE(S)                                                                              \
   template cudaError_t launch_fused1_f32<S>(const PLayout&, const S&, const S&, const void*,            \
                                             const float* const[3], bool, const CoefSet&, const SourceSet&, \
-                                            int64_t, int, const FusedConfig&, int*, cudaStream_t);       \
+                                            int64_t, int, const FusedConfig&, bool, const WaitCtl&, cudaStream_t); \
   template cudaError_t launch_fused1_batch<S>(const void*, const StepMaps*, const int4*, int, int, int,          \
-                                              const FusedConfig&, const int64_t*, int, int*, int*, cudaStream_t); \
+                                              const FusedConfig&, const int64_t*, int, int*, const WaitCtl&,     \
+                                              cudaStream_t);                                                     \
   template int fused1_box_width<S>();
 FDTD_INSTANTIATE(StoreF32)
 FDTD_INSTANTIATE(StoreF32C)

@@ -2,6 +2,9 @@
 // diagnostics, and small helpers.
 #include "engine_internal.h"
 
+#include <algorithm>
+#include <cmath>
+
 namespace fdtd {
 
 namespace {
@@ -149,7 +152,64 @@ __global__ void __launch_bounds__(kDiagThreads) sums_pass2(const double* partial
   }
 }
 
+// Largest |stored value| of each FP16 component over the grid's cells: the
+// rows (y, z) are taken by blocks in turn; per block the six maxima go to
+// out[c] with atomicMax on the FP32 bit pattern (non-negative floats order
+// as their bits; NaN is skipped by fmaxf).  out must hold zeros.
+__global__ void __launch_bounds__(256) f16_absmax_kernel(PLayout L, StoreF16 st, unsigned* out) {
+  float m[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  const int64_t rows = (int64_t)L.Nj * L.Nk;
+  for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int z = (int)(row / L.Nj), y = (int)(row - (int64_t)z * L.Nj);
+    const int64_t base = L.at(0, y, z);
+    for (int x = threadIdx.x; x < L.Ni; x += blockDim.x)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) m[c] = fmaxf(m[c], fabsf(__half2float(st.v[c][base + x])));
+  }
+  __shared__ float red[8][6];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    float v = m[c];
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) red[warp][c] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    float v = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmaxf(v, red[w][threadIdx.x]);
+    atomicMax(&out[threadIdx.x], __float_as_uint(v));
+  }
+}
+
+// v[i] = v[i] * 2^d over n (even) stored FP16 words, two at a time: exact
+// unless a value leaves FP16's normal range.
+__global__ void f16_rescale_kernel(__half2* v, int64_t pairs, float factor) {
+  const float2 f = make_float2(factor, factor);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < pairs; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 x = __half22float2(v[i]);
+    v[i] = __float22half2_rn(make_float2(x.x * f.x, x.y * f.y));
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_f16_absmax(const PLayout& L, const StoreF16& st, unsigned* out_dev, cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(out_dev, 0, 6 * sizeof(unsigned), stream);
+  if (e != cudaSuccess) return e;
+  const int64_t rows = (int64_t)L.Nj * L.Nk;
+  const int blocks = (int)std::min<int64_t>(rows, 152 * 16);
+  f16_absmax_kernel<<<blocks, 256, 0, stream>>>(L, st, out_dev);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_f16_rescale(__half* v, int64_t n, int shift, cudaStream_t stream) {
+  if (shift == 0 || n <= 0) return cudaSuccess;
+  const int64_t pairs = n / 2;
+  f16_rescale_kernel<<<conv_blocks(pairs), kConvThreads, 0, stream>>>(reinterpret_cast<__half2*>(v), pairs,
+                                                                      std::ldexp(1.0f, shift));
+  return cudaGetLastError();
+}
 
 cudaError_t launch_import(const StateView& v, int c, const double* src, int64_t off, int64_t n,
                           cudaStream_t st) {

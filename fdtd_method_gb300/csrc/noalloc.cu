@@ -17,10 +17,13 @@
 //
 // The first call on a device looks up the array's device address with
 // cudaGetSymbolAddress (the host-side name of a __device__ array is not a
-// device address); make that first call before any stream capture.  All calls
-// share the one array: calls whose kernels overlap on the GPU (different
-// streams, no ordering between them) race on it.  Every slot a call reads is
-// written by the same call first, so nothing needs clearing between calls.
+// device address); make that first call before any stream capture.  Later
+// calls look it up again unless their stream is capturing (the address moves
+// if the device's context was reset and the module reloaded); a capturing
+// call uses the address found last.  All calls share the one array: calls
+// whose kernels overlap on the GPU (different streams, no ordering between
+// them) race on it.  Every slot a call reads is written by the same call
+// first, so nothing needs clearing between calls.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -110,15 +113,23 @@ int noalloc_fail(int code, const std::string& msg) {
   return code;
 }
 
-// Device address of the static partials on the current device (looked up
-// once per device).
-int partials_address(double** out) {
+// Device address of the static partials on the current device: looked up on
+// the device's first call and on every call outside a stream capture; a call
+// on a capturing stream takes the address found last.
+int partials_address(cudaStream_t st, double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return noalloc_fail(FDTD_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(FDTD_ERR_UNSUPPORTED, "device index beyond the supported range");
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(st, &cs);
+  if (e != cudaSuccess)
+    return noalloc_fail(FDTD_ERR_CUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_partials_addr[dev]) {
+  if (!g_partials_addr[dev] || cs == cudaStreamCaptureStatusNone) {
+    if (cs != cudaStreamCaptureStatusNone)
+      return noalloc_fail(FDTD_ERR_INVALID_ARGUMENT,
+                          "the first call on a device must come before any stream capture");
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_partials);
     if (e != cudaSuccess || !p)
@@ -143,9 +154,9 @@ int fdtd_field_sums_noalloc(const double* const fields[6], int64_t cells, double
     return noalloc_fail(FDTD_ERR_INVALID_ARGUMENT,
                         "grid too large for fdtd_field_sums_noalloc: at most 268435456 cells "
                         "(its fixed device scratch holds 65536 block partials); use fdtd_field_sums");
-  double* partials = nullptr;
-  if (int rc = partials_address(&partials)) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double* partials = nullptr;
+  if (int rc = partials_address(st, &partials)) return rc;
   noalloc_pass1<<<(unsigned)blocks, kNoAllocThreads, 0, st>>>(fields[0], fields[1], fields[2], fields[3],
                                                                 fields[4], fields[5], cells, partials);
   cudaError_t e = cudaGetLastError();

@@ -52,15 +52,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
-// Waits for phase `parity` of the barrier with a bounded number of polls; on
-// giving up it records code 1 in *err and returns false (the caller carries
-// on with whatever the buffer holds, so that no thread is left at a barrier).
+// Bounded waits.  A wait polls the barrier at most `polls` times; on giving
+// up it records bit 0 in *err and returns false.  The fused kernels then stop
+// their tile loops uniformly (the CTA's barrier reduces every thread's
+// outcome), wait (again bounded) for the copies they still have in flight,
+// record bit 1 if one of those waits gives up too, and return: no thread is
+// left at a barrier and no copy lands in a CTA that has exited.
 constexpr uint32_t kMaxBarrierPolls = 1u << 24;
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
-  for (uint32_t n = 0; n < kMaxBarrierPolls; ++n)
+struct WaitCtl {
+  int* err;        // device status word, read and cleared by fdtd_synchronize
+  uint32_t polls;  // polls before a wait gives up (kMaxBarrierPolls)
+  int withhold;    // test hook of the timeout path: issue no tile loads, so
+                   // every wait gives up with no copy in flight (0: off)
+};
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, const WaitCtl& wc, int code = 1) {
+  for (uint32_t n = 0; n < wc.polls; ++n)
     if (mbar_try_wait(bar, parity)) return true;
-  atomicOr(err, 1);
+  atomicOr(wc.err, code);
   return false;
 }
 

@@ -305,11 +305,35 @@ class FDTD:
         arr = (ctypes.c_int * 6)(*[int(e) for e in exps])
         _lib.check(self._lib.fdtd_set_fp16_exponents(self._handle(), arr))
 
+    def fp16_exponents(self):
+        arr = (ctypes.c_int * 6)()
+        _lib.check(self._lib.fdtd_get_fp16_exponents(self._handle(), arr))
+        return list(arr)
+
+    def fp16_autoscale(self, target_log2=12):
+        """FP16 form: re-encode every component with a nonzero peak so that
+        its stored peak lies in (2^(target-1), 2^target]; returns the exponents."""
+        arr = (ctypes.c_int * 6)()
+        _lib.check(self._lib.fdtd_fp16_autoscale(self._handle(), int(target_log2), arr))
+        return list(arr)
+
+    def set_fp16_autoscale(self, every_steps, target_log2=12):
+        """FP16 form: step() scans the stored peaks every `every_steps` steps
+        (0: never) and re-encodes components that left the band around
+        2^target."""
+        _lib.check(self._lib.fdtd_set_fp16_autoscale(self._handle(), int(every_steps), int(target_log2)))
+
     def set_fp64_arith(self, contracted):
         """FP64 form: False keeps the reference's arithmetic bit for bit (the
         default); True accumulates each curl and current term with DFMA
         (fewer FP64 instructions; within a few ulps per step)."""
         _lib.check(self._lib.fdtd_set_fp64_arith(self._handle(), 1 if contracted else 0))
+
+    def set_wait_limit(self, polls=0, withhold_loads=False):
+        """Test hook of the bounded device waits (fdtd_set_wait_limit): waits
+        give up after `polls` polls (0: the default); withhold_loads makes the
+        fused sweeps issue no tile loads, so every wait gives up."""
+        _lib.check(self._lib.fdtd_set_wait_limit(self._handle(), int(polls), 1 if withhold_loads else 0))
 
     KERNEL_KINDS = ("e_update", "b_half", "b_double", "fused_step")
     PIPELINES = {"auto": 0, "split": 1, "fused": 2}

@@ -30,7 +30,7 @@ from . import _lib
 from ._lib import InvalidArgument
 from .fdtd import FDTD, Parameters, Precision, Const
 
-SWEEP_B_HALF, SWEEP_B_DOUBLE, SWEEP_E = 0, 1, 2
+SWEEP_B_HALF, SWEEP_B_DOUBLE, SWEEP_E, SWEEP_B_DEFER = 0, 1, 2, 3
 HALO_E, HALO_B = 0, 1
 PLANE_HALO_BELOW, PLANE_FIRST, PLANE_LAST, PLANE_HALO_ABOVE = 0, 1, 2, 3
 
@@ -50,22 +50,25 @@ def slab_bounds(nk, n):
     return out
 
 
-def step_schedule(n):
+def step_schedule(n, defer=False, pending=False):
     """The operations of n update_fields steps on a set of slabs, in order:
     ("exchange", HALO_E | HALO_B) or ("sweep", SWEEP_*).
 
     One step is B/2, E, B/2 (src/FDTD_kokkos/FDTD_kokkos.cpp:91-104); the
     trailing B half step of one step and the leading one of the next share a
-    sweep (SWEEP_B_DOUBLE), as in the single-grid engine.  The E halo is
-    exchanged first, so fields set from the host since the last step are
-    seen across the slab faces."""
+    sweep (SWEEP_B_DOUBLE), as in the single-grid engine.  With `defer` the
+    last step's trailing half is left pending (SWEEP_B_DEFER, the
+    FP32-arithmetic forms), and a call made with `pending` starts with the
+    double sweep that applies it.  The E halo is exchanged first, so fields
+    set from the host since the last step are seen across the slab faces."""
     n = int(n)
     if n <= 0:
         return []
-    ops = [("exchange", HALO_E), ("sweep", SWEEP_B_HALF)]
+    ops = [("exchange", HALO_E), ("sweep", SWEEP_B_DOUBLE if pending else SWEEP_B_HALF)]
     for s in range(n):
+        last = SWEEP_B_DEFER if defer else SWEEP_B_HALF
         ops += [("exchange", HALO_B), ("sweep", SWEEP_E), ("exchange", HALO_E),
-                ("sweep", SWEEP_B_DOUBLE if s + 1 < n else SWEEP_B_HALF)]
+                ("sweep", SWEEP_B_DOUBLE if s + 1 < n else last)]
     return ops
 
 
@@ -162,6 +165,10 @@ class FDTDSlabs:
             raise
         self._lib = _lib.load()
         self._arr = (ctypes.c_void_p * len(self.slabs))(*[s._handle().value for s in self.slabs])
+        # FP32-arithmetic forms leave the last step's trailing B half pending,
+        # as the whole-grid handle does (the FP64 form applies every half)
+        self._defer = self.precision != Precision.FP64
+        self._pending = False
 
     def close(self):
         for s in self.slabs:
@@ -192,12 +199,15 @@ class FDTDSlabs:
         """n consecutive update_fields() calls on every slab."""
         if int(n) < 0:
             raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "negative step count")
-        for op, arg in step_schedule(n):
+        if int(n) == 0:
+            return
+        for op, arg in step_schedule(n, self._defer, self._pending):
             if op == "exchange":
                 self.exchange(arg)
             else:
                 for s in self.slabs:
                     s.sweep(arg)
+        self._pending = self._defer
 
     def update_fields(self):
         self.step(1)
@@ -240,6 +250,8 @@ class FDTDSlabs:
         plane = int(self.parameters.Ni) * int(self.parameters.Nj)
         for s, (k0, k1) in zip(self.slabs, self.bounds):
             s.copy_from_host(comp, a[k0 * plane:k1 * plane])
+        if int(comp) < 6:
+            self._pending = False  # every slab applied its pending half before the write
 
     def field_sums(self):
         """Sums over all cells (the slabs' FP64 sums added)."""
@@ -253,6 +265,7 @@ class FDTDSlabs:
     def set_fp16_exponents(self, exps):
         for s in self.slabs:
             s.set_fp16_exponents(exps)
+        self._pending = False
 
     @property
     def step_index(self):

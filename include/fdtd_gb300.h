@@ -132,7 +132,13 @@ int fdtd_get_pml(fdtd_handle* h, int sizes[3]);
 int fdtd_destroy(fdtd_handle* h);
 
 /* Replaces FDTD::update_fields() (src/FDTD_kokkos/FDTD_kokkos.cpp:91-104):
- * one full step B/2, E, B/2.  Asynchronous on the handle's stream. */
+ * one full step B/2, E, B/2.  Asynchronous on the handle's stream.
+ * In the FP32-arithmetic forms with the default fused pipeline a step is one
+ * sweep (B half steps, then E): the trailing B/2 of the step is applied by
+ * the next step's sweep, together with that step's leading B/2.  Every entry
+ * point that reads B (copies, exports, field sums) sees it applied, and every
+ * one that writes E or B applies it first, so a sequence of update_fields
+ * calls, with or without reads in between, gives the bits of fdtd_step(n). */
 int fdtd_update_fields(fdtd_handle* h);
 
 /* n consecutive update_fields() calls, scheduled as one sequence (the two B
@@ -196,6 +202,15 @@ int fdtd_synchronize(fdtd_handle* h);
 enum fdtd_fp64_arith { FDTD_FP64_BITWISE = 0, FDTD_FP64_CONTRACTED = 1 };
 int fdtd_set_fp64_arith(fdtd_handle* h, int arith);
 
+/* Test hook of the bounded device waits (new).  The fused sweeps' waits on
+ * their tile loads give up after `polls` polls (0: the default, 2^24) and
+ * then stop the sweep: every CTA leaves its tile loop, waits (bounded) for
+ * its copies in flight and exits; fdtd_synchronize then reports
+ * FDTD_ERR_TIMEOUT and the step's results are invalid.  withhold_loads != 0
+ * makes the sweeps issue no tile loads at all, so that every wait gives up
+ * with no copy in flight: the way to exercise that path without a fault. */
+int fdtd_set_wait_limit(fdtd_handle* h, int64_t polls, int withhold_loads);
+
 /* Measured issue rate of the FP64 pipe of the current device (new; the
  * roofline of the FP64 sweeps): independent DMUL/DADD chains on every SM,
  * timed with CUDA events.  Synchronous; about 50 ms. */
@@ -204,6 +219,20 @@ int fdtd_measure_fp64_rate(double* dp_instr_per_s, double* ms);
 /* Per-component power-of-two scales of the FP16_SCALED form: stored value =
  * field * 2^exponent.  `exponents` has 6 entries (Ex..Bz), each in [-60, 60]. */
 int fdtd_set_fp16_exponents(fdtd_handle* h, const int exponents[6]);
+int fdtd_get_fp16_exponents(fdtd_handle* h, int exponents[6]);
+/* Exponents chosen by the engine (new).  fdtd_fp16_autoscale scans the
+ * stored peak of each component now and re-encodes every component with a
+ * nonzero peak so that it lies in (2^(target_log2-1), 2^target_log2]
+ * (target_log2 in [0, 15]; 12 leaves 16x of growth below FP16's largest
+ * value); the chosen exponents go to `exponents` if non-null.
+ * fdtd_set_fp16_autoscale makes fdtd_step scan every `every_steps` steps
+ * (0: never) and re-encode the components whose peak left
+ * [2^(target_log2-4), 2^(target_log2+2)].  Re-encoding multiplies stored
+ * values by a power of two, which commutes with the FP32 arithmetic on them:
+ * results change only where a value would otherwise have left FP16's normal
+ * range.  Each scan synchronises the handle's stream. */
+int fdtd_fp16_autoscale(fdtd_handle* h, int target_log2, int exponents[6]);
+int fdtd_set_fp16_autoscale(fdtd_handle* h, int every_steps, int target_log2);
 
 /* Kernel timing (new; for roofline accounting).  While enabled, every kernel
  * launch of the step pipeline is bracketed by CUDA events on the handle's
@@ -254,12 +283,14 @@ int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out);
  * holds n independent periodic domains of any sizes on one GPU, stored in an
  * FP32-arithmetic form (FP32, FP32_COMP or FP16_SCALED), all with the same
  * dt.  fdtd_batch_step(b, n) advances every domain by n update_fields steps:
- * one launch does the leading B half step of every domain, then each fused
- * sweep of all domains is one persistent kernel launch that works through a
- * per-domain tile table; the whole step group runs as one CUDA graph
- * (captured on first use for each step count, then replayed).  Each domain's
- * results are bit-identical to a single-domain handle of the same form run
- * alone.  Domains take analytic sources only (no dense J arrays).
+ * each B-first fused sweep of all domains is one persistent kernel launch
+ * that works through a per-domain tile table, and the whole step group runs
+ * as one CUDA graph (captured on first use for each step count, then
+ * replayed).  As on a single handle, the last step's trailing B half step is
+ * applied by the next group's first sweep; domain reads see it applied and
+ * domain writes apply it first (to every domain).  Each domain's results are
+ * bit-identical to a single-domain handle of the same form run alone with
+ * the same step calls.  Domains take analytic sources only (no dense J arrays).
  * Not thread-safe per batch. */
 typedef struct fdtd_batch fdtd_batch;
 
@@ -305,8 +336,9 @@ int fdtd_batch_synchronize(fdtd_batch* b);
  * 65536 block partials built into the library (5 MiB per device that loads
  * it, held until exit), which caps `cells` at 268,435,456; larger grids give
  * FDTD_ERR_INVALID_ARGUMENT.  The first call on a device resolves that array's
- * device address (make it before any stream capture).  Calls share the array:
- * calls that overlap on the GPU race. */
+ * device address (make it before any stream capture); later calls resolve it
+ * again unless their stream is capturing, so a reset device context is
+ * followed.  Calls share the array: calls that overlap on the GPU race. */
 int fdtd_field_sums_noalloc(const double* const fields[6], int64_t cells, double* out_device, void* stream);
 
 /* ------------------------------------------------------------------------
@@ -339,9 +371,11 @@ int fdtd_sync(fdtd_handle* h);
  *
  * A set of slabs that tile the planes in order (k_begin of the first 0, each
  * k_end the next k_begin, the last k_end Nk) steps like one handle of the
- * whole grid when every slab runs, per update_fields,
- *     B_HALF (B_DOUBLE between steps), exchange B, E, exchange E, B_HALF,
- * and exchange E once before the first B sweep (after the fields were set):
+ * whole grid when every slab runs, per call of n update_fields steps,
+ *     exchange E, B_HALF (B_DOUBLE if the previous call left a half step
+ *     pending), then per step: exchange B, E, exchange E, B_DOUBLE between
+ *     steps and after the last one B_DEFER (FP32-arithmetic forms; B_HALF in
+ *     the FP64 form):
  * the results are the whole-grid handle's bit for bit, in every precision.
  * fdtd_step on a slab gives FDTD_ERR_UNSUPPORTED; slabs run the split sweeps
  * (no fused pipeline, no autotuner) and have no PML.
@@ -358,9 +392,16 @@ int fdtd_slab_info(fdtd_handle* h, int* k_begin, int* k_end, int* nk_global);
 enum fdtd_sweep {
     FDTD_SWEEP_B_HALF = 0,   /* B += curl term (kokkos_functors.h:128-151), once  */
     FDTD_SWEEP_B_DOUBLE = 1, /* the same term added twice (two half steps)        */
-    FDTD_SWEEP_E = 2         /* E update of the current step; the step count + 1  */
+    FDTD_SWEEP_E = 2,        /* E update of the current step; the step count + 1  */
+    FDTD_SWEEP_B_DEFER = 3   /* no sweep: the step's trailing B half is left
+                                pending (FP32-arithmetic forms), as fdtd_step
+                                leaves it; the next B_DOUBLE sweep applies it
+                                with the next step's leading half, readers of
+                                B see it applied, writers apply it first      */
 };
-/* One sweep over the owned planes (any non-PML handle: the whole grid). */
+/* One sweep over the owned planes (any non-PML handle: the whole grid).  With
+ * a B half step pending, B_HALF applies it and B_DOUBLE applies it and one
+ * more; E applies it first. */
 int fdtd_slab_sweep(fdtd_handle* h, int sweep);
 
 enum fdtd_plane {

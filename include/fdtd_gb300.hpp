@@ -211,7 +211,7 @@ class FDTD_PML : public FDTD {
 class Slabs {
  public:
   Slabs(Parameters parameters, FP dt, int n_slabs, Precision precision = Precision::FP64)
-      : parameters_(parameters) {
+      : parameters_(parameters), defer_(precision != Precision::FP64) {
     if (n_slabs <= 0 || n_slabs > parameters.Nk) throw std::invalid_argument("need 1 <= slabs <= Nk");
     fdtd_params p{parameters.Ni, parameters.Nj, parameters.Nk, parameters.ax, parameters.bx, parameters.ay,
                   parameters.by, parameters.az, parameters.bz, parameters.dx, parameters.dy, parameters.dz};
@@ -245,17 +245,20 @@ class Slabs {
   }
   // n update_fields steps: exchange E, B/2, then per step exchange B, E,
   // exchange E, B (the trailing and leading B halves of consecutive steps in
-  // one sweep).
+  // one sweep).  The FP32-arithmetic forms leave the last step's trailing
+  // half pending, as a whole-grid handle does, and the next call's first
+  // sweep applies it with that call's leading half.
   void step(int64_t n) {
     if (n <= 0) return;
     exchange(FDTD_HALO_E);
-    sweep(FDTD_SWEEP_B_HALF);
+    sweep(pending_ ? FDTD_SWEEP_B_DOUBLE : FDTD_SWEEP_B_HALF);
     for (int64_t s = 0; s < n; ++s) {
       exchange(FDTD_HALO_B);
       sweep(FDTD_SWEEP_E);
       exchange(FDTD_HALO_E);
-      sweep(s + 1 < n ? FDTD_SWEEP_B_DOUBLE : FDTD_SWEEP_B_HALF);
+      sweep(s + 1 < n ? FDTD_SWEEP_B_DOUBLE : (defer_ ? FDTD_SWEEP_B_DEFER : FDTD_SWEEP_B_HALF));
     }
+    pending_ = defer_;
   }
   void fence() {
     for (fdtd_handle* h : slabs_) check(fdtd_synchronize(h));
@@ -272,6 +275,7 @@ class Slabs {
     for (std::size_t s = 0; s < slabs_.size(); ++s)
       check(fdtd_copy_field_from_host(slabs_[s], static_cast<int>(c), host + plane * bounds_[s].first,
                                       plane * (bounds_[s].second - bounds_[s].first)));
+    if (static_cast<int>(c) < FDTD_JX) pending_ = false;  // each slab applied its pending half first
   }
   const Parameters& parameters() const { return parameters_; }
 
@@ -285,6 +289,8 @@ class Slabs {
     slabs_.clear();
   }
   Parameters parameters_;
+  bool defer_;            // leave the last trailing B half pending (not FP64)
+  bool pending_ = false;  // a trailing B half step is pending on every slab
   std::vector<fdtd_handle*> slabs_;
   std::vector<std::pair<int, int>> bounds_;
 };

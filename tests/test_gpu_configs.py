@@ -6,8 +6,9 @@
   energy drift).
 * 1536 x 1536 x 1024 periodic grid (2.4e9 cells, past the reference's int32
   indexing), 16 pulses, 1000 steps: FP16 storage with per-component
-  power-of-two scales against plain FP32 on the same GPU, and the same 16
-  pulses rerun on 256^3 in FP16 against the FP64 form.
+  power-of-two scales chosen by the engine (rescans every 25 steps) against
+  plain FP32 on the same GPU, and the same 16 pulses rerun on 256^3 in FP16
+  against the FP64 form.
 
 Fields are compared on the device through fdtd_export_field; torch only
 holds the FP64 comparison buffers."""
@@ -22,7 +23,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 CHUNK = 1 << 27  # cells per comparison chunk (1 GiB of FP64 per buffer)
-FP16_EXPONENTS = [6] * 6
+AUTOSCALE_EVERY = 25  # steps between the FP16 form's range checks
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -90,7 +91,7 @@ def test_fp16_1536x1536x1024_16_pulses_1000_steps():
     steps = 1000
     srcs = sources.random_pulses(p, 16, seed=0, n_steps=steps, comps=("z", "x"))
     half = FDTD(p, COURANT_DT, Precision.FP16_SCALED)
-    half.set_fp16_exponents(FP16_EXPONENTS)
+    half.set_fp16_autoscale(AUTOSCALE_EVERY)
     single = FDTD(p, COURANT_DT, Precision.FP32)
     for s in (half, single):
         for q in srcs:
@@ -99,8 +100,11 @@ def test_fp16_1536x1536x1024_16_pulses_1000_steps():
         s.step(steps)
     num, den = sq_sums(single, half, p.cells)
     total, per = rel_l2(num, den)
-    print("1536x1536x1024 FP16_SCALED vs FP32: rel-L2 %.3e per component %s" % (total, ["%.2e" % x for x in per]))
+    exps = half.fp16_exponents()
+    print("1536x1536x1024 FP16_SCALED vs FP32: rel-L2 %.3e per component %s, exponents %s"
+          % (total, ["%.2e" % x for x in per], exps))
     assert total <= 5e-2
+    assert len(set(exps)) > 1
     half.close()
     single.close()
 
@@ -109,7 +113,7 @@ def test_fp16_1536x1536x1024_16_pulses_1000_steps():
     small = _scaled_pulses(srcs, p, q)
     ref = FDTD(q, COURANT_DT, Precision.FP64)
     h16 = FDTD(q, COURANT_DT, Precision.FP16_SCALED)
-    h16.set_fp16_exponents(FP16_EXPONENTS)
+    h16.set_fp16_autoscale(AUTOSCALE_EVERY)
     for s in (ref, h16):
         for x in small:
             s.add_source(x)

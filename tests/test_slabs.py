@@ -59,6 +59,18 @@ def test_schedule_matches_the_reference_step_order():
     assert slabs.step_schedule(0) == []
 
 
+def test_schedule_with_a_pending_half_step():
+    """FP32-arithmetic slabs leave the last trailing B half pending (as a
+    whole-grid handle does): two calls of 2 steps make the sweeps of one call
+    of 4, the pending half becoming the first half of the second call's
+    double sweep."""
+    first = [a for op, a in slabs.step_schedule(2, defer=True) if op == "sweep"]
+    second = [a for op, a in slabs.step_schedule(2, defer=True, pending=True) if op == "sweep"]
+    whole = [a for op, a in slabs.step_schedule(4, defer=True) if op == "sweep"]
+    assert first[-1] == slabs.SWEEP_B_DEFER and second[0] == slabs.SWEEP_B_DOUBLE
+    assert first[:-1] + second == whole
+
+
 def _initial_fields(p, seed):
     rng = np.random.default_rng(seed)
     n = p.Ni * p.Nj * p.Nk

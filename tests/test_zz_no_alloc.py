@@ -48,6 +48,43 @@ def test_noalloc_field_sums_match_handle_entry_point_twice():
         assert got[9] == want[9] == 0
 
 
+def test_noalloc_many_partials_non_finite_values_and_a_stream():
+    """128^3 cells give 512 block partials, so the second pass folds more
+    slots than it has threads; NaN and Inf values are counted; the call runs
+    on a stream of the caller's."""
+    torch = pytest.importorskip("torch")
+    build.build()
+    lib = _lib.load()
+    p = normalised_parameters(128, 128, 128)
+    sim = FDTD(p, COURANT_DT)
+    rng = np.random.default_rng(7)
+    vals = [rng.standard_normal(p.cells) for _ in range(6)]
+    for c in range(6):
+        sim.get_field(c).assign(vals[c])
+    want = sim.field_sums()
+    ptrs = (ctypes.c_void_p * 6)(*[sim.get_field(c).device_ptr for c in range(6)])
+    stream = torch.cuda.Stream()
+    out = _device_out(torch)
+    rc = lib.fdtd_field_sums_noalloc(ptrs, p.cells, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+    assert rc == 0, lib.fdtd_last_error()
+    stream.synchronize()
+    got = out.cpu().numpy()
+    np.testing.assert_allclose(got[:6], want[:6], rtol=1e-12)
+    scale = float(np.abs(want[:6]).sum())
+    np.testing.assert_allclose(got[6:9], want[6:9], rtol=1e-9, atol=1e-12 * scale)
+    assert got[9] == 0
+    vals[2][12345] = np.nan
+    vals[4][0] = np.inf
+    vals[4][p.cells - 1] = -np.inf
+    sim.get_field(2).assign(vals[2])
+    sim.get_field(4).assign(vals[4])
+    sim.synchronize()
+    rc = lib.fdtd_field_sums_noalloc(ptrs, p.cells, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+    assert rc == 0, lib.fdtd_last_error()
+    stream.synchronize()
+    assert out.cpu().numpy()[9] == 3 == sim.field_sums()[9]
+
+
 def test_noalloc_rejects_grids_beyond_its_scratch():
     torch = pytest.importorskip("torch")
     build.build()
