@@ -95,8 +95,8 @@ SIGNATURES = {
     "fdtd_set_fp16_exponents": [_H, ctypes.POINTER(ctypes.c_int)],
     "fdtd_set_fp64_arith": [_H, ctypes.c_int],
     "fdtd_get_fp16_exponents": [_H, ctypes.POINTER(ctypes.c_int)],
-    "fdtd_fp16_autoscale": [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
-    "fdtd_set_fp16_autoscale": [_H, ctypes.c_int, ctypes.c_int],
+    "fdtd_fp16_autoscale": [_H, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
+    "fdtd_set_fp16_autoscale": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "fdtd_set_wait_limit": [_H, ctypes.c_int64, ctypes.c_int],
     "fdtd_measure_fp64_rate": [_D, _D],
     "fdtd_set_kernel_timing": [_H, ctypes.c_int],

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -375,9 +376,30 @@ int ensure_alt(fdtd_handle* h) {
   if (h->maps_tile_y != key) {
     const HiType ht = h->form == Form::F16 ? HiType::F16 : HiType::F32;
     const bool two = h->fused_cfg.cells_per_thread == 2;
-    const int bw = h->form == Form::F16 ? (two ? fused_box_width<StoreF16>() : fused1_box_width<StoreF16>())
-                                        : (two ? fused_box_width<StoreF32>() : fused1_box_width<StoreF32>());
-    const int lbw = two ? fused_lo_box_width() : fused1_lo_box_width();
+    // box widths per component: the two-cell kernel's are uniform; the
+    // one-cell kernel's depend on the sweep order
+    int bw[6], lbw[6], bbw[6], blbw[6];
+    if (two) {
+      for (int c = 0; c < 6; ++c) {
+        bw[c] = h->form == Form::F16 ? fused_box_width<StoreF16>() : fused_box_width<StoreF32>();
+        lbw[c] = fused_lo_box_width();
+      }
+    } else {
+      switch (h->form) {
+        case Form::F16:
+          fused1_box_widths<StoreF16>(false, bw, lbw);
+          fused1_box_widths<StoreF16>(true, bbw, blbw);
+          break;
+        case Form::F32C:
+          fused1_box_widths<StoreF32C>(false, bw, lbw);
+          fused1_box_widths<StoreF32C>(true, bbw, blbw);
+          break;
+        default:
+          fused1_box_widths<StoreF32>(false, bw, lbw);
+          fused1_box_widths<StoreF32>(true, bbw, blbw);
+          break;
+      }
+    }
     LoT* const* lo_cur = h->form == Form::F32C ? h->lo : nullptr;
     LoT* const* lo_alt = h->form == Form::F32C ? h->alt_lo : nullptr;
     const int ty = h->fused_cfg.tile_y;
@@ -385,11 +407,11 @@ int ensure_alt(fdtd_handle* h) {
     if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, lbw, ty, trim) != cudaSuccess ||
         build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, ty, trim) != cudaSuccess)
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
-    if (!two && (build_tma_maps(&h->bmaps_cur, h->L, ht, h->field, lo_cur, bw, lbw, ty, BoxTrim::BFirst) != cudaSuccess ||
-                 build_tma_maps(&h->bmaps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, ty, BoxTrim::BFirst) != cudaSuccess))
+    if (!two && (build_tma_maps(&h->bmaps_cur, h->L, ht, h->field, lo_cur, bbw, blbw, ty, BoxTrim::BFirst) != cudaSuccess ||
+                 build_tma_maps(&h->bmaps_alt, h->L, ht, h->alt_field, lo_alt, bbw, blbw, ty, BoxTrim::BFirst) != cudaSuccess))
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
-    if (!two && (build_tma_store_maps(&h->smaps_cur, h->L, ht, h->field, lo_cur, h->fused_cfg.tile_y) != cudaSuccess ||
-                 build_tma_store_maps(&h->smaps_alt, h->L, ht, h->alt_field, lo_alt, h->fused_cfg.tile_y) != cudaSuccess))
+    if (!two && (build_tma_store_maps(&h->smaps_cur, h->L, ht, h->field, lo_cur, ty) != cudaSuccess ||
+                 build_tma_store_maps(&h->smaps_alt, h->L, ht, h->alt_field, lo_alt, ty) != cudaSuccess))
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
     h->maps_tile_y = key;
   }
@@ -413,8 +435,11 @@ int read_view(fdtd_handle* h, StateView* v) {
   }
   if (!h->b_side) {
     // B with the pending half step, into the second copy's B arrays (the next
-    // sweep overwrites that copy anyway); a z slab uses side arrays, and its
-    // halo plane above holds the neighbour's E from the last exchange.
+    // sweep overwrites that copy anyway; split sweeps may not have made it
+    // yet); a z slab uses side arrays, and its halo plane above holds the
+    // neighbour's E from the last exchange.
+    if (!h->zhalo)
+      if (int rc = ensure_alt(h)) return rc;
     if (h->zhalo && !h->side_b[0]) {
       const int64_t n = h->L.elems() + 2 * h->halo_elems();
       for (int c = 0; c < 3; ++c) {
@@ -745,30 +770,43 @@ int step_sweeps(fdtd_handle* h, int64_t n) {
   return FDTD_OK;
 }
 
-// FP16 range check (fdtd_set_fp16_autoscale): re-encodes every component
-// whose stored peak left [2^(target-4), 2^(target+2)] so that it sits in
-// (2^(target-1), 2^target]; `force` re-encodes every component with a
-// nonzero, finite peak.  Synchronous (reads six maxima).
-int fp16_rescan(fdtd_handle* h, int target, bool force, int out[6]) {
+// FP16 exponents (fdtd_fp16_autoscale, fdtd_set_fp16_autoscale).  From the
+// stored peaks m_c, the field peak of component c is below 2^k_c with
+// k_c = ceil(log2 m_c) - e_c, and k_all = max k_c.  The wanted exponent puts
+// the component's peak at 2^target, but never more than 2^headroom above the
+// strongest component's scale: e*_c = min(target - k_c, target + headroom -
+// k_all) (a component with no field gets the bound).  `force` sets every
+// exponent to e*; otherwise a component is re-encoded when its exponent is
+// above the bound or 3 or more from e*.  Synchronous (reads six maxima).
+int fp16_rescan(fdtd_handle* h, int target, int headroom, bool force, int out[6]) {
   unsigned* d_max = reinterpret_cast<unsigned*>(h->d_diag_out);
   FDTD_CUDA(launch_f16_absmax(h->L, h->view().s16, d_max, h->stream), "FP16 peak scan");
   unsigned bits[6];
   FDTD_CUDA(cudaMemcpyAsync(bits, d_max, sizeof(bits), cudaMemcpyDeviceToHost, h->stream), "FP16 peak scan");
   FDTD_CUDA(cudaStreamSynchronize(h->stream), "FP16 peak scan");
+  int k[6];
+  bool has[6];
+  int k_all = INT_MIN;
   for (int c = 0; c < 6; ++c) {
     float m;
     std::memcpy(&m, &bits[c], sizeof(m));
+    has[c] = m > 0.f && std::isfinite(m);
+    k[c] = has[c] ? (int)std::ceil(std::log2((double)m)) - h->fp16_exp[c] : 0;
+    if (has[c]) k_all = std::max(k_all, k[c]);
+  }
+  for (int c = 0; c < 6; ++c) {
     if (out) out[c] = h->fp16_exp[c];
-    if (!(m > 0.f) || !std::isfinite(m)) continue;
-    const int k = (int)std::ceil(std::log2((double)m));  // stored peak <= 2^k
-    if (!force && k >= target - 4 && k <= target + 2) continue;
-    const int e_new = std::max(-60, std::min(60, h->fp16_exp[c] + target - k));
-    const int shift = e_new - h->fp16_exp[c];
-    if (shift == 0) continue;
-    FDTD_CUDA(launch_f16_rescale(static_cast<__half*>(h->field[c]), h->L.elems(), shift, h->stream), "FP16 rescale");
-    h->fp16_exp[c] = e_new;
+    if (k_all == INT_MIN) continue;  // no field anywhere: nothing to go by
+    const int bound = target + headroom - k_all;
+    const int want = std::max(-60, std::min(60, has[c] ? std::min(target - k[c], bound) : bound));
+    const int cur = h->fp16_exp[c];
+    if (!force && cur <= bound && std::abs(want - cur) < 3) continue;
+    if (want == cur) continue;
+    FDTD_CUDA(launch_f16_rescale(static_cast<__half*>(h->field[c]), h->L.elems(), want - cur, h->stream),
+              "FP16 rescale");
+    h->fp16_exp[c] = want;
     h->b_side = false;
-    if (out) out[c] = e_new;
+    if (out) out[c] = want;
   }
   return FDTD_OK;
 }
@@ -792,7 +830,7 @@ int fdtd_step(fdtd_handle* h, int64_t n) {
     n -= m;
     if (every > 0 && (h->fp16_autoscale_count += (int)m) >= every) {
       h->fp16_autoscale_count = 0;
-      if (int rc = fp16_rescan(h, h->fp16_autoscale_target, false, nullptr)) return rc;
+      if (int rc = fp16_rescan(h, h->fp16_autoscale_target, h->fp16_autoscale_headroom, false, nullptr)) return rc;
     }
   }
   return FDTD_OK;
@@ -1155,23 +1193,26 @@ int fdtd_synchronize(fdtd_handle* h) {
   return FDTD_OK;
 }
 
-int fdtd_fp16_autoscale(fdtd_handle* h, int target_log2, int exponents[6]) {
+int fdtd_fp16_autoscale(fdtd_handle* h, int target_log2, int headroom_log2, int exponents[6]) {
   if (int rc = check_handle(h)) return rc;
   if (h->form != Form::F16) return fail(FDTD_ERR_UNSUPPORTED, "scales apply to the FP16_SCALED form only");
   if (target_log2 < 0 || target_log2 > 15) return fail(FDTD_ERR_INVALID_ARGUMENT, "target_log2 must be in [0, 15]");
+  if (headroom_log2 < 0 || headroom_log2 > 60) return fail(FDTD_ERR_INVALID_ARGUMENT, "headroom_log2 must be in [0, 60]");
   DeviceGuard dg(h->device);
-  if (int rc = fp16_rescan(h, target_log2, true, exponents)) return rc;
+  if (int rc = fp16_rescan(h, target_log2, headroom_log2, true, exponents)) return rc;
   FDTD_CUDA(cudaStreamSynchronize(h->stream), "FP16 rescale");
   return FDTD_OK;
 }
 
-int fdtd_set_fp16_autoscale(fdtd_handle* h, int every_steps, int target_log2) {
+int fdtd_set_fp16_autoscale(fdtd_handle* h, int every_steps, int target_log2, int headroom_log2) {
   if (int rc = check_handle(h)) return rc;
   if (h->form != Form::F16) return fail(FDTD_ERR_UNSUPPORTED, "scales apply to the FP16_SCALED form only");
   if (every_steps < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "every_steps must be >= 0");
   if (target_log2 < 0 || target_log2 > 15) return fail(FDTD_ERR_INVALID_ARGUMENT, "target_log2 must be in [0, 15]");
+  if (headroom_log2 < 0 || headroom_log2 > 60) return fail(FDTD_ERR_INVALID_ARGUMENT, "headroom_log2 must be in [0, 60]");
   h->fp16_autoscale_every = every_steps;
   h->fp16_autoscale_target = target_log2;
+  h->fp16_autoscale_headroom = headroom_log2;
   h->fp16_autoscale_count = 0;
   return FDTD_OK;
 }

@@ -131,9 +131,10 @@ cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const
                               const float* const J[3], bool dense_j, const CoefSet& cs,
                               const SourceSet& ss, int64_t step, int applications,
                               const FusedConfig& cfg, bool b_first, const WaitCtl& wc, cudaStream_t stream);
+// Per-component box widths (hi and lo words) of the one-cell kernel's load
+// maps, for its E-first or B-first sweep.
 template <class S>
-int fused1_box_width();
-int fused1_lo_box_width();
+void fused1_box_widths(bool b_first, int hi[6], int lo[6]);
 
 // Batched form: one record per domain in device memory (its layout, its two
 // state copies, coefficients and sources).
@@ -179,7 +180,7 @@ cudaError_t build_tma_store_maps(void* maps, const PLayout& L, HiType ht, void* 
 // and the others tile_y + 1 (the row below).
 enum class BoxTrim { None, EFirst, BFirst };
 cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6],
-                           LoT* const lo[6], int box_w, int lo_box_w, int tile_y, BoxTrim trim);
+                           LoT* const lo[6], const int box_w[6], const int lo_box_w[6], int tile_y, BoxTrim trim);
 
 // misc.cu — conversions, diagnostics, small helpers.
 enum class Form { F64 = 0, F32 = 1, F32C = 2, F16 = 3 };

@@ -66,7 +66,8 @@ struct fdtd_handle {
   // FP16 range checks (fdtd_set_fp16_autoscale): every n steps (0: off) the
   // stored peaks are scanned and components re-encoded around 2^target.
   int fp16_autoscale_every = 0;
-  int fp16_autoscale_target = 12;
+  int fp16_autoscale_target = 10;
+  int fp16_autoscale_headroom = 5;
   int fp16_autoscale_count = 0;  // steps since the last check
 
   // Sources.

@@ -131,17 +131,17 @@ __global__ void __launch_bounds__(256) e_update_fp64(Grid g, Box b, const double
     const double by_ip = By[col_ip + base];
     const double bx_jp = Bx[col_jp + base];
 
-    bool has_j = false;
-    double jx = 0.0, jy = 0.0, jz = 0.0;
-    if (kDenseJ) {
-      jx = Jx[col + base];
-      jy = Jy[col + base];
-      jz = Jz[col + base];
-      has_j = true;
-    }
-    if (kSources) has_j |= source_current(ss, s, i, j, k, g, jx, jy, jz);
     if (kFma) {
       // E + cJ J + c1 d1 - c2 d2 as DFMAs into E
+      bool has_j = false;
+      double jx = 0.0, jy = 0.0, jz = 0.0;
+      if (kDenseJ) {
+        jx = Jx[col + base];
+        jy = Jy[col + base];
+        jz = Jz[col + base];
+        has_j = true;
+      }
+      if (kSources) has_j |= source_current(ss, s, i, j, k, g, jx, jy, jz);
       double ex = Ex[col + base], ey = Ey[col + base], ez = Ez[col + base];
       if (has_j) {
         ex = __fma_rn(cJ, jx, ex);
@@ -159,6 +159,16 @@ __global__ void __launch_bounds__(256) e_update_fp64(Grid g, Box b, const double
     double tx = DSUB(DMUL(cy, DSUB(bz, bz_jp)), DMUL(cz, DSUB(by, by_kp)));
     double ty = DSUB(DMUL(cz, DSUB(bx, bx_kp)), DMUL(cx, DSUB(bz, bz_ip)));
     double tz = DSUB(DMUL(cx, DSUB(by, by_ip)), DMUL(cy, DSUB(bx, bx_jp)));
+
+    bool has_j = false;
+    double jx = 0.0, jy = 0.0, jz = 0.0;
+    if (kDenseJ) {
+      jx = Jx[col + base];
+      jy = Jy[col + base];
+      jz = Jz[col + base];
+      has_j = true;
+    }
+    if (kSources) has_j |= source_current(ss, s, i, j, k, g, jx, jy, jz);
     if (has_j) {
       // (cJ*J + c1*d1) - c2*d2, the reference's association.
       tx = DSUB(DADD(DMUL(cJ, jx), DMUL(cy, DSUB(bz, bz_jp))), DMUL(cz, DSUB(by, by_kp)));

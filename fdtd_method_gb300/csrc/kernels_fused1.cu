@@ -71,10 +71,15 @@ template <> struct ArithOf1<StoreF32C> { using type = ArithComp; };
 constexpr int kStages1 = 3;
 constexpr int kLoOff1 = 8;  // BF16 lo boxes start 8 columns left of the tile
 
+// Box widths (elements) and the left offset of the boxes that hold the
+// column left of the tile.  kW / kLoW reach the column right of the tile
+// (x0+32); the B-first sweep's Ex and B boxes need no column right of the
+// tile and take the narrower kWs / kLoWs (one 32-byte sector less per row).
+// Every start and width keeps rows on 16-byte boundaries.
 template <class S> struct Box1;
-template <> struct Box1<StoreF32> { static constexpr int kW = 40, kOff = 4, kLoW = 0; };
-template <> struct Box1<StoreF32C> { static constexpr int kW = 40, kOff = 4, kLoW = 48; };
-template <> struct Box1<StoreF16> { static constexpr int kW = 48, kOff = 8, kLoW = 0; };
+template <> struct Box1<StoreF32> { static constexpr int kW = 40, kWs = 36, kOff = 4, kLoW = 0, kLoWs = 0; };
+template <> struct Box1<StoreF32C> { static constexpr int kW = 40, kWs = 36, kOff = 4, kLoW = 48, kLoWs = 40; };
+template <> struct Box1<StoreF16> { static constexpr int kW = 48, kWs = 40, kOff = 8, kLoW = 0, kLoWs = 0; };
 
 constexpr int round128(int b) { return (b + 127) / 128 * 128; }
 
@@ -103,11 +108,13 @@ constexpr int kMinCtas1 = RY == 30 ? 1 : 2;
 struct BoxTable {
   int hi[7], lo[7];    // byte offsets ([6]: end of the hi / lo boxes)
   int rows[6], row0[6], xoff[6], lxoff[6];
+  int w[6], lw[6];     // box widths (elements)
   unsigned tx;         // bytes the six (twelve) copies write
   int stage;           // stage size, 128-byte multiple
 };
 
-constexpr BoxTable box_table(int RY, int W, int LW, int HS, int LS, bool lo, int off, int lo_off, bool bfirst) {
+constexpr BoxTable box_table(int RY, int W, int Ws, int LW, int LWs, int HS, int LS, bool lo, int off, int lo_off,
+                             bool bfirst) {
   BoxTable b{};
   int at = 0;
   unsigned tx = 0;
@@ -115,30 +122,36 @@ constexpr BoxTable box_table(int RY, int W, int LW, int HS, int LS, bool lo, int
     if (bfirst) {
       // every box starts at the row below and the column left of the tile
       // (the halo warps' cells); Ex and Ez also hold the row above (B'z and
-      // B'x read them at j+1).  Box row 0 is y0-1.
+      // B'x read them at j+1), Ey and Ez the column right of it (B'z and B'y
+      // read them at i+1).  Box row 0 is y0-1.
       b.rows[c] = (c == 0 || c == 2) ? RY + 2 : RY + 1;
       b.row0[c] = 0;
       b.xoff[c] = off;
       b.lxoff[c] = lo_off;
+      const bool right = (c == 1 || c == 2);
+      b.w[c] = right ? W : Ws;
+      b.lw[c] = right ? LW : LWs;
     } else {
       const bool below = (c == 3 || c == 5), left = (c == 4 || c == 5);
       b.rows[c] = below ? RY + 2 : RY + 1;
       b.row0[c] = below ? 0 : 1;
       b.xoff[c] = left ? off : 0;
       b.lxoff[c] = left ? lo_off : 0;
+      b.w[c] = W;
+      b.lw[c] = LW;
     }
   }
   for (int c = 0; c < 6; ++c) {
     b.hi[c] = at;
-    at = (at + b.rows[c] * W * HS + 127) / 128 * 128;
-    tx += (unsigned)(b.rows[c] * W * HS);
+    at = (at + b.rows[c] * b.w[c] * HS + 127) / 128 * 128;
+    tx += (unsigned)(b.rows[c] * b.w[c] * HS);
   }
   b.hi[6] = at;
   for (int c = 0; c < 6; ++c) {
     b.lo[c] = at;
     if (lo) {
-      at = (at + b.rows[c] * LW * LS + 127) / 128 * 128;
-      tx += (unsigned)(b.rows[c] * LW * LS);
+      at = (at + b.rows[c] * b.lw[c] * LS + 127) / 128 * 128;
+      tx += (unsigned)(b.rows[c] * b.lw[c] * LS);
     }
   }
   b.lo[6] = at;
@@ -155,6 +168,7 @@ struct Plan1 {
   static constexpr bool kLo = S::kComp;
   static constexpr int ROWS = RY + 2;
   static constexpr int W = Box1<S>::kW, LW = Box1<S>::kLoW, OFF = Box1<S>::kOff;
+  static constexpr int Ws = Box1<S>::kWs, LWs = Box1<S>::kLoWs;
   static constexpr int HS = (int)sizeof(HiT), LS = (int)sizeof(LoT);
   // Ring stage: 6 hi boxes, then 6 lo boxes.  Each component's box holds
   // only the halos its stencil reads.  E-first: the column left of the tile
@@ -165,14 +179,16 @@ struct Plan1 {
   // Every box starts on a 128-byte boundary, as tensor copies require.
   // Per-component scalars of the table (device code may use scalar
   // constants, not the table object).
-  static constexpr BoxTable box() { return box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF); }
-  template <int c> static constexpr int kHiAt = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).hi[c];
-  template <int c> static constexpr int kLoAt = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).lo[c];
-  template <int c> static constexpr int kRow0 = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).row0[c];
-  template <int c> static constexpr int kXOff = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).xoff[c];
-  template <int c> static constexpr int kLXOff = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).lxoff[c];
-  static constexpr uint32_t kTx = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).tx;
-  static constexpr int kStage = box_table(RY, W, LW, HS, LS, kLo, OFF, kLoOff1, BF).stage;
+  static constexpr BoxTable box() { return box_table(RY, W, Ws, LW, LWs, HS, LS, kLo, OFF, kLoOff1, BF); }
+  template <int c> static constexpr int kHiAt = box().hi[c];
+  template <int c> static constexpr int kLoAt = box().lo[c];
+  template <int c> static constexpr int kRow0 = box().row0[c];
+  template <int c> static constexpr int kXOff = box().xoff[c];
+  template <int c> static constexpr int kLXOff = box().lxoff[c];
+  template <int c> static constexpr int kW = box().w[c];
+  template <int c> static constexpr int kLW = box().lw[c];
+  static constexpr uint32_t kTx = box().tx;
+  static constexpr int kStage = box().stage;
   // Exchange / staging buffer of the first half-sweep's field (E' in the
   // E-first sweep, B' in the B-first one): per component RY+2 rows of 32
   // (rows 0..RY-1 the tile, row RY the halo row, row RY+1 the halo column by
@@ -195,6 +211,10 @@ struct Plan1 {
   // The box the B-first sweep's halo column reads starts one column left of
   // the tile, inside every box's left offset.
   static_assert(!BF || (OFF >= 1 && (!kLo || kLoOff1 >= 1)), "B-first boxes need the left halo column");
+  static_assert(Ws - OFF >= 32 && (!kLo || LWs - kLoOff1 >= 32) && W - OFF >= 33 && (!kLo || LW - kLoOff1 >= 33),
+                "boxes must reach the tile's last column (and the one right of it)");
+  static_assert((Ws * HS) % 16 == 0 && (W * HS) % 16 == 0 && (LWs * LS) % 16 == 0 && (LW * LS) % 16 == 0,
+                "box rows must be whole 16-byte units");
   static_assert(box().hi[1] % 128 == 0 && box().hi[5] % 128 == 0 && box().lo[0] % 128 == 0 &&
                     box().lo[5] % 128 == 0,
                 "ring boxes must start on 128-byte boundaries");
@@ -605,8 +625,6 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
   const int xo_left = (lane == 0) ? (RY + 1) * 32 + w : w * 32 + lane - 1;
   const int xo_down = (w == 0) ? RY * 32 + lane : (w - 1) * 32 + lane;
   const int bo_own = w * 32 + lane;
-  const int hi_own = r * P::W + cx;
-  const int lo_own = r * P::LW + cx;
 
   // Iteration it handles plane t = k1-1-it (t = -1 is plane Nk-1) from ring
   // fill `it` of the tile.
@@ -665,13 +683,16 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
     const int cur = it & 1;
     const bool timed_out = !mbar_wait_bounded(&bar[slot], phase, wc);
     const unsigned char* stage = smem + P::kRing + slot * P::kStage;
-    const HiT* H = reinterpret_cast<const HiT*>(stage) + hi_own;
-    const LoT* Q = reinterpret_cast<const LoT*>(stage) + lo_own;
+    const HiT* H = reinterpret_cast<const HiT*>(stage);
+    const LoT* Q = reinterpret_cast<const LoT*>(stage);
+    // component c at (dr rows, dc columns) from the thread's cell (box row r,
+    // tile column cx); each component's box has its own width
     auto V = [&](auto cc, int dr, int dc) -> Pair {
       constexpr int c = decltype(cc)::value;
-      const HiT h = H[P::template kHiAt<c> / P::HS + (dr - P::template kRow0<c>) * P::W + P::template kXOff<c> + dc];
-      const LoT q = P::kLo ? Q[P::template kLoAt<c> / P::LS + (dr - P::template kRow0<c>) * P::LW +
-                               P::template kLXOff<c> + dc]
+      const HiT h = H[P::template kHiAt<c> / P::HS + (r + dr - P::template kRow0<c>) * P::template kW<c> +
+                      P::template kXOff<c> + cx + dc];
+      const LoT q = P::kLo ? Q[P::template kLoAt<c> / P::LS + (r + dr - P::template kRow0<c>) * P::template kLW<c> +
+                               P::template kLXOff<c> + cx + dc]
                            : LoT(0);
       return st.decode(c, h, q);
     };
@@ -1086,8 +1107,13 @@ cudaError_t launch_fused1_batch(const void* doms, const StepMaps* maps, const in
 }
 
 template <class S>
-int fused1_box_width() { return Box1<S>::kW; }
-int fused1_lo_box_width() { return Box1<StoreF32C>::kLoW; }
+void fused1_box_widths(bool b_first, int hi[6], int lo[6]) {
+  const BoxTable b = b_first ? Plan1<S, 14, true>::box() : Plan1<S, 14, false>::box();
+  for (int c = 0; c < 6; ++c) {
+    hi[c] = b.w[c];
+    lo[c] = b.lw[c];
+  }
+}
 
 #define FDTD_INSTANTIATE(S)                                                                              \
   template cudaError_t launch_fused1_f32<S>(const PLayout&, const S&, const S&, const void*,            \
@@ -1096,7 +1122,7 @@ int fused1_lo_box_width() { return Box1<StoreF32C>::kLoW; }
   template cudaError_t launch_fused1_batch<S>(const void*, const StepMaps*, const int4*, int, int, int,          \
                                               const FusedConfig&, const int64_t*, int, int*, const WaitCtl&,     \
                                               cudaStream_t);                                                     \
-  template int fused1_box_width<S>();
+  template void fused1_box_widths<S>(bool, int[6], int[6]);
 FDTD_INSTANTIATE(StoreF32)
 FDTD_INSTANTIATE(StoreF32C)
 FDTD_INSTANTIATE(StoreF16)

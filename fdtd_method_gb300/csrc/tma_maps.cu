@@ -91,7 +91,7 @@ cudaError_t build_tma_store_maps(void* maps, const PLayout& L, HiType ht, void* 
 }
 
 cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], LoT* const lo[6],
-                           int box_w, int lo_box_w, int tile_y, BoxTrim trim) {
+                           const int box_w[6], const int lo_box_w[6], int tile_y, BoxTrim trim) {
   TmaMaps* m = static_cast<TmaMaps*>(maps);
   std::memset(m, 0, sizeof(TmaMaps));
   const CUtensorMapDataType dt = ht == HiType::F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
@@ -102,8 +102,8 @@ cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const 
     // row above it); every other box is one row shorter.
     const bool tall = trim == BoxTrim::None || (trim == BoxTrim::EFirst ? (c == 3 || c == 5) : (c == 0 || c == 2));
     const int ty = tall ? tile_y : tile_y - 1;
-    if (!encode(&m->hi[c], dt, es, hi[c], L, box_w, ty)) return cudaErrorInvalidValue;
-    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, sizeof(LoT), lo[c], L, lo_box_w, ty))
+    if (!encode(&m->hi[c], dt, es, hi[c], L, box_w[c], ty)) return cudaErrorInvalidValue;
+    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, sizeof(LoT), lo[c], L, lo_box_w[c], ty))
       return cudaErrorInvalidValue;
   }
   return cudaSuccess;

@@ -310,18 +310,20 @@ class FDTD:
         _lib.check(self._lib.fdtd_get_fp16_exponents(self._handle(), arr))
         return list(arr)
 
-    def fp16_autoscale(self, target_log2=12):
-        """FP16 form: re-encode every component with a nonzero peak so that
-        its stored peak lies in (2^(target-1), 2^target]; returns the exponents."""
+    def fp16_autoscale(self, target_log2=10, headroom_log2=5):
+        """FP16 form: choose every component's exponent now (peak at
+        2^target, at most 2^headroom above the strongest component's scale;
+        see fdtd_fp16_autoscale); returns the exponents."""
         arr = (ctypes.c_int * 6)()
-        _lib.check(self._lib.fdtd_fp16_autoscale(self._handle(), int(target_log2), arr))
+        _lib.check(self._lib.fdtd_fp16_autoscale(self._handle(), int(target_log2), int(headroom_log2), arr))
         return list(arr)
 
-    def set_fp16_autoscale(self, every_steps, target_log2=12):
-        """FP16 form: step() scans the stored peaks every `every_steps` steps
-        (0: never) and re-encodes components that left the band around
-        2^target."""
-        _lib.check(self._lib.fdtd_set_fp16_autoscale(self._handle(), int(every_steps), int(target_log2)))
+    def set_fp16_autoscale(self, every_steps, target_log2=10, headroom_log2=5):
+        """FP16 form: step() rescans the stored peaks every `every_steps`
+        steps (0: never) and re-encodes components whose exponent drifted
+        from the wanted one (fdtd_set_fp16_autoscale)."""
+        _lib.check(self._lib.fdtd_set_fp16_autoscale(self._handle(), int(every_steps), int(target_log2),
+                                                     int(headroom_log2)))
 
     def set_fp64_arith(self, contracted):
         """FP64 form: False keeps the reference's arithmetic bit for bit (the

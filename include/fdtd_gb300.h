@@ -220,19 +220,27 @@ int fdtd_measure_fp64_rate(double* dp_instr_per_s, double* ms);
  * field * 2^exponent.  `exponents` has 6 entries (Ex..Bz), each in [-60, 60]. */
 int fdtd_set_fp16_exponents(fdtd_handle* h, const int exponents[6]);
 int fdtd_get_fp16_exponents(fdtd_handle* h, int exponents[6]);
-/* Exponents chosen by the engine (new).  fdtd_fp16_autoscale scans the
- * stored peak of each component now and re-encodes every component with a
- * nonzero peak so that it lies in (2^(target_log2-1), 2^target_log2]
- * (target_log2 in [0, 15]; 12 leaves 16x of growth below FP16's largest
- * value); the chosen exponents go to `exponents` if non-null.
+/* Exponents chosen by the engine (new).  From the stored peaks, each
+ * component's field peak is below 2^k_c; with k_all the largest, the wanted
+ * exponent puts the component's peak at 2^target_log2 but never more than
+ * 2^headroom_log2 above the strongest component's scale:
+ *     e_c = min(target_log2 - k_c, target_log2 + headroom_log2 - k_all)
+ * (a component with no field gets the second term).  The bound keeps a weak
+ * component that grows to the strongest one's size inside FP16's range
+ * (target 10, headroom 5: peaks up to 2^15 before anything overflows, and
+ * 64x of growth for the strongest); where components cannot exchange
+ * magnitude, a large headroom gives each its own scale.
+ * fdtd_fp16_autoscale sets the exponents now (target_log2 in [0, 15],
+ * headroom_log2 in [0, 60]) and returns them in `exponents` if non-null.
  * fdtd_set_fp16_autoscale makes fdtd_step scan every `every_steps` steps
- * (0: never) and re-encode the components whose peak left
- * [2^(target_log2-4), 2^(target_log2+2)].  Re-encoding multiplies stored
- * values by a power of two, which commutes with the FP32 arithmetic on them:
- * results change only where a value would otherwise have left FP16's normal
- * range.  Each scan synchronises the handle's stream. */
-int fdtd_fp16_autoscale(fdtd_handle* h, int target_log2, int exponents[6]);
-int fdtd_set_fp16_autoscale(fdtd_handle* h, int every_steps, int target_log2);
+ * (0: never) and re-encode a component whose exponent is above the bound or
+ * 3 or more from the wanted one; the scan interval must be short against the
+ * fields' growth.  Re-encoding multiplies stored values by a power of two,
+ * which commutes with the FP32 arithmetic on them: results change only where
+ * a value would otherwise have left FP16's normal range.  Each scan
+ * synchronises the handle's stream. */
+int fdtd_fp16_autoscale(fdtd_handle* h, int target_log2, int headroom_log2, int exponents[6]);
+int fdtd_set_fp16_autoscale(fdtd_handle* h, int every_steps, int target_log2, int headroom_log2);
 
 /* Kernel timing (new; for roofline accounting).  While enabled, every kernel
  * launch of the step pipeline is bracketed by CUDA events on the handle's
