@@ -63,7 +63,7 @@ class Source(ctypes.Structure):
 class TuneResult(ctypes.Structure):
     _fields_ = [("tile_y", ctypes.c_int), ("kchunk", ctypes.c_int), ("cells_per_thread", ctypes.c_int),
                 ("ms_per_sweep", ctypes.c_double), ("candidates", ctypes.c_int), ("cached", ctypes.c_int),
-                ("split_sources", ctypes.c_int)]
+                ("split_sources", ctypes.c_int), ("depth", ctypes.c_int)]
 
 
 _H = ctypes.c_void_p
@@ -98,6 +98,7 @@ SIGNATURES = {
     "fdtd_fp16_autoscale": [_H, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
     "fdtd_set_fp16_autoscale": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "fdtd_set_wait_limit": [_H, ctypes.c_int64, ctypes.c_int],
+    "fdtd_set_temporal_depth": [_H, ctypes.c_int],
     "fdtd_measure_fp64_rate": [_D, _D],
     "fdtd_set_kernel_timing": [_H, ctypes.c_int],
     "fdtd_kernel_times": [_H, _D, ctypes.POINTER(ctypes.c_int64)],

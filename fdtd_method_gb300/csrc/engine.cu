@@ -245,7 +245,7 @@ bool b_first(const fdtd_handle* h) { return h->fused_cfg.cells_per_thread == 1; 
 // without the swap (the autotuner repeats it to time a tile shape: the state
 // is only read).  B-first: `apps` B half steps, then E; E-first: E, then
 // `apps` B half steps.
-cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps) {
+cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps, int depth = 1) {
   SourceSet ss = h->source_set();
   StateView v = h->view();
   StateView w = h->view_alt();
@@ -258,6 +258,25 @@ cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps) {
   sm.ld = bf ? h->bmaps_cur : h->maps_cur;
   sm.st = h->smaps_alt;
   cudaError_t e = cudaSuccess;
+  if (depth == 2) {
+    // both ghost rings of the input copy, then two steps in one pass
+    GhostArrays ga{{h->field[0], h->field[1], h->field[2], h->field[3], h->field[4], h->field[5]}};
+    e = launch_refresh_ghosts(h->L, ga, h->form == Form::F16 ? 2 : 4, h->stream);
+    if (e == cudaSuccess && h->form == Form::F32C) {
+      GhostArrays gl{{h->lo[0], h->lo[1], h->lo[2], h->lo[3], h->lo[4], h->lo[5]}};
+      e = launch_refresh_ghosts(h->L, gl, 2, h->stream);
+    }
+    if (e != cudaSuccess) return e;
+    StepMaps tm;
+    tm.ld = h->tmaps_cur;
+    tm.st = h->smaps_alt;
+    switch (h->form) {
+      case Form::F32: return launch_tblock2_f32(h->L, v.s32, w.s32, &tm, J, dj, h->cs, ss, step, apps, cf, wc, h->stream);
+      case Form::F32C: return launch_tblock2_f32(h->L, v.s32c, w.s32c, &tm, J, dj, h->cs, ss, step, apps, cf, wc, h->stream);
+      case Form::F16: return launch_tblock2_f32(h->L, v.s16, w.s16, &tm, J, dj, h->cs, ss, step, apps, cf, wc, h->stream);
+      default: return cudaErrorInvalidValue;
+    }
+  }
   if (cf.cells_per_thread == 2) {
     const void* m = &h->maps_cur;
     switch (h->form) {
@@ -277,10 +296,10 @@ cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps) {
   return e;
 }
 
-int run_fused(fdtd_handle* h, int64_t step, int apps) {
+int run_fused(fdtd_handle* h, int64_t step, int apps, int depth = 1) {
   if (int rc = ensure_alt(h)) return rc;
-  LaunchTimer lt(h, FDTD_KERNEL_FUSED);
-  cudaError_t e = launch_fused_sweep(h, step, apps);
+  LaunchTimer lt(h, depth == 2 ? FDTD_KERNEL_FUSED2 : FDTD_KERNEL_FUSED);
+  cudaError_t e = launch_fused_sweep(h, step, apps, depth);
   lt.done();
   if (e != cudaSuccess) return cuda_fail(e, "fused step launch");
   swap_copies(h);
@@ -292,6 +311,10 @@ int run_fused(fdtd_handle* h, int64_t step, int apps) {
 constexpr int kTuneRows1[] = {6, 14, 30};
 constexpr int kTuneRows2[] = {6, 14};
 constexpr int kTuneChunks[] = {16, 24, 32, 48, 64, 96};
+// The depth-2 sweep: 6- or 14-row tiles; it reads four planes past its chunk,
+// so only longer chunks.
+constexpr int kTuneRowsDepth2[] = {6, 14};
+constexpr int kTuneChunksDepth2[] = {24, 48, 96};
 
 struct TuneKey {
   int form, Ni, Nj, Nk;
@@ -410,6 +433,18 @@ int ensure_alt(fdtd_handle* h) {
     if (!two && (build_tma_maps(&h->bmaps_cur, h->L, ht, h->field, lo_cur, bbw, blbw, ty, BoxTrim::BFirst) != cudaSuccess ||
                  build_tma_maps(&h->bmaps_alt, h->L, ht, h->alt_field, lo_alt, bbw, blbw, ty, BoxTrim::BFirst) != cudaSuccess))
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
+    if (!two && ty != 30) {
+      int tw[6], tlw[6];
+      switch (h->form) {
+        case Form::F16: tblock2_box_widths<StoreF16>(tw, tlw); break;
+        case Form::F32C: tblock2_box_widths<StoreF32C>(tw, tlw); break;
+        default: tblock2_box_widths<StoreF32>(tw, tlw); break;
+      }
+      // depth-2 boxes: rows y0-2 .. y0+ty+1 for Ex, Ez, y0-2 .. y0+ty otherwise
+      if (build_tma_maps(&h->tmaps_cur, h->L, ht, h->field, lo_cur, tw, tlw, ty + 2, BoxTrim::BFirst) != cudaSuccess ||
+          build_tma_maps(&h->tmaps_alt, h->L, ht, h->alt_field, lo_alt, tw, tlw, ty + 2, BoxTrim::BFirst) != cudaSuccess)
+        return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
+    }
     if (!two && (build_tma_store_maps(&h->smaps_cur, h->L, ht, h->field, lo_cur, ty) != cudaSuccess ||
                  build_tma_store_maps(&h->smaps_alt, h->L, ht, h->alt_field, lo_alt, ty) != cudaSuccess))
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
@@ -426,6 +461,7 @@ void swap_copies(fdtd_handle* h) {
   std::swap(h->maps_cur, h->maps_alt);
   std::swap(h->smaps_cur, h->smaps_alt);
   std::swap(h->bmaps_cur, h->bmaps_alt);
+  std::swap(h->tmaps_cur, h->tmaps_alt);
 }
 
 int read_view(fdtd_handle* h, StateView* v) {
@@ -742,11 +778,13 @@ int step_sweeps(fdtd_handle* h, int64_t n) {
   const bool fused = h->pipeline != FDTD_PIPELINE_SPLIT;
   if (fused && b_first(h)) {
     // B-first sweeps: sweep s applies the B half steps that meet before step
-    // s, then E.
-    for (int64_t s = 0; s < n; ++s) {
-      if (int rc = run_fused(h, h->host_step + s, h->b_pending ? 2 : 1)) return rc;
+    // s, then E; a depth-2 sweep does that for steps s and s+1.
+    for (int64_t s = 0; s < n;) {
+      const int depth = (h->fused_cfg.depth == 2 && s + 1 < n) ? 2 : 1;
+      if (int rc = run_fused(h, h->host_step + s, h->b_pending ? 2 : 1, depth)) return rc;
       h->b_pending = true;
       h->b_side = false;
+      s += depth;
     }
     return FDTD_OK;
   }
@@ -1066,6 +1104,8 @@ int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int 
     return fail(FDTD_ERR_INVALID_ARGUMENT, "cells_per_thread must be 0 (default), 1 or 2");
   if (h->zhalo && pipeline == FDTD_PIPELINE_FUSED)
     return fail(FDTD_ERR_UNSUPPORTED, "a z slab runs the split sweeps");
+  if (h->fused_cfg.depth == 2 && (cells_per_thread == 2 || tile_y == 30))
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "the depth-2 sweep needs cells_per_thread 1 and tile_y 6 or 14");
   h->pipeline = pipeline;
   h->fused_cfg.tile_y = tile_y ? tile_y : 14;
   h->fused_cfg.kchunk = kchunk ? kchunk : 48;
@@ -1098,36 +1138,47 @@ int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out) 
       return fail(FDTD_ERR_CUDA, "autotune events");
     }
     best.ms_per_sweep = 1e30;
+    // candidates: (depth, cells per thread, tile rows, chunk)
+    std::vector<std::tuple<int, int, int, int>> cands;
+    for (int cpt = 1; cpt <= 2; ++cpt)
+      for (int ry : (cpt == 1 ? std::vector<int>(std::begin(kTuneRows1), std::end(kTuneRows1))
+                              : std::vector<int>(std::begin(kTuneRows2), std::end(kTuneRows2))))
+        for (int kc : kTuneChunks) cands.emplace_back(1, cpt, ry, kc);
+    for (int ry : kTuneRowsDepth2)
+      for (int kc : kTuneChunksDepth2) cands.emplace_back(2, 1, ry, kc);
+    const int depth_before = h->fused_cfg.depth;
     int rc = FDTD_OK;
-    for (int cpt = 1; cpt <= 2 && rc == FDTD_OK; ++cpt) {
-      const int* rows = cpt == 1 ? kTuneRows1 : kTuneRows2;
-      const int nrows = cpt == 1 ? 3 : 2;
-      for (int a = 0; a < nrows && rc == FDTD_OK; ++a)
-        for (int kc : kTuneChunks) {
-          h->fused_cfg.tile_y = rows[a];
-          h->fused_cfg.kchunk = kc;
-          h->fused_cfg.cells_per_thread = cpt;
-          if ((rc = ensure_alt(h)) != FDTD_OK) break;
-          cudaError_t e = launch_fused_sweep(h, h->host_step, 2);  // warm-up
-          if (e == cudaSuccess) e = cudaEventRecord(e0, h->stream);
-          for (int q = 0; q < sweeps && e == cudaSuccess; ++q) e = launch_fused_sweep(h, h->host_step, 2);
-          if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
-          if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-          float ms = 0.f;
-          if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-          if (e != cudaSuccess) {
-            rc = cuda_fail(e, "autotune sweep");
-            break;
-          }
-          best.candidates += 1;
-          if (ms / sweeps < best.ms_per_sweep) {
-            best.ms_per_sweep = ms / sweeps;
-            best.tile_y = rows[a];
-            best.kchunk = kc;
-            best.cells_per_thread = cpt;
-          }
-        }
+    for (const auto& cand : cands) {
+      const int depth = std::get<0>(cand);
+      h->fused_cfg.depth = 1;
+      h->fused_cfg.cells_per_thread = std::get<1>(cand);
+      h->fused_cfg.tile_y = std::get<2>(cand);
+      h->fused_cfg.kchunk = std::get<3>(cand);
+      if ((rc = ensure_alt(h)) != FDTD_OK) break;
+      // the timed sweeps read the current copy (a depth-2 sweep also rewrites
+      // its ghost copies with the values they hold) and write the second one
+      cudaError_t e = launch_fused_sweep(h, h->host_step, 2, depth);  // warm-up
+      if (e == cudaSuccess) e = cudaEventRecord(e0, h->stream);
+      for (int q = 0; q < sweeps && e == cudaSuccess; ++q) e = launch_fused_sweep(h, h->host_step, 2, depth);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) {
+        rc = cuda_fail(e, "autotune sweep");
+        break;
+      }
+      best.candidates += 1;
+      const double per_step = ms / sweeps / depth;
+      if (per_step < best.ms_per_sweep) {
+        best.ms_per_sweep = per_step;
+        best.tile_y = std::get<2>(cand);
+        best.kchunk = std::get<3>(cand);
+        best.cells_per_thread = std::get<1>(cand);
+        best.depth = depth;
+      }
     }
+    h->fused_cfg.depth = depth_before;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     h->b_side = false;  // the timed sweeps wrote the second copy
@@ -1138,6 +1189,7 @@ int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out) 
   h->fused_cfg.tile_y = best.tile_y;
   h->fused_cfg.kchunk = best.kchunk;
   h->fused_cfg.cells_per_thread = best.cells_per_thread;
+  h->fused_cfg.depth = best.depth;
   if (int rc = ensure_alt(h)) return rc;
   if (out) {
     *out = best;
@@ -1221,6 +1273,19 @@ int fdtd_get_fp16_exponents(fdtd_handle* h, int exponents[6]) {
   if (int rc = check_handle(h)) return rc;
   if (!exponents) return fail(FDTD_ERR_INVALID_ARGUMENT, "null exponents");
   for (int c = 0; c < 6; ++c) exponents[c] = h->fp16_exp[c];
+  return FDTD_OK;
+}
+
+int fdtd_set_temporal_depth(fdtd_handle* h, int depth) {
+  if (int rc = check_handle(h)) return rc;
+  if (depth != 1 && depth != 2) return fail(FDTD_ERR_INVALID_ARGUMENT, "depth must be 1 or 2");
+  if (depth == 2) {
+    if (h->form == Form::F64 || h->zhalo || h->pml)
+      return fail(FDTD_ERR_UNSUPPORTED, "the depth-2 sweep runs the FP32-arithmetic forms of whole grids");
+    if (h->fused_cfg.cells_per_thread != 1 || h->fused_cfg.tile_y == 30)
+      return fail(FDTD_ERR_INVALID_ARGUMENT, "the depth-2 sweep needs cells_per_thread 1 and tile_y 6 or 14");
+  }
+  h->fused_cfg.depth = depth;
   return FDTD_OK;
 }
 

@@ -62,6 +62,7 @@ __device__ __forceinline__ Coef jcoef(const CoefSet& cs, const S& st, int c) {
 // Launch shape of the fused step kernel: interior tile rows (14 or 6) and
 // planes per tile.
 struct FusedConfig {
+  int depth = 1;     // steps per sweep: 1, or 2 (temporal blocking, kernels_tblock.cu)
   int tile_y = 14;
   int kchunk = 48;  // planes per tile (the autotuner picks from 16 to 96)
   int cells_per_thread = 1;  // 1: 32-wide tiles (kernels_fused1.cu); 2: 64-wide, packed float2
@@ -135,6 +136,23 @@ cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const
 // maps, for its E-first or B-first sweep.
 template <class S>
 void fused1_box_widths(bool b_first, int hi[6], int lo[6]);
+
+// kernels_tblock.cu: the depth-2 sweep (two B-first steps per pass; the
+// first step applies `apps1` B half steps, the second two) of one cell per
+// thread, 32 x tile_y tiles (6 or 14); `maps` is a StepMaps whose load maps
+// (BoxTrim::BFirst, tile_y + 2, widths tblock2_box_widths) cover two rings of
+// halo.  The input's second ghost ring must be current: launch_refresh_ghosts
+// rewrites both rings of six padded arrays (elem_bytes 4 or 2) from the grid.
+struct GhostArrays {
+  void* p[6];
+};
+cudaError_t launch_refresh_ghosts(const PLayout& L, const GhostArrays& arrays, int elem_bytes, cudaStream_t stream);
+template <class S>
+cudaError_t launch_tblock2_f32(const PLayout& L, const S& st, const S& out, const void* maps, const float* const J[3],
+                               bool dense_j, const CoefSet& cs, const SourceSet& ss, int64_t step, int apps1,
+                               const FusedConfig& cfg, const WaitCtl& wc, cudaStream_t stream);
+template <class S>
+void tblock2_box_widths(int hi[6], int lo[6]);
 
 // Batched form: one record per domain in device memory (its layout, its two
 // state copies, coefficients and sources).

@@ -125,9 +125,12 @@ struct fdtd_handle {
   // fused kernel.
   TmaMaps smaps_cur;
   TmaMaps smaps_alt;
-  // Load maps of the B-first sweep (its boxes hold other halo rows).
+  // Load maps of the B-first sweep (its boxes hold other halo rows) and of
+  // the depth-2 sweep (two rings of halo).
   TmaMaps bmaps_cur;
   TmaMaps bmaps_alt;
+  TmaMaps tmaps_cur;
+  TmaMaps tmaps_alt;
   int maps_tile_y = 0;
   int* d_err = nullptr;  // device status word (bounded waits that gave up)
   // Bounded waits of the fused sweeps: polls before a wait gives up, and the

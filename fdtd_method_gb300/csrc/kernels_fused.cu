@@ -142,10 +142,10 @@ __global__ void __launch_bounds__(32 * (RY + 2))
     unsigned char* base = smem + slot * SP::kStageBytes;
     mbar_arrive_expect_tx(&bar[slot], SP::kTx);
     for (int c = 0; c < 6; ++c)
-      tma_load_3d(base + c * ROWS * W * sizeof(HiT), &maps.hi[c], x0 + kPadX - OFF, y0, kk, &bar[slot]);
+      tma_load_3d(base + c * ROWS * W * sizeof(HiT), &maps.hi[c], x0 + kPadX - OFF, y0 - 1 + kPadY, kk, &bar[slot]);
     if (S::kComp)
       for (int c = 0; c < 6; ++c)
-        tma_load_3d(base + SP::kHiBytes + c * ROWS * LW * sizeof(LoT), &maps.lo[c], x0 + kPadX - kLoOff, y0, kk,
+        tma_load_3d(base + SP::kHiBytes + c * ROWS * LW * sizeof(LoT), &maps.lo[c], x0 + kPadX - kLoOff, y0 - 1 + kPadY, kk,
                     &bar[slot]);
   };
 

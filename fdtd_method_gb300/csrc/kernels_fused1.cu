@@ -326,14 +326,14 @@ __device__ __forceinline__ bool fused1_planes(const PLayout& L, const S& st, con
     const int kk = (t == L.Nk) ? 0 : t;
     unsigned char* base = smem + P::kRing + slot * P::kStage;
     mbar_arrive_expect_tx(&bar[slot], P::kTx);
-    // (y coordinates are padded rows: logical row y0-1 is padded row y0)
+    // (y coordinates are padded rows: logical row y is padded row y + kPadY)
     for_each_comp([&](auto cc) {
       constexpr int c = decltype(cc)::value;
       tma_load_3d(base + P::template kHiAt<c>, &maps.ld.hi[c], x0 + kPadX - P::template kXOff<c>,
-                  y0 + P::template kRow0<c>, kk, &bar[slot]);
+                  y0 - 1 + kPadY + P::template kRow0<c>, kk, &bar[slot]);
       if (P::kLo)
         tma_load_3d(base + P::template kLoAt<c>, &maps.ld.lo[c], x0 + kPadX - P::template kLXOff<c>,
-                    y0 + P::template kRow0<c>, kk, &bar[slot]);
+                    y0 - 1 + kPadY + P::template kRow0<c>, kk, &bar[slot]);
     });
   };
 
@@ -639,11 +639,11 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
     mbar_arrive_expect_tx(&bar[slot], P::kTx);
     for_each_comp([&](auto cc) {
       constexpr int c = decltype(cc)::value;
-      tma_load_3d(base + P::template kHiAt<c>, &maps.ld.hi[c], x0 + kPadX - P::template kXOff<c>, y0, kk,
-                  &bar[slot]);
+      tma_load_3d(base + P::template kHiAt<c>, &maps.ld.hi[c], x0 + kPadX - P::template kXOff<c>, y0 - 1 + kPadY,
+                  kk, &bar[slot]);
       if (P::kLo)
-        tma_load_3d(base + P::template kLoAt<c>, &maps.ld.lo[c], x0 + kPadX - P::template kLXOff<c>, y0, kk,
-                    &bar[slot]);
+        tma_load_3d(base + P::template kLoAt<c>, &maps.ld.lo[c], x0 + kPadX - P::template kLXOff<c>,
+                    y0 - 1 + kPadY, kk, &bar[slot]);
     });
   };
   if (leader)

@@ -1,16 +1,20 @@
 // Padded field layout of the FP32-arithmetic forms.
 //
-// Each component is stored as a 3-D array with a ghost row below and above
-// the grid in y and a 32-element margin left and right of it in x, so that
-//   * every x/y neighbour of a grid cell exists in memory (the ghost cells
-//     hold periodic copies: ghost x = -1 is cell Ni-1, ghost x = Ni is cell 0,
-//     likewise in y and at the four corners), and
+// Each component is stored as a 3-D array with kPadY ghost rows below and
+// above the grid in y and a 32-element margin left and right of it in x, so
+// that
+//   * every x/y neighbour of a grid cell exists in memory (the first ghost
+//     row and column on each side hold periodic copies: ghost x = -1 is cell
+//     Ni-1, ghost x = Ni is cell 0, likewise in y and at the four corners),
+//     and the second ones (x = -2, Ni+1; y = -2, Nj+1) have room for the
+//     copies a two-step sweep reads, which it refreshes before it runs;
 //   * cell x = 0 of every row starts a 32-byte memory sector for every
 //     element size (pitch is a multiple of 32 elements), so the stores of a
 //     warp's row segment cover whole sectors (no read-modify-write in L2)
 //     and the tile copies start on the 16-byte boundaries TMA requires.
-// The writer of a boundary cell also writes its ghost copies, so the ghosts
-// are current whenever the cell is.  z is not padded: planes wrap by index.
+// The writer of a boundary cell also writes its first-ring ghost copies, so
+// those are current whenever the cell is.  z is not padded: planes wrap by
+// index.
 //
 // The FP64 drop-in keeps the reference's dense layout i + j*Ni + k*Ni*Nj.
 #pragma once
@@ -20,14 +24,15 @@
 namespace fdtd {
 
 constexpr int kPadX = 32;
+constexpr int kPadY = 2;  // ghost rows on each side (padded row = logical row + kPadY)
 
 struct PLayout {
   int Ni, Nj, Nk;
   int64_t pitch;   // elements per padded row
-  int64_t pplane;  // elements per padded plane = pitch * (Nj + 2)
+  int64_t pplane;  // elements per padded plane = pitch * (Nj + 2 kPadY)
 
   __host__ __device__ __forceinline__ int64_t at(int x, int y, int z) const {
-    return (int64_t)(x + kPadX) + (int64_t)(y + 1) * pitch + (int64_t)z * pplane;
+    return (int64_t)(x + kPadX) + (int64_t)(y + kPadY) * pitch + (int64_t)z * pplane;
   }
   __host__ __device__ __forceinline__ int64_t elems() const { return pplane * Nk; }
 
@@ -37,7 +42,7 @@ struct PLayout {
     L.Nj = Nj;
     L.Nk = Nk;
     L.pitch = ((int64_t)Ni + 2 * kPadX + 31) / 32 * 32;
-    L.pplane = L.pitch * (Nj + 2);
+    L.pplane = L.pitch * (Nj + 2 * kPadY);
     return L;
   }
 };

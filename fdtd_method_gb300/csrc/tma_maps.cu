@@ -31,19 +31,19 @@ EncodeTiled encode_fn() {
   return fn;
 }
 
-// One 3-D map over a padded array for the tile loads: dims {kPadX + Ni + 1,
-// Nj + 2, Nk} (the left margin, the grid and the right ghost column, the
-// last column a tile reads), box {box_w, tile_y + 2, 1}.  Box columns past
-// the ghost column are outside the map: the copy engine fills them with
-// zeros instead of reading memory (a tile narrower than 32 columns reads only
-// what it uses).
+// One 3-D map over a padded array for the tile loads: dims {kPadX + Ni + 2,
+// Nj + 2 kPadY, Nk} (the left margin, the grid and the two right ghost
+// columns, the last column a two-step tile reads; every ghost row), box
+// {box_w, box rows, 1}.  Box columns past the second ghost column are outside
+// the map: the copy engine fills them with zeros instead of reading memory (a
+// tile narrower than 32 columns reads only what it uses).
 bool encode(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const PLayout& L, int box_w,
-            int tile_y) {
+            int box_rows) {
   EncodeTiled fn = encode_fn();
   if (!fn) return false;
-  const cuuint64_t dims[3] = {(cuuint64_t)(kPadX + L.Ni + 1), (cuuint64_t)(L.Nj + 2), (cuuint64_t)L.Nk};
+  const cuuint64_t dims[3] = {(cuuint64_t)(kPadX + L.Ni + 2), (cuuint64_t)(L.Nj + 2 * kPadY), (cuuint64_t)L.Nk};
   const cuuint64_t strides[2] = {(cuuint64_t)(L.pitch * es), (cuuint64_t)(L.pplane * es)};
-  const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)(tile_y + 2), 1};
+  const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_rows, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
   return fn(m, dt, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -101,9 +101,9 @@ cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const 
     // (the row below the tile); B-first sweep: only Ex and Ez (0, 2) do (the
     // row above it); every other box is one row shorter.
     const bool tall = trim == BoxTrim::None || (trim == BoxTrim::EFirst ? (c == 3 || c == 5) : (c == 0 || c == 2));
-    const int ty = tall ? tile_y : tile_y - 1;
-    if (!encode(&m->hi[c], dt, es, hi[c], L, box_w[c], ty)) return cudaErrorInvalidValue;
-    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, sizeof(LoT), lo[c], L, lo_box_w[c], ty))
+    const int rows = tall ? tile_y + 2 : tile_y + 1;
+    if (!encode(&m->hi[c], dt, es, hi[c], L, box_w[c], rows)) return cudaErrorInvalidValue;
+    if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, sizeof(LoT), lo[c], L, lo_box_w[c], rows))
       return cudaErrorInvalidValue;
   }
   return cudaSuccess;

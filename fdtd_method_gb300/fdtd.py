@@ -337,7 +337,7 @@ class FDTD:
         fused sweeps issue no tile loads, so every wait gives up."""
         _lib.check(self._lib.fdtd_set_wait_limit(self._handle(), int(polls), 1 if withhold_loads else 0))
 
-    KERNEL_KINDS = ("e_update", "b_half", "b_double", "fused_step")
+    KERNEL_KINDS = ("e_update", "b_half", "b_double", "fused_step", "fused_step2")
     PIPELINES = {"auto": 0, "split": 1, "fused": 2}
 
     def set_pipeline(self, pipeline="auto", tile_y=0, kchunk=0, cells_per_thread=0):
@@ -354,8 +354,13 @@ class FDTD:
         as a dict; results are cached per (precision, grid) in the process."""
         r = _lib.TuneResult()
         _lib.check(self._lib.fdtd_autotune(self._handle(), int(sweeps), 1 if reuse else 0, ctypes.byref(r)))
-        return {"tile_y": r.tile_y, "kchunk": r.kchunk, "cells_per_thread": r.cells_per_thread,
-                "ms_per_sweep": r.ms_per_sweep, "candidates": r.candidates, "cached": bool(r.cached)}
+        return {"tile_y": r.tile_y, "kchunk": r.kchunk, "cells_per_thread": r.cells_per_thread, "depth": r.depth,
+                "ms_per_step": r.ms_per_sweep, "candidates": r.candidates, "cached": bool(r.cached)}
+
+    def set_temporal_depth(self, depth):
+        """Steps per pass over the state: 1, or 2 (temporal blocking; same
+        bits).  See fdtd_set_temporal_depth."""
+        _lib.check(self._lib.fdtd_set_temporal_depth(self._handle(), int(depth)))
 
     def set_kernel_timing(self, enabled):
         """Bracket every step-pipeline kernel launch with CUDA events."""
@@ -363,8 +368,8 @@ class FDTD:
 
     def kernel_times(self):
         """{kind: (total ms, launches)} since the previous call."""
-        ms = (ctypes.c_double * 4)()
-        n = (ctypes.c_int64 * 4)()
+        ms = (ctypes.c_double * len(self.KERNEL_KINDS))()
+        n = (ctypes.c_int64 * len(self.KERNEL_KINDS))()
         _lib.check(self._lib.fdtd_kernel_times(self._handle(), ms, n))
         return {k: (ms[q], n[q]) for q, k in enumerate(self.KERNEL_KINDS)}
 

@@ -246,13 +246,15 @@ int fdtd_set_fp16_autoscale(fdtd_handle* h, int every_steps, int target_log2, in
  * launch of the step pipeline is bracketed by CUDA events on the handle's
  * stream.  fdtd_kernel_times synchronizes, then returns per kernel kind the
  * summed duration in milliseconds and the launch count since the last call,
- * and clears them.  Kinds: FDTD_KERNEL_E, _B_HALF, _B_DOUBLE, _FUSED. */
+ * and clears them.  Kinds: FDTD_KERNEL_E, _B_HALF, _B_DOUBLE, _FUSED,
+ * _FUSED2. */
 enum fdtd_kernel_kind {
     FDTD_KERNEL_E = 0,        /* E update sweep                            */
     FDTD_KERNEL_B_HALF = 1,   /* one B half step                           */
     FDTD_KERNEL_B_DOUBLE = 2, /* two B half steps sharing one sweep        */
     FDTD_KERNEL_FUSED = 3,    /* a whole step (B/2, E, B/2) in one sweep   */
-    FDTD_KERNEL_KINDS = 4
+    FDTD_KERNEL_FUSED2 = 4,   /* two whole steps in one sweep (depth 2)    */
+    FDTD_KERNEL_KINDS = 5
 };
 int fdtd_set_kernel_timing(fdtd_handle* h, int enabled);
 
@@ -271,7 +273,9 @@ int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t laun
 /* Autotuner (new).  Times `sweeps` fused sweeps (0 = 10) for every candidate
  * launch shape of the FP32-arithmetic forms (cells_per_thread 1 with tile_y
  * 6, 14 and 30; cells_per_thread 2 with tile_y 6 and 14; each with kchunk 16,
- * 24, 32, 48, 64 and 96) on the handle's own grid, and keeps the fastest
+ * 24, 32, 48, 64 and 96; and the depth-2 sweep with tile_y 6 and 14 and
+ * kchunk 24, 48 and 96, compared per step) on the handle's own grid, and
+ * keeps the fastest
  * (fdtd_set_pipeline's shape arguments).  The timed sweeps read the current
  * state and write the handle's second copy, so the simulation state does not
  * change.  Results are cached per (precision, Ni, Nj, Nk) in the process;
@@ -279,12 +283,22 @@ int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t laun
  * form gives FDTD_ERR_UNSUPPORTED. */
 typedef struct fdtd_tune_result {
     int tile_y, kchunk, cells_per_thread;
-    double ms_per_sweep;  /* of the chosen shape */
+    double ms_per_sweep;  /* of the chosen shape, per step (a depth-2 sweep's time halved) */
     int candidates;       /* shapes timed */
     int cached;           /* 1 if taken from the cache */
     int split_sources;    /* batched sweep: 1 if the chosen sweep runs the split plane loop */
+    int depth;            /* steps per sweep of the chosen shape: 1 or 2 */
 } fdtd_tune_result;
 int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out);
+
+/* Temporal blocking (new).  depth 2: fdtd_step runs two steps per pass over
+ * the state (a depth-2 sweep reads E and B once and writes them once for both
+ * steps; an odd last step is a one-step sweep); depth 1: one step per sweep.
+ * Both give the same bits.  Depth 2 needs the FP32-arithmetic forms, the
+ * fused pipeline with one cell per thread, and tile_y 6 or 14; the
+ * autotuner also tries it (its result's depth field).  Batches and z slabs
+ * step one step per sweep. */
+int fdtd_set_temporal_depth(fdtd_handle* h, int depth);
 
 /* ------------------------------------------------------------------------
  * Batched form (new; the reference advances one grid per object).  A batch

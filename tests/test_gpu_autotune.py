@@ -37,9 +37,10 @@ def test_autotune_leaves_state_and_bits_unchanged(prec):
         _setup(s, p, 3)
     before = _fields(a)
     r = a.autotune(sweeps=2, reuse=False)
-    assert r["candidates"] == 30 and not r["cached"]  # (3 + 2 tile shapes) x 6 chunk lengths
+    # (3 + 2 tile shapes) x 6 chunk lengths, and the depth-2 sweep's 2 x 3
+    assert r["candidates"] == 36 and not r["cached"]
     assert (r["cells_per_thread"], r["tile_y"]) in {(1, 6), (1, 14), (1, 30), (2, 6), (2, 14)}
-    assert r["kchunk"] in (16, 24, 32, 48) and r["ms_per_sweep"] > 0
+    assert r["kchunk"] in (16, 24, 32, 48, 64, 96) and r["ms_per_step"] > 0 and r["depth"] in (1, 2)
     for x, y in zip(before, _fields(a)):
         np.testing.assert_array_equal(x, y)
     a.step(7)
@@ -48,8 +49,8 @@ def test_autotune_leaves_state_and_bits_unchanged(prec):
         np.testing.assert_array_equal(x, y)
     c = FDTD(p, COURANT_DT, prec)
     r2 = c.autotune(reuse=True)
-    assert r2["cached"] and (r2["tile_y"], r2["kchunk"], r2["cells_per_thread"]) == (r["tile_y"], r["kchunk"],
-                                                                                    r["cells_per_thread"])
+    assert r2["cached"] and (r2["tile_y"], r2["kchunk"], r2["cells_per_thread"], r2["depth"]) == (
+        r["tile_y"], r["kchunk"], r["cells_per_thread"], r["depth"])
 
 
 def test_autotune_rejects_fp64():
