@@ -76,6 +76,7 @@ def parse_args():
     ap.add_argument("--tile-y", type=int, default=0)
     ap.add_argument("--kchunk", type=int, default=0)
     ap.add_argument("--cells-per-thread", type=int, default=0)
+    ap.add_argument("--depth", type=int, default=0, help="steps per sweep of the chosen form (0: the autotuner's)")
     ap.add_argument("--run-length", type=int, default=1000, help="steps of the accuracy run")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -638,8 +639,11 @@ def run_ours(args):
     sim.set_stream(stream.cuda_stream)
     sim.add_source(src)
     tuned = None
-    if not args.no_autotune and args.pipeline != "split" and not (args.tile_y or args.kchunk or args.cells_per_thread):
+    if not args.no_autotune and args.pipeline != "split" and not (args.tile_y or args.kchunk or args.cells_per_thread
+                                                                   or args.depth):
         tuned = sim.autotune(sweeps=10, reuse=False)  # before the timed region; the state is only read
+    if args.depth:
+        sim.set_temporal_depth(args.depth)
     sim.step(W)
     sim.synchronize()
     sim.kernel_times()
