@@ -247,6 +247,27 @@ bool b_first(const fdtd_handle* h) { return h->fused_cfg.cells_per_thread == 1; 
 // `apps` B half steps.
 cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps, int depth = 1) {
   SourceSet ss = h->source_set();
+  if (h->zhalo) {
+    // z slab: the B-first sweep over the storage's owned planes, reading the
+    // halo planes below and above (the copies carry them; the maps cover them)
+    if (depth != 1 || !b_first(h)) return cudaErrorInvalidValue;
+    const StateView v = h->sweep_view(), w = h->with_halo(h->view_alt());
+    const int64_t dj0 = h->zhalo * h->g.plane;
+    const bool dj = h->dense_j && h->jf[0];
+    const float* J[3] = {dj ? h->jf[0] - dj0 : nullptr, dj ? h->jf[1] - dj0 : nullptr, dj ? h->jf[2] - dj0 : nullptr};
+    StepMaps sm;
+    sm.ld = h->bmaps_cur;
+    sm.st = h->smaps_alt;
+    const int kb = h->zhalo, ke = h->zhalo + h->g.Nk;
+    const FusedConfig& cf = h->fused_cfg;
+    const WaitCtl wc = h->wait_ctl();
+    switch (h->form) {
+      case Form::F32: return launch_fused1_f32(v.L, v.s32, w.s32, &sm, J, dj, h->cs, ss, step, apps, cf, true, wc, h->stream, kb, ke);
+      case Form::F32C: return launch_fused1_f32(v.L, v.s32c, w.s32c, &sm, J, dj, h->cs, ss, step, apps, cf, true, wc, h->stream, kb, ke);
+      case Form::F16: return launch_fused1_f32(v.L, v.s16, w.s16, &sm, J, dj, h->cs, ss, step, apps, cf, true, wc, h->stream, kb, ke);
+      default: return cudaErrorInvalidValue;
+    }
+  }
   StateView v = h->view();
   StateView w = h->view_alt();
   const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
@@ -383,14 +404,21 @@ namespace fdtd {
 // Second copy of the E/B storage for the fused sweep (allocated on first
 // use) and the TMA maps of both copies for the current tile shape.
 int ensure_alt(fdtd_handle* h) {
+  const size_t eb = elem_bytes(h->form);
+  // a z slab's second copy has halo planes too (its fused step swaps copies)
+  const int64_t halo = h->halo_elems();
   if (!h->alt_field[0]) {
-    const size_t eb = elem_bytes(h->form);
+    const int64_t n = h->L.elems() + 2 * halo;
     for (int c = 0; c < 6; ++c) {
-      FDTD_CUDA(dev_alloc(h, &h->alt_field[c], eb * h->L.elems()), "second field copy");
-      FDTD_CUDA(cudaMemsetAsync(h->alt_field[c], 0, eb * h->L.elems(), h->stream), "zero second copy");
+      void* base = nullptr;
+      FDTD_CUDA(dev_alloc(h, &base, eb * n), "second field copy");
+      FDTD_CUDA(cudaMemsetAsync(base, 0, eb * n, h->stream), "zero second copy");
+      h->alt_field[c] = static_cast<unsigned char*>(base) + eb * halo;
       if (h->form == Form::F32C) {
-        FDTD_CUDA(dev_alloc(h, (void**)&h->alt_lo[c], sizeof(LoT) * h->L.elems()), "second compensation copy");
-        FDTD_CUDA(cudaMemsetAsync(h->alt_lo[c], 0, sizeof(LoT) * h->L.elems(), h->stream), "zero second copy");
+        LoT* lb = nullptr;
+        FDTD_CUDA(dev_alloc(h, (void**)&lb, sizeof(LoT) * n), "second compensation copy");
+        FDTD_CUDA(cudaMemsetAsync(lb, 0, sizeof(LoT) * n, h->stream), "zero second copy");
+        h->alt_lo[c] = lb + halo;
       }
     }
     h->maps_tile_y = 0;
@@ -423,15 +451,28 @@ int ensure_alt(fdtd_handle* h) {
           break;
       }
     }
-    LoT* const* lo_cur = h->form == Form::F32C ? h->lo : nullptr;
-    LoT* const* lo_alt = h->form == Form::F32C ? h->alt_lo : nullptr;
+    // The maps cover the storage: on a z slab its halo planes as well (plane
+    // p of the map is storage plane p, the owned planes being 1..Nk).
+    const PLayout Lm = h->zhalo ? PLayout::make(h->g.Ni, h->g.Nj, h->g.Nk + 2 * h->zhalo) : h->L;
+    void* f_cur[6];
+    void* f_alt[6];
+    LoT* l_cur[6];
+    LoT* l_alt[6];
+    for (int c = 0; c < 6; ++c) {
+      f_cur[c] = static_cast<unsigned char*>(h->field[c]) - eb * halo;
+      f_alt[c] = static_cast<unsigned char*>(h->alt_field[c]) - eb * halo;
+      l_cur[c] = h->form == Form::F32C ? h->lo[c] - halo : nullptr;
+      l_alt[c] = h->form == Form::F32C ? h->alt_lo[c] - halo : nullptr;
+    }
+    LoT* const* lo_cur = h->form == Form::F32C ? l_cur : nullptr;
+    LoT* const* lo_alt = h->form == Form::F32C ? l_alt : nullptr;
     const int ty = h->fused_cfg.tile_y;
     const BoxTrim trim = two ? BoxTrim::None : BoxTrim::EFirst;
-    if (build_tma_maps(&h->maps_cur, h->L, ht, h->field, lo_cur, bw, lbw, ty, trim) != cudaSuccess ||
-        build_tma_maps(&h->maps_alt, h->L, ht, h->alt_field, lo_alt, bw, lbw, ty, trim) != cudaSuccess)
+    if (build_tma_maps(&h->maps_cur, Lm, ht, f_cur, lo_cur, bw, lbw, ty, trim) != cudaSuccess ||
+        build_tma_maps(&h->maps_alt, Lm, ht, f_alt, lo_alt, bw, lbw, ty, trim) != cudaSuccess)
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
-    if (!two && (build_tma_maps(&h->bmaps_cur, h->L, ht, h->field, lo_cur, bbw, blbw, ty, BoxTrim::BFirst) != cudaSuccess ||
-                 build_tma_maps(&h->bmaps_alt, h->L, ht, h->alt_field, lo_alt, bbw, blbw, ty, BoxTrim::BFirst) != cudaSuccess))
+    if (!two && (build_tma_maps(&h->bmaps_cur, Lm, ht, f_cur, lo_cur, bbw, blbw, ty, BoxTrim::BFirst) != cudaSuccess ||
+                 build_tma_maps(&h->bmaps_alt, Lm, ht, f_alt, lo_alt, bbw, blbw, ty, BoxTrim::BFirst) != cudaSuccess))
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
     if (!two && ty != 30) {
       int tw[6], tlw[6];
@@ -441,12 +482,12 @@ int ensure_alt(fdtd_handle* h) {
         default: tblock2_box_widths<StoreF32>(tw, tlw); break;
       }
       // depth-2 boxes: rows y0-2 .. y0+ty+1 for Ex, Ez, y0-2 .. y0+ty otherwise
-      if (build_tma_maps(&h->tmaps_cur, h->L, ht, h->field, lo_cur, tw, tlw, ty + 2, BoxTrim::BFirst) != cudaSuccess ||
-          build_tma_maps(&h->tmaps_alt, h->L, ht, h->alt_field, lo_alt, tw, tlw, ty + 2, BoxTrim::BFirst) != cudaSuccess)
+      if (build_tma_maps(&h->tmaps_cur, Lm, ht, f_cur, lo_cur, tw, tlw, ty + 2, BoxTrim::BFirst) != cudaSuccess ||
+          build_tma_maps(&h->tmaps_alt, Lm, ht, f_alt, lo_alt, tw, tlw, ty + 2, BoxTrim::BFirst) != cudaSuccess)
         return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
     }
-    if (!two && (build_tma_store_maps(&h->smaps_cur, h->L, ht, h->field, lo_cur, ty) != cudaSuccess ||
-                 build_tma_store_maps(&h->smaps_alt, h->L, ht, h->alt_field, lo_alt, ty) != cudaSuccess))
+    if (!two && (build_tma_store_maps(&h->smaps_cur, Lm, ht, f_cur, lo_cur, ty) != cudaSuccess ||
+                 build_tma_store_maps(&h->smaps_alt, Lm, ht, f_alt, lo_alt, ty) != cudaSuccess))
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
     h->maps_tile_y = key;
   }
@@ -1102,8 +1143,8 @@ int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int 
   if (kchunk < 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "kchunk must be >= 0");
   if (cells_per_thread < 0 || cells_per_thread > 2)
     return fail(FDTD_ERR_INVALID_ARGUMENT, "cells_per_thread must be 0 (default), 1 or 2");
-  if (h->zhalo && pipeline == FDTD_PIPELINE_FUSED)
-    return fail(FDTD_ERR_UNSUPPORTED, "a z slab runs the split sweeps");
+  if (h->zhalo && cells_per_thread == 2)
+    return fail(FDTD_ERR_UNSUPPORTED, "a z slab's fused sweep has one cell per thread");
   if (h->fused_cfg.depth == 2 && (cells_per_thread == 2 || tile_y == 30))
     return fail(FDTD_ERR_INVALID_ARGUMENT, "the depth-2 sweep needs cells_per_thread 1 and tile_y 6 or 14");
   h->pipeline = pipeline;
@@ -1116,7 +1157,7 @@ int fdtd_set_pipeline(fdtd_handle* h, int pipeline, int tile_y, int kchunk, int 
 int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out) {
   if (int rc = check_handle(h)) return rc;
   if (h->form == Form::F64) return fail(FDTD_ERR_UNSUPPORTED, "the FP64 form has one pipeline; nothing to tune");
-  if (h->zhalo) return fail(FDTD_ERR_UNSUPPORTED, "a z slab runs the split sweeps; nothing to tune");
+  if (h->zhalo) return fail(FDTD_ERR_UNSUPPORTED, "a z slab has no autotuner (fdtd_set_pipeline sets its fused sweep's shape)");
   if (sweeps <= 0) sweeps = 10;
   DeviceGuard dg(h->device);
   const TuneKey key{(int)h->form, h->g.Ni, h->g.Nj, h->g.Nk};
@@ -1426,9 +1467,21 @@ int fdtd_slab_info(fdtd_handle* h, int* k_begin, int* k_end, int* nk_global) {
 int fdtd_slab_sweep(fdtd_handle* h, int sweep) {
   if (int rc = check_handle(h)) return rc;
   if (h->pml) return fail(FDTD_ERR_UNSUPPORTED, "the PML form steps through fdtd_step");
-  if (sweep < FDTD_SWEEP_B_HALF || sweep > FDTD_SWEEP_B_DEFER) return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid sweep");
+  if (sweep < FDTD_SWEEP_B_HALF || sweep > FDTD_SWEEP_STEP) return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid sweep");
   DeviceGuard dg(h->device);
   switch (sweep) {
+    case FDTD_SWEEP_STEP:
+      // One B-first fused sweep (the single-grid step's kernel, over the
+      // owned planes of the storage): the pending half with the leading one,
+      // then E; the trailing half stays pending.
+      if (h->form == Form::F64) return fail(FDTD_ERR_UNSUPPORTED, "the FP64 form runs the split sweeps");
+      if (h->fused_cfg.cells_per_thread != 1)
+        return fail(FDTD_ERR_UNSUPPORTED, "a z slab's fused sweep has one cell per thread");
+      if (int rc = run_fused(h, h->host_step, h->b_pending ? 2 : 1)) return rc;
+      ++h->host_step;
+      h->b_pending = true;
+      h->b_side = false;
+      return FDTD_OK;
     case FDTD_SWEEP_E:
       if (int rc = resolve_pending(h)) return rc;
       if (int rc = run_e(h, h->host_step)) return rc;
@@ -1483,19 +1536,17 @@ int fdtd_slab_plane(fdtd_handle* h, int comp, int plane, int part, void** device
     return fail(FDTD_ERR_INVALID_ARGUMENT, "only a z slab has halo planes");
   if (part != 0 && !(part == 1 && h->form == Form::F32C))
     return fail(FDTD_ERR_INVALID_ARGUMENT, "part 1 (compensation words) exists in the FP32_COMP form only");
-  if (comp >= FDTD_BX) {
-    // the caller addresses stored B planes: they must hold the whole step (E
-    // planes do not depend on a pending half step)
-    DeviceGuard dg(h->device);
-    if (int rc = resolve_pending(h)) return rc;
-  }
+  // Planes are handed out as stored: with a B half step pending, B lacks it
+  // on every slab alike (the schedules exchange B that way, and the next
+  // sweep applies the half on both sides of each face).
   *device_ptr = slab_plane(h, comp, plane, part, bytes);
   return FDTD_OK;
 }
 
 int fdtd_slab_exchange(fdtd_handle* const* slabs, int n, int halo) {
   if (!slabs || n <= 0) return fail(FDTD_ERR_INVALID_ARGUMENT, "no slabs");
-  if (halo != FDTD_HALO_E && halo != FDTD_HALO_B) return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid halo");
+  if (halo != FDTD_HALO_E && halo != FDTD_HALO_B && halo != FDTD_HALO_STEP)
+    return fail(FDTD_ERR_INVALID_ARGUMENT, "invalid halo");
   for (int s = 0; s < n; ++s)
     if (!slabs[s] || !slabs[s]->zhalo) return fail(FDTD_ERR_INVALID_ARGUMENT, "every handle must be a z slab");
   for (int s = 0; s < n; ++s) {
@@ -1513,30 +1564,43 @@ int fdtd_slab_exchange(fdtd_handle* const* slabs, int n, int halo) {
   DeviceGuard dg(slabs[0]->device);
   // E: slab s's first owned plane of Ex, Ey becomes the halo above of slab
   // s-1.  B: slab s's last owned plane of Bx, By becomes the halo below of
-  // slab s+1.  The ring closes periodically, as the reference's z wrap does.
-  const bool e_halo = halo == FDTD_HALO_E;
-  const int c0 = e_halo ? FDTD_EX : FDTD_BX;
-  const int from = e_halo ? FDTD_PLANE_FIRST : FDTD_PLANE_LAST;
-  const int to = e_halo ? FDTD_PLANE_HALO_ABOVE : FDTD_PLANE_HALO_BELOW;
+  // slab s+1; STEP sends Ex, Ey, Ez of that plane along with them.  The ring
+  // closes periodically, as the reference's z wrap does.
+  struct Group {
+    int comps[5];
+    int n_comps, from, to;
+    bool up;  // sent to the slab above (else below)
+  };
+  Group groups[2];
+  int n_groups = 0;
+  if (halo != FDTD_HALO_B) groups[n_groups++] = {{FDTD_EX, FDTD_EY}, 2, FDTD_PLANE_FIRST, FDTD_PLANE_HALO_ABOVE, false};
+  if (halo == FDTD_HALO_B) groups[n_groups++] = {{FDTD_BX, FDTD_BY}, 2, FDTD_PLANE_LAST, FDTD_PLANE_HALO_BELOW, true};
+  if (halo == FDTD_HALO_STEP)
+    groups[n_groups++] = {{FDTD_BX, FDTD_BY, FDTD_EX, FDTD_EY, FDTD_EZ}, 5, FDTD_PLANE_LAST, FDTD_PLANE_HALO_BELOW, true};
   const int parts = slabs[0]->form == Form::F32C ? 2 : 1;
-  auto dest = [&](int s) { return slabs[e_halo ? (s + n - 1) % n : (s + 1) % n]; };
   for (int s = 0; s < n; ++s) FDTD_CUDA(cudaEventRecord(slabs[s]->xev[0], slabs[s]->stream), "halo exchange");
-  for (int s = 0; s < n; ++s) {
-    fdtd_handle* src = slabs[s];
-    fdtd_handle* dst = dest(s);
-    FDTD_CUDA(cudaStreamWaitEvent(dst->stream, src->xev[0], 0), "halo exchange");
-    for (int c = c0; c < c0 + 2; ++c)
-      for (int part = 0; part < parts; ++part) {
-        size_t nb = 0, nb2 = 0;
-        unsigned char* a = slab_plane(src, c, from, part, &nb);
-        unsigned char* b = slab_plane(dst, c, to, part, &nb2);
-        FDTD_CUDA(cudaMemcpyAsync(b, a, nb, cudaMemcpyDeviceToDevice, dst->stream), "halo exchange");
-      }
+  // Each slab receives on its own stream, after its sources' queued work.
+  for (int d = 0; d < n; ++d) {
+    fdtd_handle* dst = slabs[d];
+    for (int g = 0; g < n_groups; ++g) {
+      const Group& q = groups[g];
+      fdtd_handle* src = slabs[q.up ? (d + n - 1) % n : (d + 1) % n];
+      FDTD_CUDA(cudaStreamWaitEvent(dst->stream, src->xev[0], 0), "halo exchange");
+      for (int i = 0; i < q.n_comps; ++i)
+        for (int part = 0; part < parts; ++part) {
+          size_t nb = 0, nb2 = 0;
+          unsigned char* a = slab_plane(src, q.comps[i], q.from, part, &nb);
+          unsigned char* b = slab_plane(dst, q.comps[i], q.to, part, &nb2);
+          FDTD_CUDA(cudaMemcpyAsync(b, a, nb, cudaMemcpyDeviceToDevice, dst->stream), "halo exchange");
+        }
+    }
   }
   // A slab rewrites the planes it sent only after the copies have read them.
   for (int s = 0; s < n; ++s) FDTD_CUDA(cudaEventRecord(slabs[s]->xev[1], slabs[s]->stream), "halo exchange");
   for (int s = 0; s < n; ++s)
-    FDTD_CUDA(cudaStreamWaitEvent(slabs[s]->stream, dest(s)->xev[1], 0), "halo exchange");
+    for (int g = 0; g < n_groups; ++g)
+      FDTD_CUDA(cudaStreamWaitEvent(slabs[s]->stream, slabs[groups[g].up ? (s + 1) % n : (s + n - 1) % n]->xev[1], 0),
+                "halo exchange");
   return FDTD_OK;
 }
 

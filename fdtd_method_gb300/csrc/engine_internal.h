@@ -127,11 +127,14 @@ int fused_lo_box_width();
 // `maps` is a StepMaps: load maps of `st`'s arrays (built with the trim of
 // the sweep order), store maps of `out`'s.  b_first: the B-first sweep (B
 // half steps, then E), otherwise the E-first one (E, then B half steps).
+// [kbeg, kend) are the planes it updates (kend < 0: Nk); a z slab's storage
+// sweeps [1, nk+1) and reads its halo planes 0 and nk+1 unwrapped (B-first).
 template <class S>
 cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const void* maps,
                               const float* const J[3], bool dense_j, const CoefSet& cs,
                               const SourceSet& ss, int64_t step, int applications,
-                              const FusedConfig& cfg, bool b_first, const WaitCtl& wc, cudaStream_t stream);
+                              const FusedConfig& cfg, bool b_first, const WaitCtl& wc, cudaStream_t stream,
+                              int kbeg = 0, int kend = -1);
 // Per-component box widths (hi and lo words) of the one-cell kernel's load
 // maps, for its E-first or B-first sweep.
 template <class S>

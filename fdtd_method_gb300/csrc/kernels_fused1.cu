@@ -255,7 +255,7 @@ __device__ __forceinline__ void drain_tile(uint64_t* bar, uint32_t ring, int fir
 
 template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSrc>
 __device__ __forceinline__ bool fused1_planes(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
-                                              const CoefSet& cs, int bx, int by, int bz, int kchunk,
+                                              const CoefSet& cs, int bx, int by, int bz, int kchunk, int2 zr,
                                               const float* __restrict__ Jx, const float* __restrict__ Jy,
                                               const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
                                               const WaitCtl& wc, unsigned char* smem, uint32_t& ring, int nsrc) {
@@ -279,8 +279,8 @@ __device__ __forceinline__ bool fused1_planes(const PLayout& L, const S& st, con
   // logical coordinates (x = Ni and y = Nj are the ghost copies of 0)
   const int xu = x0 + cx, yu = y0 + r - 1;
   const int xl = xu >= L.Ni ? xu - L.Ni : xu, yl = yu >= L.Nj ? yu - L.Nj : yu;
-  const int k0 = bz * kchunk;
-  const int k1 = min(k0 + kchunk, L.Nk);
+  const int k0 = zr.x + bz * kchunk;
+  const int k1 = min(k0 + kchunk, zr.y);
   // The copy-engine leader (ring refills, bulk stores and their waits) is
   // lane 0 of the halo-column warp, which has the least arithmetic per plane.
   const bool leader = (w == RY + 1 && lane == 0);
@@ -582,7 +582,7 @@ __device__ __forceinline__ bool fused1_planes(const PLayout& L, const S& st, con
 // k0-1.  Same contract as fused1_planes.
 template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSrc>
 __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
-                                               const CoefSet& cs, int bx, int by, int bz, int kchunk,
+                                               const CoefSet& cs, int bx, int by, int bz, int kchunk, int2 zr,
                                                const float* __restrict__ Jx, const float* __restrict__ Jy,
                                                const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
                                                const WaitCtl& wc, unsigned char* smem, uint32_t& ring, int nsrc) {
@@ -607,8 +607,8 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
   // unwrapped coordinates (x = -1 and y = -1 are the ghost copies of Ni-1 and
   // Nj-1); interior cells have 0 <= x < Ni, 0 <= y < Nj
   const int xu = x0 + cx, yu = y0 + r - 1;
-  const int k0 = bz * kchunk;
-  const int k1 = min(k0 + kchunk, L.Nk);
+  const int k0 = zr.x + bz * kchunk;
+  const int k1 = min(k0 + kchunk, zr.y);
   const int n_it = k1 - k0 + 1;
   const bool leader = (w == RY + 1 && lane == 0);
   const int slot0 = (int)(ring % NS);
@@ -897,7 +897,7 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
 // the CTA).
 template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSplit, bool kBF>
 __device__ __forceinline__ bool fused1_tile(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
-                                            const CoefSet& cs, int bx, int by, int bz, int kchunk,
+                                            const CoefSet& cs, int bx, int by, int bz, int kchunk, int2 zr,
                                             const float* __restrict__ Jx, const float* __restrict__ Jy,
                                             const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
                                             const WaitCtl& wc, unsigned char* smem, uint32_t& ring) {
@@ -927,9 +927,9 @@ __device__ __forceinline__ bool fused1_tile(const PLayout& L, const S& st, const
   __syncthreads();
   const int nsrc = list[kMaxSources];
 #define FDTD_PLANES(SRC, NSRC)                                                                                   \
-  return kBF ? fused1b_planes<S, A, RY, kApps, kDenseJ, SRC>(L, st, out, maps, cs, bx, by, bz, kchunk, Jx, Jy, Jz, \
+  return kBF ? fused1b_planes<S, A, RY, kApps, kDenseJ, SRC>(L, st, out, maps, cs, bx, by, bz, kchunk, zr, Jx, Jy, Jz, \
                                                             ss, step, wc, smem, ring, NSRC)                      \
-             : fused1_planes<S, A, RY, kApps, kDenseJ, SRC>(L, st, out, maps, cs, bx, by, bz, kchunk, Jx, Jy, Jz,  \
+             : fused1_planes<S, A, RY, kApps, kDenseJ, SRC>(L, st, out, maps, cs, bx, by, bz, kchunk, zr, Jx, Jy, Jz, \
                                                            ss, step, wc, smem, ring, NSRC)
   if (!kSplit || nsrc > 0) FDTD_PLANES(true, nsrc);
   FDTD_PLANES(false, 0);
@@ -947,13 +947,13 @@ __device__ __forceinline__ void init_ring(uint64_t* bar) {
 
 template <class S, class A, int RY, int kApps, bool kDenseJ, bool kBF>
 __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
-    fused1(PLayout L, S st, S out, const __grid_constant__ StepMaps maps, CoefSet cs, int kchunk,
+    fused1(PLayout L, S st, S out, const __grid_constant__ StepMaps maps, CoefSet cs, int kchunk, int2 zr,
            const float* __restrict__ Jx, const float* __restrict__ Jy, const float* __restrict__ Jz,
            SourceSet ss, int64_t step, WaitCtl wc) {
   extern __shared__ __align__(128) unsigned char smem[];
   init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY, kBF>::kBar));
   uint32_t ring = 0;
-  fused1_tile<S, A, RY, kApps, kDenseJ, true, kBF>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z, kchunk,
+  fused1_tile<S, A, RY, kApps, kDenseJ, true, kBF>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z, kchunk, zr,
                                                    Jx, Jy, Jz, ss, step, wc, smem, ring);
   if (threadIdx.x == 0 && threadIdx.y == RY + 1) bulk_wait_all();  // the copy-engine leader's stores
 }
@@ -998,7 +998,8 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
     }
     __syncthreads();
     const bool ok = fused1_tile<S, A, RY, kApps, false, kSplit, true>(
-        dom.L, dom.s[parity], dom.s[parity ^ 1], maps[2 * w.x + parity], dom.cs, w.y, w.z, w.w, kchunk, nullptr,
+        dom.L, dom.s[parity], dom.s[parity ^ 1], maps[2 * w.x + parity], dom.cs, w.y, w.z, w.w, kchunk,
+        make_int2(0, dom.L.Nk), nullptr,
         nullptr, nullptr, dom.ss, step, wc, smem, ring);
     if (!ok) break;  // a wait gave up: this CTA takes no more tiles
     __syncthreads();
@@ -1017,25 +1018,27 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
 
 template <class S, int RY, int APPS, bool DJ, bool BF>
 static cudaError_t launch1_one(dim3 grid, const PLayout& L, const S& st, const S& out, const StepMaps& maps,
-                               const CoefSet& cs, int kchunk, const float* const J[3], const SourceSet& ss,
+                               const CoefSet& cs, int kchunk, int2 zr, const float* const J[3], const SourceSet& ss,
                                int64_t step, const WaitCtl& wc, cudaStream_t stream) {
   using A = typename ArithOf1<S>::type;
   auto kern = fused1<S, A, RY, APPS, DJ, BF>;
   const int bytes = Plan1<S, RY, BF>::kTotal;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
-  kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(L, st, out, maps, cs, kchunk, J[0], J[1], J[2], ss, step, wc);
+  kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(L, st, out, maps, cs, kchunk, zr, J[0], J[1], J[2], ss, step, wc);
   return cudaGetLastError();
 }
 
 template <class S, int RY, bool BF>
 static cudaError_t launch1_ry(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                               const float* const J[3], bool dense_j, const CoefSet& cs, const SourceSet& ss,
-                              int64_t step, int applications, int kchunk, const WaitCtl& wc, cudaStream_t stream) {
+                              int64_t step, int applications, int kchunk, int2 zr, const WaitCtl& wc,
+                              cudaStream_t stream) {
   if (ss.count > kMaxSources) return cudaErrorInvalidValue;
-  dim3 grid((L.Ni + 31) / 32, (L.Nj + RY - 1) / RY, (L.Nk + kchunk - 1) / kchunk);
+  if (zr.x < 0 || zr.y > L.Nk || zr.y <= zr.x) return cudaErrorInvalidValue;
+  dim3 grid((L.Ni + 31) / 32, (L.Nj + RY - 1) / RY, (zr.y - zr.x + kchunk - 1) / kchunk);
 #define FDTD_F(APPS, DJ) \
-  return launch1_one<S, RY, APPS, DJ, BF>(grid, L, st, out, maps, cs, kchunk, J, ss, step, wc, stream)
+  return launch1_one<S, RY, APPS, DJ, BF>(grid, L, st, out, maps, cs, kchunk, zr, J, ss, step, wc, stream)
   if (applications == 2) {
     if (dense_j) FDTD_F(2, true);
     FDTD_F(2, false);
@@ -1049,12 +1052,14 @@ template <class S>
 cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const void* maps,
                               const float* const J[3], bool dense_j, const CoefSet& cs, const SourceSet& ss,
                               int64_t step, int applications, const FusedConfig& cfg, bool b_first,
-                              const WaitCtl& wc, cudaStream_t stream) {
+                              const WaitCtl& wc, cudaStream_t stream, int kbeg, int kend) {
   const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 48;
   const StepMaps& m = *static_cast<const StepMaps*>(maps);
-#define FDTD_RY(RY)                                                                                                 \
-  return b_first ? launch1_ry<S, RY, true>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, wc, stream) \
-                 : launch1_ry<S, RY, false>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, wc, stream)
+  const int2 zr = make_int2(kbeg, kend < 0 ? L.Nk : kend);
+#define FDTD_RY(RY)                                                                                               \
+  return b_first                                                                                                  \
+             ? launch1_ry<S, RY, true>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, zr, wc, stream) \
+             : launch1_ry<S, RY, false>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, zr, wc, stream)
   if (cfg.tile_y == 6) FDTD_RY(6);
   if (cfg.tile_y == 30) FDTD_RY(30);
   FDTD_RY(14);
@@ -1118,7 +1123,8 @@ void fused1_box_widths(bool b_first, int hi[6], int lo[6]) {
 #define FDTD_INSTANTIATE(S)                                                                              \
   template cudaError_t launch_fused1_f32<S>(const PLayout&, const S&, const S&, const void*,            \
                                             const float* const[3], bool, const CoefSet&, const SourceSet&, \
-                                            int64_t, int, const FusedConfig&, bool, const WaitCtl&, cudaStream_t); \
+                                            int64_t, int, const FusedConfig&, bool, const WaitCtl&, cudaStream_t,   \
+                                            int, int);                                                     \
   template cudaError_t launch_fused1_batch<S>(const void*, const StepMaps*, const int4*, int, int, int,          \
                                               const FusedConfig&, const int64_t*, int, int*, const WaitCtl&,     \
                                               cudaStream_t);                                                     \

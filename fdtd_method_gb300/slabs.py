@@ -17,7 +17,10 @@ planes with one halo plane below and one above; its sweeps update the owned
 planes only, and a halo exchange fills the halo planes.  ``step_schedule``
 is the order of sweeps and exchanges that makes a set of slabs step exactly
 like one handle of the whole grid (bit for bit: every cell sees the same
-operands in the same order).  ``FDTDSlabs`` runs it on one GPU, the slabs
+operands in the same order).  In the FP32-arithmetic forms a step can also be
+one fused sweep (SWEEP_STEP: the single-grid engine's B-first kernel over the
+owned planes), which reads E and B of the halo plane below and E of the one
+above, so its exchange (HALO_STEP) carries Ex, Ey, Ez with Bx, By.  ``FDTDSlabs`` runs it on one GPU, the slabs
 exchanging through device copies (``fdtd_slab_exchange``);
 ``ring_exchange`` is the same exchange between processes over
 torch.distributed, one slab per rank.
@@ -30,8 +33,8 @@ from . import _lib
 from ._lib import InvalidArgument
 from .fdtd import FDTD, Parameters, Precision, Const
 
-SWEEP_B_HALF, SWEEP_B_DOUBLE, SWEEP_E, SWEEP_B_DEFER = 0, 1, 2, 3
-HALO_E, HALO_B = 0, 1
+SWEEP_B_HALF, SWEEP_B_DOUBLE, SWEEP_E, SWEEP_B_DEFER, SWEEP_STEP = 0, 1, 2, 3, 4
+HALO_E, HALO_B, HALO_STEP = 0, 1, 2
 PLANE_HALO_BELOW, PLANE_FIRST, PLANE_LAST, PLANE_HALO_ABOVE = 0, 1, 2, 3
 
 
@@ -50,9 +53,9 @@ def slab_bounds(nk, n):
     return out
 
 
-def step_schedule(n, defer=False, pending=False):
+def step_schedule(n, defer=False, pending=False, fused=False):
     """The operations of n update_fields steps on a set of slabs, in order:
-    ("exchange", HALO_E | HALO_B) or ("sweep", SWEEP_*).
+    ("exchange", HALO_*) or ("sweep", SWEEP_*).
 
     One step is B/2, E, B/2 (src/FDTD_kokkos/FDTD_kokkos.cpp:91-104); the
     trailing B half step of one step and the leading one of the next share a
@@ -60,10 +63,23 @@ def step_schedule(n, defer=False, pending=False):
     last step's trailing half is left pending (SWEEP_B_DEFER, the
     FP32-arithmetic forms), and a call made with `pending` starts with the
     double sweep that applies it.  The E halo is exchanged first, so fields
-    set from the host since the last step are seen across the slab faces."""
+    set from the host since the last step are seen across the slab faces.
+
+    With `fused` (FP32-arithmetic forms: it needs `defer`), each step is one
+    SWEEP_STEP, which applies the pending half itself; an exchange precedes
+    the first sweep and follows every sweep, so the halo planes are current
+    for any reader that applies the pending half between calls."""
     n = int(n)
     if n <= 0:
         return []
+    if fused:
+        if not defer:
+            raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT,
+                                  "the fused schedule leaves the trailing B half pending (defer)")
+        ops = [("exchange", HALO_STEP)]
+        for _ in range(n):
+            ops += [("sweep", SWEEP_STEP), ("exchange", HALO_STEP)]
+        return ops
     ops = [("exchange", HALO_E), ("sweep", SWEEP_B_DOUBLE if pending else SWEEP_B_HALF)]
     for s in range(n):
         last = SWEEP_B_DEFER if defer else SWEEP_B_HALF
@@ -72,35 +88,50 @@ def step_schedule(n, defer=False, pending=False):
     return ops
 
 
-def halo_planes(halo):
-    """(components, sent plane, received plane) of an exchange: E sends Ex, Ey
-    of each slab's first plane to the slab below's halo above; B sends Bx, By
-    of each slab's last plane to the slab above's halo below."""
+def halo_groups(halo):
+    """The parts of an exchange: a list of (components, sent plane, received
+    plane, sent to the slab above).  E sends Ex, Ey of each slab's first
+    plane to the slab below's halo above; B sends Bx, By of each slab's last
+    plane to the slab above's halo below; STEP sends the E part and Bx, By,
+    Ex, Ey, Ez of the last plane to the slab above's halo below."""
+    e = ((0, 1), PLANE_FIRST, PLANE_HALO_ABOVE, False)
     if halo == HALO_E:
-        return (0, 1), PLANE_FIRST, PLANE_HALO_ABOVE
-    return (3, 4), PLANE_LAST, PLANE_HALO_BELOW
+        return [e]
+    if halo == HALO_B:
+        return [((3, 4), PLANE_LAST, PLANE_HALO_BELOW, True)]
+    if halo == HALO_STEP:
+        return [e, ((3, 4, 0, 1, 2), PLANE_LAST, PLANE_HALO_BELOW, True)]
+    raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "invalid halo")
+
+
+def halo_planes(halo):
+    """(components, sent plane, received plane) of HALO_E or HALO_B."""
+    g = halo_groups(halo)
+    if len(g) != 1:
+        raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "the exchange has several parts: use halo_groups")
+    return g[0][:3]
 
 
 def ring_exchange(send, recv, halo, rank, world, group=None):
     """Halo exchange between processes, one slab per rank in plane order (the
     grid is periodic: rank world-1's neighbour above is rank 0).  send /
-    recv: per component of ``halo_planes(halo)``, the tensor of the plane
-    this rank sends and the tensor its halo plane is received into.  E goes
-    to the rank below, B to the rank above (coarray/fdtd.F90:90-91, 97-98)."""
+    recv: per component of ``halo_groups(halo)``, in order, the tensor of the
+    plane this rank sends and the tensor its halo plane is received into.  E
+    goes to the rank below, B to the rank above (coarray/fdtd.F90:90-91,
+    97-98)."""
     import torch.distributed as dist
-    comps, _, _ = halo_planes(halo)
-    if halo == HALO_E:
-        to, frm = (rank - 1) % world, (rank + 1) % world
-    else:
-        to, frm = (rank + 1) % world, (rank - 1) % world
-    if world == 1:
-        for c in range(len(comps)):
-            recv[c].copy_(send[c])
-        return
     reqs = []
-    for c in range(len(comps)):
-        reqs.append(dist.isend(send[c], to, group=group, tag=10 * halo + c))
-        reqs.append(dist.irecv(recv[c], frm, group=group, tag=10 * halo + c))
+    q = 0
+    for g, (comps, _, _, up) in enumerate(halo_groups(halo)):
+        to, frm = ((rank + 1) % world, (rank - 1) % world) if up else ((rank - 1) % world, (rank + 1) % world)
+        for c in range(len(comps)):
+            if world == 1:
+                recv[q].copy_(send[q])
+            else:
+                tag = 100 * halo + 10 * g + c
+                reqs.append(dist.isend(send[q], to, group=group, tag=tag))
+                reqs.append(dist.irecv(recv[q], frm, group=group, tag=tag))
+            q += 1
     for r in reqs:
         r.wait()
 
@@ -132,8 +163,9 @@ class Slab(FDTD):
                                      parameters.dx, parameters.dy, parameters.dz)
 
     def sweep(self, kind):
-        """One sweep over the owned planes (SWEEP_B_HALF, SWEEP_B_DOUBLE or
-        SWEEP_E; SWEEP_E advances the step count)."""
+        """One sweep over the owned planes (SWEEP_B_HALF, SWEEP_B_DOUBLE,
+        SWEEP_E, SWEEP_B_DEFER or SWEEP_STEP; SWEEP_E and SWEEP_STEP advance
+        the step count)."""
         _lib.check(self._lib.fdtd_slab_sweep(self._handle(), int(kind)))
 
     def plane(self, comp, which, part=0):
@@ -151,7 +183,7 @@ class FDTDSlabs:
     sources, step count) are those of one FDTD of the whole grid in the same
     precision, bit for bit."""
 
-    def __init__(self, parameters, dt, n_slabs, precision=Precision.FP64):
+    def __init__(self, parameters, dt, n_slabs, precision=Precision.FP64, fused=None):
         self.parameters = parameters
         self.dt = float(dt)
         self.precision = Precision(precision)
@@ -169,6 +201,11 @@ class FDTDSlabs:
         # as the whole-grid handle does (the FP64 form applies every half)
         self._defer = self.precision != Precision.FP64
         self._pending = False
+        # one fused sweep per step (FP32-arithmetic forms; the default there)
+        self.fused = self._defer if fused is None else bool(fused)
+        if self.fused and not self._defer:
+            self.close()
+            raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "the FP64 form runs the split sweeps")
 
     def close(self):
         for s in self.slabs:
@@ -201,7 +238,7 @@ class FDTDSlabs:
             raise InvalidArgument(_lib.FDTD_ERR_INVALID_ARGUMENT, "negative step count")
         if int(n) == 0:
             return
-        for op, arg in step_schedule(n, self._defer, self._pending):
+        for op, arg in step_schedule(n, self._defer, self._pending, self.fused):
             if op == "exchange":
                 self.exchange(arg)
             else:

@@ -399,8 +399,15 @@ int fdtd_sync(fdtd_handle* h);
  *     steps and after the last one B_DEFER (FP32-arithmetic forms; B_HALF in
  *     the FP64 form):
  * the results are the whole-grid handle's bit for bit, in every precision.
- * fdtd_step on a slab gives FDTD_ERR_UNSUPPORTED; slabs run the split sweeps
- * (no fused pipeline, no autotuner) and have no PML.
+ * In the FP32-arithmetic forms a call may instead run the fused schedule,
+ *     exchange STEP, then per step: STEP, exchange STEP
+ * (one fused sweep and one exchange per step; the trailing B half stays
+ * pending as above, and the exchange after each sweep keeps the halo planes
+ * current for readers that apply it).  Both schedules give the whole-grid
+ * handle's bits and may alternate between calls.
+ * fdtd_step on a slab gives FDTD_ERR_UNSUPPORTED; slabs take no autotuner
+ * (the fused sweep uses the handle's launch shape: fdtd_set_pipeline with one
+ * cell per thread) and have no PML.
  *
  * One GPU: fdtd_slab_exchange copies the boundary planes between the slabs
  * of one device.  Several GPUs: each rank exchanges the planes that
@@ -415,11 +422,19 @@ enum fdtd_sweep {
     FDTD_SWEEP_B_HALF = 0,   /* B += curl term (kokkos_functors.h:128-151), once  */
     FDTD_SWEEP_B_DOUBLE = 1, /* the same term added twice (two half steps)        */
     FDTD_SWEEP_E = 2,        /* E update of the current step; the step count + 1  */
-    FDTD_SWEEP_B_DEFER = 3   /* no sweep: the step's trailing B half is left
+    FDTD_SWEEP_B_DEFER = 3,  /* no sweep: the step's trailing B half is left
                                 pending (FP32-arithmetic forms), as fdtd_step
                                 leaves it; the next B_DOUBLE sweep applies it
                                 with the next step's leading half, readers of
                                 B see it applied, writers apply it first      */
+    FDTD_SWEEP_STEP = 4      /* a whole update_fields step as one fused
+                                B-first sweep (FP32-arithmetic forms): the
+                                pending B half, if any, and the step's leading
+                                half, then E; the trailing half is left
+                                pending (as B_DEFER); the step count + 1.
+                                Reads Bx, By, Ex, Ey, Ez of the halo below and
+                                Ex, Ey of the halo above: run FDTD_HALO_STEP
+                                before it                                     */
 };
 /* One sweep over the owned planes (any non-PML handle: the whole grid).  With
  * a B half step pending, B_HALF applies it and B_DOUBLE applies it and one
@@ -430,8 +445,10 @@ enum fdtd_plane {
     FDTD_PLANE_HALO_BELOW = 0, FDTD_PLANE_FIRST = 1, FDTD_PLANE_LAST = 2, FDTD_PLANE_HALO_ABOVE = 3
 };
 enum fdtd_halo {
-    FDTD_HALO_E = 0, /* Ex, Ey of each slab's first plane -> the halo above of the slab below */
-    FDTD_HALO_B = 1  /* Bx, By of each slab's last plane  -> the halo below of the slab above */
+    FDTD_HALO_E = 0,    /* Ex, Ey of each slab's first plane -> the halo above of the slab below */
+    FDTD_HALO_B = 1,    /* Bx, By of each slab's last plane  -> the halo below of the slab above */
+    FDTD_HALO_STEP = 2  /* what FDTD_SWEEP_STEP reads: HALO_E, and Bx, By, Ex, Ey, Ez of each
+                           slab's last plane -> the halo below of the slab above */
 };
 /* Device address and size in bytes of one stored plane of component comp
  * (FDTD_EX..FDTD_BZ) in the handle's storage form: part 0 the E/B words,

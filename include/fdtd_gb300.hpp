@@ -207,11 +207,13 @@ class FDTD_PML : public FDTD {
 // reference's coarray program (coarray/fdtd.F90:149-164: the first Nk mod n
 // slabs get one plane more) with its halo exchange (:86-102) as device
 // copies.  Results equal one FDTD of the whole grid in the same precision,
-// bit for bit.
+// bit for bit.  The FP32-arithmetic forms run one fused sweep per step
+// (FDTD_SWEEP_STEP) unless `fused` is false; the FP64 form runs the split
+// sweeps.
 class Slabs {
  public:
-  Slabs(Parameters parameters, FP dt, int n_slabs, Precision precision = Precision::FP64)
-      : parameters_(parameters), defer_(precision != Precision::FP64) {
+  Slabs(Parameters parameters, FP dt, int n_slabs, Precision precision = Precision::FP64, bool fused = true)
+      : parameters_(parameters), defer_(precision != Precision::FP64), fused_(fused && defer_) {
     if (n_slabs <= 0 || n_slabs > parameters.Nk) throw std::invalid_argument("need 1 <= slabs <= Nk");
     fdtd_params p{parameters.Ni, parameters.Nj, parameters.Nk, parameters.ax, parameters.bx, parameters.ay,
                   parameters.by, parameters.az, parameters.bz, parameters.dx, parameters.dy, parameters.dz};
@@ -247,9 +249,19 @@ class Slabs {
   // exchange E, B (the trailing and leading B halves of consecutive steps in
   // one sweep).  The FP32-arithmetic forms leave the last step's trailing
   // half pending, as a whole-grid handle does, and the next call's first
-  // sweep applies it with that call's leading half.
+  // sweep applies it with that call's leading half.  Fused: an exchange,
+  // then per step one fused sweep and an exchange.
   void step(int64_t n) {
     if (n <= 0) return;
+    if (fused_) {
+      exchange(FDTD_HALO_STEP);
+      for (int64_t s = 0; s < n; ++s) {
+        sweep(FDTD_SWEEP_STEP);
+        exchange(FDTD_HALO_STEP);
+      }
+      pending_ = true;
+      return;
+    }
     exchange(FDTD_HALO_E);
     sweep(pending_ ? FDTD_SWEEP_B_DOUBLE : FDTD_SWEEP_B_HALF);
     for (int64_t s = 0; s < n; ++s) {
@@ -290,6 +302,7 @@ class Slabs {
   }
   Parameters parameters_;
   bool defer_;            // leave the last trailing B half pending (not FP64)
+  bool fused_;            // one fused sweep per step (FP32-arithmetic forms)
   bool pending_ = false;  // a trailing B half step is pending on every slab
   std::vector<fdtd_handle*> slabs_;
   std::vector<std::pair<int, int>> bounds_;

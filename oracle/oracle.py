@@ -244,6 +244,7 @@ class OracleSlab:
         self.plane = params.Ni * params.Nj
         self.f = [np.zeros(self.plane * (self.nk + 2)) for _ in range(9)]
         self.step_index = 0
+        self.pending = False  # a trailing B half step left pending (sweep kinds 3, 4)
 
     def owned(self, comp):
         """View of the owned planes of component comp (flat, i fastest)."""
@@ -254,17 +255,44 @@ class OracleSlab:
         return self.f[int(comp)][self.plane * k:self.plane * (k + 1)]
 
     def sweep(self, kind):
-        """kind 0: B half step, 1: two B half steps, 2: E (kokkos_functors.h:128-151, :64-90)."""
+        """kind 0: B half step, 1: two B half steps, 2: E (kokkos_functors.h:128-151, :64-90),
+        3: leave the step's trailing B half pending, 4: a whole step as the
+        fused slab sweep does it: the pending half (if any) and the leading
+        one on the owned planes and the halo plane below (which holds the
+        neighbour's last plane of B and E), then E on the owned planes; the
+        trailing half is left pending.  2 applies a pending half first; 0 and
+        1 count it as their first half."""
         box = OracleBox(0, self.Ni, 0, self.Nj, 1, self.nk + 1)
         nk = self.nk + 2
         f, c = self.f, self.coef
-        if kind == 2:
+
+        def b_half(b):
+            oracle_lib().oracle_update_B_box(self.Ni, self.Nj, nk, b, *[_ptr(f[q]) for q in range(6)], c[3], c[4], c[5])
+
+        def e_sweep():
             oracle_lib().oracle_update_E_box(self.Ni, self.Nj, nk, box, *[_ptr(f[q]) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)],
                                              c[6], c[0], c[1], c[2])
             self.step_index += 1
+
+        if kind == 3:
+            self.pending = True
+            return
+        if kind == 4:
+            wide = OracleBox(0, self.Ni, 0, self.Nj, 0, self.nk + 1)
+            for _ in range(2 if self.pending else 1):
+                b_half(wide)
+            e_sweep()
+            self.pending = True
+            return
+        if kind == 2:
+            if self.pending:
+                b_half(box)
+                self.pending = False
+            e_sweep()
             return
         for _ in range(2 if kind == 1 else 1):
-            oracle_lib().oracle_update_B_box(self.Ni, self.Nj, nk, box, *[_ptr(f[q]) for q in range(6)], c[3], c[4], c[5])
+            b_half(box)
+        self.pending = False
 
 
 # ---------------------------------------------------------------------------

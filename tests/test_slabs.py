@@ -71,6 +71,21 @@ def test_schedule_with_a_pending_half_step():
     assert first[:-1] + second == whole
 
 
+def test_fused_schedule():
+    """One fused sweep per step, each followed by an exchange of what the next
+    one reads (and what a reader applying the pending half reads)."""
+    ops = slabs.step_schedule(3, defer=True, fused=True)
+    assert ops == [("exchange", slabs.HALO_STEP)] + [("sweep", slabs.SWEEP_STEP), ("exchange", slabs.HALO_STEP)] * 3
+    with pytest.raises(ValueError):
+        slabs.step_schedule(2, fused=True)
+    # the halo the fused sweep reads: E above; B and E below
+    groups = slabs.halo_groups(slabs.HALO_STEP)
+    assert groups == [((0, 1), slabs.PLANE_FIRST, slabs.PLANE_HALO_ABOVE, False),
+                      ((3, 4, 0, 1, 2), slabs.PLANE_LAST, slabs.PLANE_HALO_BELOW, True)]
+    with pytest.raises(ValueError):
+        slabs.halo_planes(slabs.HALO_STEP)
+
+
 def _initial_fields(p, seed):
     rng = np.random.default_rng(seed)
     n = p.Ni * p.Nj * p.Nk
@@ -94,17 +109,34 @@ def _whole_grid(p, dt, fields, steps):
     return [o.get(c) for c in range(6)]
 
 
-def _run_slab(slab, rank, world, fields, plane, k0, k1, steps, exchange):
+def _run_slab(slab, rank, world, fields, plane, k0, k1, steps, exchange, fused=False):
     for c in range(9):
         slab.owned(c)[...] = fields[c][k0 * plane:k1 * plane]
-    for op, arg in slabs.step_schedule(steps):
+    for op, arg in slabs.step_schedule(steps, defer=fused, fused=fused):
         if op == "sweep":
             slab.sweep(arg)
         else:
             exchange(arg)
+    if fused:
+        slab.sweep(slabs.SWEEP_B_HALF)
 
 
-def test_oracle_slabs_in_one_process_equal_the_whole_grid():
+def _exchange_in_process(ss, halo):
+    n = len(ss)
+    for comps, frm, to, up in slabs.halo_groups(halo):
+        for r, s in enumerate(ss):
+            dst = ss[(r + 1) % n] if up else ss[(r - 1) % n]
+            kf = 1 if frm == slabs.PLANE_FIRST else s.nk
+            kt = dst.nk + 1 if to == slabs.PLANE_HALO_ABOVE else 0
+            for c in comps:
+                dst.plane_view(c, kt)[...] = s.plane_view(c, kf)
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_oracle_slabs_in_one_process_equal_the_whole_grid(fused):
+    """The split schedule, and the fused one in FP64 arithmetic (two calls of
+    3 steps; the pending half applied at the end by a B half sweep, which
+    reads the E halo the last exchange left current)."""
     from oracle import OracleSlab
     p = normalised_parameters(12, 10, 23)
     fields = _initial_fields(p, 5)
@@ -116,25 +148,21 @@ def test_oracle_slabs_in_one_process_equal_the_whole_grid():
         for s, (k0, k1) in zip(ss, bounds):
             for c in range(9):
                 s.owned(c)[...] = fields[c][k0 * plane:k1 * plane]
-
-        def exchange(halo):
-            comps, frm, to = slabs.halo_planes(halo)
-            for r, s in enumerate(ss):
-                dst = ss[(r - 1) % n] if halo == slabs.HALO_E else ss[(r + 1) % n]
-                kf = 1 if frm == slabs.PLANE_FIRST else s.nk
-                kt = dst.nk + 1 if to == slabs.PLANE_HALO_ABOVE else 0
-                for c in comps:
-                    dst.plane_view(c, kt)[...] = s.plane_view(c, kf)
-
-        for op, arg in slabs.step_schedule(6):
-            if op == "sweep":
-                for s in ss:
-                    s.sweep(arg)
-            else:
-                exchange(arg)
+        calls = [(3, False), (3, True)] if fused else [(6, False)]
+        for steps, pending in calls:
+            for op, arg in slabs.step_schedule(steps, defer=fused, pending=pending, fused=fused):
+                if op == "sweep":
+                    for s in ss:
+                        s.sweep(arg)
+                else:
+                    _exchange_in_process(ss, arg)
+        if fused:
+            for s in ss:
+                s.sweep(slabs.SWEEP_B_HALF)
         for c in range(6):
             got = np.concatenate([s.owned(c) for s in ss])
             assert np.array_equal(got, want[c]), (n, c)
+        assert all(s.step_index == 6 for s in ss)
 
 
 def _free_port():
@@ -143,7 +171,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _rank(rank, world, port, steps, out):
+def _rank(rank, world, port, steps, out, fused=False):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
                       OMP_NUM_THREADS="1")
     sys.path.insert(0, ROOT)
@@ -160,23 +188,26 @@ def _rank(rank, world, port, steps, out):
     slab = OracleSlab(p, dt, k0, k1)
 
     def exchange(halo):
-        comps, frm, to = sl.halo_planes(halo)
-        kf = 1 if frm == sl.PLANE_FIRST else slab.nk
-        kt = slab.nk + 1 if to == sl.PLANE_HALO_ABOVE else 0
-        send = [torch.from_numpy(slab.plane_view(c, kf).copy()) for c in comps]
-        recv = [torch.empty_like(t) for t in send]
+        send, recv, dst = [], [], []
+        for comps, frm, to, _ in sl.halo_groups(halo):
+            kf = 1 if frm == sl.PLANE_FIRST else slab.nk
+            kt = slab.nk + 1 if to == sl.PLANE_HALO_ABOVE else 0
+            for c in comps:
+                send.append(torch.from_numpy(slab.plane_view(c, kf).copy()))
+                recv.append(torch.empty_like(send[-1]))
+                dst.append((c, kt))
         sl.ring_exchange(send, recv, halo, rank, world)
-        for c, t in zip(comps, recv):
+        for (c, kt), t in zip(dst, recv):
             slab.plane_view(c, kt)[...] = t.numpy()
 
-    _run_slab(slab, rank, world, fields, p.Ni * p.Nj, k0, k1, steps, exchange)
+    _run_slab(slab, rank, world, fields, p.Ni * p.Nj, k0, k1, steps, exchange, fused)
     out.put((rank, [slab.owned(c).copy() for c in range(6)]))
     dist.barrier()
     dist.destroy_process_group()
 
 
-@pytest.mark.parametrize("world", [2, 3])
-def test_gloo_ranks_exchanging_halo_planes_equal_the_whole_grid(world):
+@pytest.mark.parametrize("world,fused", [(2, False), (3, False), (2, True), (3, True)])
+def test_gloo_ranks_exchanging_halo_planes_equal_the_whole_grid(world, fused):
     pytest.importorskip("torch")
     p = normalised_parameters(12, 10, 23)
     steps = 5
@@ -184,7 +215,7 @@ def test_gloo_ranks_exchanging_halo_planes_equal_the_whole_grid(world):
     ctx = mp.get_context("spawn")
     out = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, world, port, steps, out)) for r in range(world)]
+    procs = [ctx.Process(target=_rank, args=(r, world, port, steps, out, fused)) for r in range(world)]
     for pr in procs:
         pr.start()
     res = dict(out.get(timeout=180) for _ in procs)
