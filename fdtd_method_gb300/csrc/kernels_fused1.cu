@@ -615,16 +615,8 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
   const uint32_t phase0 = (ring / NS) & 1u;
   const bool tile_edge = x0 == 0 || x0 + nx == L.Ni || y0 == 0 || y0 + ny == L.Nj;
   const bool tma_out = (nx == 32);
-  // Ghost columns of the compensated form by bulk copy: the first tile
-  // column's boxes also go to the right margin (x = Ni..Ni+7 hi words,
-  // Ni..Ni+15 lo words: whole sectors; Ni a multiple of 8); the last one,
-  // when full, sends the last 8 hi words and 16 lo words of every staged row
-  // to x = -8..-1 and -16..-1 (one 32-byte sector each, what the boxes of the
-  // first tile column read left of the tile), the lanes of the halo-column
-  // warp issuing one row copy each.
   auto ghost_r = [&]() { return P::kLo && tma_out && x0 == 0 && L.Ni % 8 == 0; };
   auto ghost_l = [&]() { return P::kLo && tma_out && x0 + 32 == L.Ni; };
-  const bool margin_lanes = (w == RY + 1) && ghost_l();  // issue (and wait for) the left-margin row copies
   const bool edge_cell = interior && (yu == 0 || yu == L.Nj - 1);
 
   // Exchange offsets: where the thread publishes B', and (interior cells)
@@ -839,10 +831,9 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
     pby = nby;
     pbz = nbz;
     fence_async_smem();
-    if (leader || margin_lanes) bulk_wait_read_all();
+    if (leader) bulk_wait_read_all();
     if (__syncthreads_or(timed_out)) {
       if (leader) drain_tile<NS>(bar, ring, it, issued, wc);
-      if (margin_lanes) bulk_wait_all();
       return false;
     }
     if (w == RY && lane < ny && (x0 == 0 || x0 + nx == L.Ni)) {
@@ -867,35 +858,12 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
                             P::kLo ? eq[c * P::kBComp] : LoT(0));
       }
     }
-    if constexpr (P::kLo) {
-      if (margin_lanes) {
-        // rows x (hi, lo) x 3 components x (B' at t, E' at t+1)
-        const int n_ops = ny * 12;
-#pragma unroll 1
-        for (int q = lane; q < n_ops; q += 32) {
-          const int row = q % ny, c = (q / ny) % 3, part = (q / (3 * ny)) & 1, e = q / (6 * ny);
-          if (e ? !e_step : t < k0) continue;
-          const int plane = e ? t + 1 : t;
-          const int comp = e ? c : 3 + c;
-          if (part == 0) {
-            const unsigned char* src = (e ? eb + c * P::kBComp * P::HS : xb + P::kXHi + c * P::kXComp * P::HS) +
-                                       (row * 32 + 24) * P::HS;
-            bulk_store_1d(out.hi[comp] + L.at(-8, y0 + row, plane), src, 32);
-          } else {
-            const unsigned char* src =
-                (e ? eb + P::kBLo + c * P::kBComp * P::LS : xb + P::kXLo + c * P::kXComp * P::LS) + (row * 32 + 16) * P::LS;
-            bulk_store_1d(out.lo[comp] + L.at(-16, y0 + row, plane), src, 32);
-          }
-        }
-        bulk_commit();
-      }
-    }
     if (leader) {
-      // the tile's boxes at its own columns, then the right margin
+      // the tile's boxes at its own columns, then the margins it fills
 #pragma unroll 1
-      for (int g = 0; g < 2 && tma_out; ++g) {
-        if (g == 1 && !ghost_r()) continue;
-        const int xs = g == 0 ? x0 + kPadX : L.Ni + kPadX;
+      for (int g = 0; g < 3 && tma_out; ++g) {
+        if ((g == 1 && !ghost_r()) || (g == 2 && !ghost_l())) continue;
+        const int xs = g == 0 ? x0 + kPadX : g == 1 ? L.Ni + kPadX : 0;
         if (t >= k0)
           for (int c = 0; c < 3; ++c) {
             tma_store_3d(&maps.st.hi[3 + c], xb + P::kXHi + c * P::kXComp * P::HS, xs, y0, t);
@@ -917,7 +885,6 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
   }
   ring += (uint32_t)n_it;
   if (leader) bulk_wait_read_all();
-  if (margin_lanes) bulk_wait_all();
   return true;
 }
 

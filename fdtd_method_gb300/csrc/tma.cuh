@@ -104,14 +104,6 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
 
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 
-// One untiled bulk copy of `bytes` (a multiple of 16; both addresses 16-byte
-// aligned) from shared to global memory, in this thread's bulk group.
-__device__ __forceinline__ void bulk_store_1d(void* dst, const void* src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(reinterpret_cast<uint64_t>(dst)),
-               "r"(smem_addr(src)), "r"(bytes)
-               : "memory");
-}
-
 // Waits until every committed bulk store of this thread has read its shared
 // memory source (the buffer may then be rewritten).
 __device__ __forceinline__ void bulk_wait_read_all() {

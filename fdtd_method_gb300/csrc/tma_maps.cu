@@ -50,23 +50,22 @@ bool encode(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Bytes of the right margin a store map covers: the ghost column and the rest
-// of its 32-byte sector (so that a margin store writes whole sectors).
-constexpr int kRightMarginBytes = 32;
+// Columns of the right margin a store map covers: the ghost column and the
+// rest of the 16-byte unit that holds it for 2-byte words.
+constexpr int kRightMargin = 8;
 
 // One 3-D map over the grid rows of a padded array with their x margins
-// (ghost rows excluded): dims {kPadX + Ni + 32 / es, Nj, Nk} from padded
+// (ghost rows excluded): dims {kPadX + Ni + kRightMargin, Nj, Nk} from padded
 // column 0, box {32, tile_y, 1}.  x coordinate kPadX + x is cell x; a store
-// at kPadX + Ni fills the first 32 bytes of the right margin (8 FP32 or 16
-// 2-byte words; the copy engine clips the rest).  Rows outside the grid are
-// not written.
+// at 0 fills the left margin (cells -32 .. -1), one at kPadX + Ni the first
+// kRightMargin columns of the right margin (the copy engine clips the rest).
+// Rows outside the grid are not written.
 bool encode_store(CUtensorMap* m, CUtensorMapDataType dt, size_t es, void* base, const PLayout& L,
                   int tile_y) {
   EncodeTiled fn = encode_fn();
   if (!fn) return false;
   void* origin = static_cast<unsigned char*>(base) + L.at(-kPadX, 0, 0) * es;
-  const cuuint64_t dims[3] = {(cuuint64_t)(L.Ni + kPadX + kRightMarginBytes / (int)es), (cuuint64_t)L.Nj,
-                              (cuuint64_t)L.Nk};
+  const cuuint64_t dims[3] = {(cuuint64_t)(L.Ni + kPadX + kRightMargin), (cuuint64_t)L.Nj, (cuuint64_t)L.Nk};
   const cuuint64_t strides[2] = {(cuuint64_t)(L.pitch * es), (cuuint64_t)(L.pplane * es)};
   const cuuint32_t box[3] = {32, (cuuint32_t)tile_y, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
