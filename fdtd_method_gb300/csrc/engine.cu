@@ -262,9 +262,9 @@ cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps, int depth
     const FusedConfig& cf = h->fused_cfg;
     const WaitCtl wc = h->wait_ctl();
     switch (h->form) {
-      case Form::F32: return launch_fused1_f32(v.L, v.s32, w.s32, &sm, J, dj, h->cs, ss, step, apps, cf, true, wc, h->stream, kb, ke);
-      case Form::F32C: return launch_fused1_f32(v.L, v.s32c, w.s32c, &sm, J, dj, h->cs, ss, step, apps, cf, true, wc, h->stream, kb, ke);
-      case Form::F16: return launch_fused1_f32(v.L, v.s16, w.s16, &sm, J, dj, h->cs, ss, step, apps, cf, true, wc, h->stream, kb, ke);
+      case Form::F32: return launch_fused1_f32(v.L, v.s32, w.s32, &sm, J, dj, h->cs, ss, step, apps, cf, wc, h->stream, kb, ke);
+      case Form::F32C: return launch_fused1_f32(v.L, v.s32c, w.s32c, &sm, J, dj, h->cs, ss, step, apps, cf, wc, h->stream, kb, ke);
+      case Form::F16: return launch_fused1_f32(v.L, v.s16, w.s16, &sm, J, dj, h->cs, ss, step, apps, cf, wc, h->stream, kb, ke);
       default: return cudaErrorInvalidValue;
     }
   }
@@ -273,10 +273,9 @@ cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps, int depth
   const float* J[3] = {h->jf[0], h->jf[1], h->jf[2]};
   const bool dj = h->dense_j && h->jf[0];
   const FusedConfig& cf = h->fused_cfg;
-  const bool bf = b_first(h);
   const WaitCtl wc = h->wait_ctl();
   StepMaps sm;
-  sm.ld = bf ? h->bmaps_cur : h->maps_cur;
+  sm.ld = h->bmaps_cur;
   sm.st = h->smaps_alt;
   cudaError_t e = cudaSuccess;
   if (depth == 2) {
@@ -309,9 +308,9 @@ cudaError_t launch_fused_sweep(fdtd_handle* h, int64_t step, int apps, int depth
     return e;
   }
   switch (h->form) {
-    case Form::F32: e = launch_fused1_f32(h->L, v.s32, w.s32, &sm, J, dj, h->cs, ss, step, apps, cf, bf, wc, h->stream); break;
-    case Form::F32C: e = launch_fused1_f32(h->L, v.s32c, w.s32c, &sm, J, dj, h->cs, ss, step, apps, cf, bf, wc, h->stream); break;
-    case Form::F16: e = launch_fused1_f32(h->L, v.s16, w.s16, &sm, J, dj, h->cs, ss, step, apps, cf, bf, wc, h->stream); break;
+    case Form::F32: e = launch_fused1_f32(h->L, v.s32, w.s32, &sm, J, dj, h->cs, ss, step, apps, cf, wc, h->stream); break;
+    case Form::F32C: e = launch_fused1_f32(h->L, v.s32c, w.s32c, &sm, J, dj, h->cs, ss, step, apps, cf, wc, h->stream); break;
+    case Form::F16: e = launch_fused1_f32(h->L, v.s16, w.s16, &sm, J, dj, h->cs, ss, step, apps, cf, wc, h->stream); break;
     default: e = cudaErrorInvalidValue; break;
   }
   return e;
@@ -427,9 +426,9 @@ int ensure_alt(fdtd_handle* h) {
   if (h->maps_tile_y != key) {
     const HiType ht = h->form == Form::F16 ? HiType::F16 : HiType::F32;
     const bool two = h->fused_cfg.cells_per_thread == 2;
-    // box widths per component: the two-cell kernel's are uniform; the
-    // one-cell kernel's depend on the sweep order
-    int bw[6], lbw[6], bbw[6], blbw[6];
+    // box widths per component: the two-cell kernel's are uniform, the
+    // one-cell kernel's trimmed to what its stencil reads
+    int bw[6], lbw[6];
     if (two) {
       for (int c = 0; c < 6; ++c) {
         bw[c] = h->form == Form::F16 ? fused_box_width<StoreF16>() : fused_box_width<StoreF32>();
@@ -437,18 +436,9 @@ int ensure_alt(fdtd_handle* h) {
       }
     } else {
       switch (h->form) {
-        case Form::F16:
-          fused1_box_widths<StoreF16>(false, bw, lbw);
-          fused1_box_widths<StoreF16>(true, bbw, blbw);
-          break;
-        case Form::F32C:
-          fused1_box_widths<StoreF32C>(false, bw, lbw);
-          fused1_box_widths<StoreF32C>(true, bbw, blbw);
-          break;
-        default:
-          fused1_box_widths<StoreF32>(false, bw, lbw);
-          fused1_box_widths<StoreF32>(true, bbw, blbw);
-          break;
+        case Form::F16: fused1_box_widths<StoreF16>(bw, lbw); break;
+        case Form::F32C: fused1_box_widths<StoreF32C>(bw, lbw); break;
+        default: fused1_box_widths<StoreF32>(bw, lbw); break;
       }
     }
     // The maps cover the storage: on a z slab its halo planes as well (plane
@@ -467,12 +457,12 @@ int ensure_alt(fdtd_handle* h) {
     LoT* const* lo_cur = h->form == Form::F32C ? l_cur : nullptr;
     LoT* const* lo_alt = h->form == Form::F32C ? l_alt : nullptr;
     const int ty = h->fused_cfg.tile_y;
-    const BoxTrim trim = two ? BoxTrim::None : BoxTrim::EFirst;
-    if (build_tma_maps(&h->maps_cur, Lm, ht, f_cur, lo_cur, bw, lbw, ty, trim) != cudaSuccess ||
-        build_tma_maps(&h->maps_alt, Lm, ht, f_alt, lo_alt, bw, lbw, ty, trim) != cudaSuccess)
+    // the two-cell (E-first) kernel's load maps, or the one-cell kernel's
+    if (two && (build_tma_maps(&h->maps_cur, Lm, ht, f_cur, lo_cur, bw, lbw, ty, BoxTrim::None) != cudaSuccess ||
+                build_tma_maps(&h->maps_alt, Lm, ht, f_alt, lo_alt, bw, lbw, ty, BoxTrim::None) != cudaSuccess))
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
-    if (!two && (build_tma_maps(&h->bmaps_cur, Lm, ht, f_cur, lo_cur, bbw, blbw, ty, BoxTrim::BFirst) != cudaSuccess ||
-                 build_tma_maps(&h->bmaps_alt, Lm, ht, f_alt, lo_alt, bbw, blbw, ty, BoxTrim::BFirst) != cudaSuccess))
+    if (!two && (build_tma_maps(&h->bmaps_cur, Lm, ht, f_cur, lo_cur, bw, lbw, ty, BoxTrim::BFirst) != cudaSuccess ||
+                 build_tma_maps(&h->bmaps_alt, Lm, ht, f_alt, lo_alt, bw, lbw, ty, BoxTrim::BFirst) != cudaSuccess))
       return fail(FDTD_ERR_CUDA, "TMA tensor map encoding failed");
     if (!two && ty != 30) {
       int tw[6], tlw[6];

@@ -123,22 +123,21 @@ cudaError_t launch_fused_f32(const PLayout& L, const S& st, const S& out, const 
 template <class S>
 int fused_box_width();
 int fused_lo_box_width();
-// kernels_fused1.cu: the same sweep with one cell per thread (32-wide tiles);
-// `maps` is a StepMaps: load maps of `st`'s arrays (built with the trim of
-// the sweep order), store maps of `out`'s.  b_first: the B-first sweep (B
-// half steps, then E), otherwise the E-first one (E, then B half steps).
-// [kbeg, kend) are the planes it updates (kend < 0: Nk); a z slab's storage
-// sweeps [1, nk+1) and reads its halo planes 0 and nk+1 unwrapped (B-first).
+// kernels_fused1.cu: the B-first sweep (B half steps, then E) with one cell
+// per thread (32-wide tiles); `maps` is a StepMaps: load maps of `st`'s
+// arrays (BoxTrim::BFirst), store maps of `out`'s.  [kbeg, kend) are the
+// planes it updates (kend < 0: Nk); a z slab's storage sweeps [1, nk+1) and
+// reads its halo planes 0 and nk+1 unwrapped.
 template <class S>
 cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const void* maps,
                               const float* const J[3], bool dense_j, const CoefSet& cs,
                               const SourceSet& ss, int64_t step, int applications,
-                              const FusedConfig& cfg, bool b_first, const WaitCtl& wc, cudaStream_t stream,
+                              const FusedConfig& cfg, const WaitCtl& wc, cudaStream_t stream,
                               int kbeg = 0, int kend = -1);
 // Per-component box widths (hi and lo words) of the one-cell kernel's load
-// maps, for its E-first or B-first sweep.
+// maps.
 template <class S>
-void fused1_box_widths(bool b_first, int hi[6], int lo[6]);
+void fused1_box_widths(int hi[6], int lo[6]);
 
 // kernels_tblock.cu: the depth-2 sweep (two B-first steps per pass; the
 // first step applies `apps1` B half steps, the second two) of one cell per
@@ -195,11 +194,9 @@ enum class HiType { F32, F16 };
 cudaError_t build_tma_store_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6], LoT* const lo[6],
                                  int tile_y);
 // Box heights of the load maps: None (the two-cell kernel) gives every
-// component tile_y + 2 rows; the one-cell kernel's E-first sweep gives Bx and
-// Bz tile_y + 2 rows (the rows below and above the tile) and the others
-// tile_y + 1 (the row above); its B-first sweep gives Ex and Ez tile_y + 2
-// and the others tile_y + 1 (the row below).
-enum class BoxTrim { None, EFirst, BFirst };
+// component tile_y + 2 rows; BFirst (the one-cell and depth-2 sweeps) gives
+// Ex and Ez tile_y + 2 and the others tile_y + 1 (the row below).
+enum class BoxTrim { None, BFirst };
 cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const hi[6],
                            LoT* const lo[6], const int box_w[6], const int lo_box_w[6], int tile_y, BoxTrim trim);
 

@@ -118,15 +118,15 @@ struct fdtd_handle {
   FusedConfig fused_cfg;
   PLayout L{};  // padded layout of the FP32-arithmetic forms
   // TMA maps of the current and the second copy (rebuilt when the tile
-  // shape changes; swapped with the copies).
+  // shape changes; swapped with the copies): load maps of the two-cell
+  // kernel (uniform boxes; built only for it)...
   TmaMaps maps_cur;
   TmaMaps maps_alt;
-  // Store maps (grid cells only) of both copies, for the one-cell-per-thread
-  // fused kernel.
+  // ... store maps (grid cells and x margins) for the one-cell kernels ...
   TmaMaps smaps_cur;
   TmaMaps smaps_alt;
-  // Load maps of the B-first sweep (its boxes hold other halo rows) and of
-  // the depth-2 sweep (two rings of halo).
+  // ... and load maps of the one-cell B-first sweep (per-component halos)
+  // and of the depth-2 sweep (two rings of halo).
   TmaMaps bmaps_cur;
   TmaMaps bmaps_alt;
   TmaMaps tmaps_cur;

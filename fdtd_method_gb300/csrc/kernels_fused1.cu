@@ -1,30 +1,20 @@
-// Fused step kernels, one cell per thread: the default step of the
+// Fused step kernel, one cell per thread: the default step of the
 // FP32-arithmetic forms.  One sweep advances one update_fields step; the
 // arithmetic is that of the split sweeps (kernels_f32.cu, the reference's
 // functors kokkos_functors.h:64-90 E and :128-151 B), reproduced bit for bit.
-// A sweep comes in two orders:
-//
-//   E-first (fused1)    E step, then `apps` B half steps (the trailing half of
-//                       this step, and with apps = 2 the leading half of the
-//                       next), marching z upward.  A run of n steps is a
-//                       leading B half sweep and n of these.
-//   B-first (fused1b)   `apps` B half steps (the trailing half of the
-//                       previous step, which was left pending, and the leading
-//                       half of this one), then the E step, marching z
-//                       downward.  A run of n steps is n of these with the
-//                       last trailing half left pending; every reader of B
-//                       applies it (engine.cu), so n update_fields calls cost
-//                       n sweeps.
-//
-// Both orders add the same terms in the same order, so they agree bit for bit
-// with each other and with the split sweeps.
+// The sweep is B-first: `apps` B half steps (the trailing half of the
+// previous step, which was left pending, and the leading half of this one),
+// then the E step, marching z downward.  A run of n steps is n of these with
+// the last trailing half left pending; every reader of B applies it
+// (engine.cu), so n update_fields calls cost n sweeps.  It adds the same
+// terms in the same order as the split sweeps (and the two-cell E-first
+// kernel, kernels_fused.cu), so all agree bit for bit.
 //
 // A CTA owns a tile of 32 x RY cells at (x0, y0) (RY = 6, 14 or 30) and
 // marches the planes of its z chunk.  Warps 0..RY-1 are the tile rows; warps
-// RY and RY+1 compute the first half-sweep's field on the tile's halo row and
-// halo column (E-first: E' on the row above and the column right of the tile,
-// which the B update reads at j+1 and i+1; B-first: B' on the row below and
-// the column left of it, which the E update reads at j-1 and i-1).
+// RY and RY+1 compute B' on the tile's halo row and halo column (the row
+// below and the column left of the tile, which the E update reads at j-1 and
+// i-1).
 //
 // Data movement, per plane:
 //   in   one 3-D TMA box per stored array (hi words: columns x0-4 .. x0+35,
@@ -38,16 +28,11 @@
 //        margins as well, which fills the ghost columns with bulk copies
 //        where the alignment allows; the remaining ghost copies (ghost
 //        rows, corners, unaligned columns) are plain stores.
-// The first half-sweep's staging box doubles as the exchange plane from which
-// the next iteration reads that field at the tile's neighbouring cells; it
-// has two extra rows, holding the halo row's and the halo column's values.
+// The B' staging box doubles as the exchange plane from which the next
+// iteration reads B' at the tile's neighbouring cells; it has two extra
+// rows, holding the halo row's and the halo column's values.
 //
-// E-first, iteration t (planes k0 .. k1):
-//   1. E'(t) = E + c curl B of the thread's cell (B at i-1, j-1 from the box,
-//      B(t-1) carried in registers);
-//   2. on interior cells (t > k0), B'(t-1) = B(t-1) + apps (c/2) curl E'
-//      (E'(t-1) at i+1, j+1 from the exchange plane, E'(t) in registers).
-// B-first, iteration t (planes k1-1 down to k0-1):
+// Iteration t (planes k1-1 down to k0-1):
 //   1. B'(t) = B + apps (c/2) curl E of the thread's cell (E at i+1, j+1 from
 //      the box, E(t+1) carried in registers);
 //   2. on interior cells (t < k1-1), E'(t+1) = E(t+1) + c curl B' + J
@@ -113,33 +98,22 @@ struct BoxTable {
   int stage;           // stage size, 128-byte multiple
 };
 
-constexpr BoxTable box_table(int RY, int W, int Ws, int LW, int LWs, int HS, int LS, bool lo, int off, int lo_off,
-                             bool bfirst) {
+constexpr BoxTable box_table(int RY, int W, int Ws, int LW, int LWs, int HS, int LS, bool lo, int off, int lo_off) {
   BoxTable b{};
   int at = 0;
   unsigned tx = 0;
   for (int c = 0; c < 6; ++c) {
-    if (bfirst) {
-      // every box starts at the row below and the column left of the tile
-      // (the halo warps' cells); Ex and Ez also hold the row above (B'z and
-      // B'x read them at j+1), Ey and Ez the column right of it (B'z and B'y
-      // read them at i+1).  Box row 0 is y0-1.
-      b.rows[c] = (c == 0 || c == 2) ? RY + 2 : RY + 1;
-      b.row0[c] = 0;
-      b.xoff[c] = off;
-      b.lxoff[c] = lo_off;
-      const bool right = (c == 1 || c == 2);
-      b.w[c] = right ? W : Ws;
-      b.lw[c] = right ? LW : LWs;
-    } else {
-      const bool below = (c == 3 || c == 5), left = (c == 4 || c == 5);
-      b.rows[c] = below ? RY + 2 : RY + 1;
-      b.row0[c] = below ? 0 : 1;
-      b.xoff[c] = left ? off : 0;
-      b.lxoff[c] = left ? lo_off : 0;
-      b.w[c] = W;
-      b.lw[c] = LW;
-    }
+    // every box starts at the row below and the column left of the tile
+    // (the halo warps' cells); Ex and Ez also hold the row above (B'z and
+    // B'x read them at j+1), Ey and Ez the column right of it (B'z and B'y
+    // read them at i+1).  Box row 0 is y0-1.
+    b.rows[c] = (c == 0 || c == 2) ? RY + 2 : RY + 1;
+    b.row0[c] = 0;
+    b.xoff[c] = off;
+    b.lxoff[c] = lo_off;
+    const bool right = (c == 1 || c == 2);
+    b.w[c] = right ? W : Ws;
+    b.lw[c] = right ? LW : LWs;
   }
   for (int c = 0; c < 6; ++c) {
     b.hi[c] = at;
@@ -160,9 +134,8 @@ constexpr BoxTable box_table(int RY, int W, int Ws, int LW, int LWs, int HS, int
   return b;
 }
 
-// Shared-memory plan (byte offsets) of the E-first (BF false) or B-first
-// (BF true) sweep.
-template <class S, int RY, bool BF = false>
+// Shared-memory plan (byte offsets) of the sweep.
+template <class S, int RY>
 struct Plan1 {
   using HiT = typename S::HiT;
   static constexpr bool kLo = S::kComp;
@@ -171,15 +144,11 @@ struct Plan1 {
   static constexpr int Ws = Box1<S>::kWs, LWs = Box1<S>::kLoWs;
   static constexpr int HS = (int)sizeof(HiT), LS = (int)sizeof(LoT);
   // Ring stage: 6 hi boxes, then 6 lo boxes.  Each component's box holds
-  // only the halos its stencil reads.  E-first: the column left of the tile
-  // for By and Bz (E update, i-1), the row below for Bx and Bz (E update,
-  // j-1); every box holds the column right of the tile and the row above,
-  // where the halo warps compute E'.  Box row 0 is y0-1 for Bx, Bz and y0
-  // otherwise (box row of thread row r: r - row0).  B-first: see box_table.
-  // Every box starts on a 128-byte boundary, as tensor copies require.
+  // only the halos its stencil reads (box_table).  Every box starts on a
+  // 128-byte boundary, as tensor copies require.
   // Per-component scalars of the table (device code may use scalar
   // constants, not the table object).
-  static constexpr BoxTable box() { return box_table(RY, W, Ws, LW, LWs, HS, LS, kLo, OFF, kLoOff1, BF); }
+  static constexpr BoxTable box() { return box_table(RY, W, Ws, LW, LWs, HS, LS, kLo, OFF, kLoOff1); }
   template <int c> static constexpr int kHiAt = box().hi[c];
   template <int c> static constexpr int kLoAt = box().lo[c];
   template <int c> static constexpr int kRow0 = box().row0[c];
@@ -189,16 +158,15 @@ struct Plan1 {
   template <int c> static constexpr int kLW = box().lw[c];
   static constexpr uint32_t kTx = box().tx;
   static constexpr int kStage = box().stage;
-  // Exchange / staging buffer of the first half-sweep's field (E' in the
-  // E-first sweep, B' in the B-first one): per component RY+2 rows of 32
-  // (rows 0..RY-1 the tile, row RY the halo row, row RY+1 the halo column by
-  // row), hi words then lo words.
+  // Exchange / staging buffer of B': per component RY+2 rows of 32 (rows
+  // 0..RY-1 the tile, row RY the halo row, row RY+1 the halo column by row),
+  // hi words then lo words.
   static constexpr int kXComp = (RY + 2) * 32;  // elements per component
   static constexpr int kXHi = 0;
   static constexpr int kXLo = round128(3 * kXComp * HS);
   static constexpr int kXBytes = kXLo + (kLo ? round128(3 * kXComp * LS) : 0);
-  // Staging buffer of the second field (B' in the E-first sweep, E' in the
-  // B-first one): per component RY rows of 32, hi words then lo words.
+  // Staging buffer of E': per component RY rows of 32, hi words then lo
+  // words.
   static constexpr int kBComp = RY * 32;
   static constexpr int kBLo = round128(3 * kBComp * HS);
   static constexpr int kBBytes = kBLo + (kLo ? round128(3 * kBComp * LS) : 0);
@@ -210,7 +178,7 @@ struct Plan1 {
   static constexpr int kTotal = kList + 4 * (kMaxSources + 1);
   // The box the B-first sweep's halo column reads starts one column left of
   // the tile, inside every box's left offset.
-  static_assert(!BF || (OFF >= 1 && (!kLo || kLoOff1 >= 1)), "B-first boxes need the left halo column");
+  static_assert(OFF >= 1 && (!kLo || kLoOff1 >= 1), "the boxes need the left halo column");
   static_assert(Ws - OFF >= 32 && (!kLo || LWs - kLoOff1 >= 32) && W - OFF >= 33 && (!kLo || LW - kLoOff1 >= 33),
                 "boxes must reach the tile's last column (and the one right of it)");
   static_assert((Ws * HS) % 16 == 0 && (W * HS) % 16 == 0 && (LWs * LS) % 16 == 0 && (LW * LS) % 16 == 0,
@@ -239,7 +207,7 @@ __device__ __forceinline__ bool window_meets(int o, int n, int N, int a, int m) 
 // tile writes staging again.
 //
 // fused1_tile lists the sources that can reach the tile, then runs the plane
-// loop, fused1_planes, compiled with (kSrc) or without source evaluation.
+// loop, fused1b_planes, compiled with (kSrc) or without source evaluation.
 // On a wait that gives up (any thread), every thread leaves the plane loop
 // after the iteration's barrier; the copy-engine leader then waits for the
 // tile's loads still in flight and its committed stores (drain_tile), and the
@@ -253,340 +221,14 @@ __device__ __forceinline__ void drain_tile(uint64_t* bar, uint32_t ring, int fir
   bulk_wait_all();
 }
 
-template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSrc>
-__device__ __forceinline__ bool fused1_planes(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
-                                              const CoefSet& cs, int bx, int by, int bz, int kchunk, int2 zr,
-                                              const float* __restrict__ Jx, const float* __restrict__ Jy,
-                                              const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
-                                              const WaitCtl& wc, unsigned char* smem, uint32_t& ring, int nsrc) {
-  using P = Plan1<S, RY>;
-  using HiT = typename S::HiT;
-  using T = typename A::Cur;
-  constexpr int NS = kStages1;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + P::kBar);
-  int* list = reinterpret_cast<int*>(smem + P::kList);
-
-  const int lane = threadIdx.x, w = threadIdx.y;
-  const int x0 = bx * 32, y0 = by * RY;
-  const int nx = min(32, L.Ni - x0), ny = min(RY, L.Nj - y0);
-  const bool hcol = (w == RY + 1);
-  // box row (lanes of the halo-column warp past the tile's rows are clamped
-  // onto its last row: they compute but never publish)
-  const int r = hcol ? min(lane, RY - 1) + 1 : w + 1;
-  const int cx = hcol ? nx : lane;        // column within the tile (0..32)
-  const bool active = hcol ? (lane < ny) : (r <= ny + 1 && lane < nx);
-  const bool interior = !hcol && r <= ny && lane < nx;
-  // logical coordinates (x = Ni and y = Nj are the ghost copies of 0)
-  const int xu = x0 + cx, yu = y0 + r - 1;
-  const int xl = xu >= L.Ni ? xu - L.Ni : xu, yl = yu >= L.Nj ? yu - L.Nj : yu;
-  const int k0 = zr.x + bz * kchunk;
-  const int k1 = min(k0 + kchunk, zr.y);
-  // The copy-engine leader (ring refills, bulk stores and their waits) is
-  // lane 0 of the halo-column warp, which has the least arithmetic per plane.
-  const bool leader = (w == RY + 1 && lane == 0);
-  const int slot0 = (int)(ring % NS);
-  const uint32_t phase0 = (ring / NS) & 1u;
-  const bool tile_edge = x0 == 0 || x0 + nx == L.Ni || y0 == 0 || y0 + ny == L.Nj;
-  // The copy engine clips a store along x in 16-byte units, not elements: a
-  // tile narrower than 32 columns would overwrite the ghost column past the
-  // grid's last cell.  Such tiles (the last tile column when Ni is not a
-  // multiple of 32) store with plain per-thread stores instead.
-  const bool tma_out = (nx == 32);
-  // Ghost columns.  By bulk copy (compensated form): the first tile column
-  // also stores its boxes into the right margin (cells 0..7 at x = Ni..Ni+7:
-  // the store map ends there) when that start is on a 16-byte boundary for
-  // every element size (Ni a multiple of 8); the last one, when full, into
-  // the left margin (cells Ni-32..Ni-1 at x = -32..-1).  Every value there is
-  // a periodic copy.  Otherwise the
-  // halo-row warp copies the edge column's stored words from staging to the
-  // ghost column, one lane per row.  Threads write only the ghost rows and
-  // their corners.  (The flags are recomputed where used: cheaper than
-  // keeping them live across the loop.)
-  // The bulk copies pay for their extra margin bytes in the compensated form
-  // (whose scalar ghost stores are twice as many: hi and lo words); the plain
-  // forms run faster with the halo-row warp's copies alone.
-  auto ghost_r = [&]() { return P::kLo && tma_out && x0 == 0 && L.Ni % 8 == 0; };
-  auto ghost_l = [&]() { return P::kLo && tma_out && x0 + 32 == L.Ni; };
-  const bool edge_cell = interior && (yl == 0 || yl == L.Nj - 1);
-
-  // Element offsets of this thread in the exchange rows: where it publishes
-  // E', and where it finds E' at (r+1, cx) and (r, cx+1).
-  const int xo_own = hcol ? (RY + 1) * 32 + (r - 1) : (r == ny + 1 ? RY * 32 + cx : (r - 1) * 32 + cx);
-  const int xo_up = (r == ny) ? RY * 32 + cx : r * 32 + cx;
-  const int xo_right = (cx + 1 == nx) ? (RY + 1) * 32 + (r - 1) : (r - 1) * 32 + cx + 1;
-  const int bo_own = (r - 1) * 32 + cx;
-  const int hi_own = r * P::W + cx;  // ring box element offsets, before each component's shifts
-  const int lo_own = r * P::LW + cx;
-
-  int issued = 0;  // ring fills of this tile issued so far (the leader's count)
-  auto issue = [&](int t) {
-    if (wc.withhold) return;
-    ++issued;
-    const int slot = (slot0 + t - k0) % NS;
-    const int kk = (t == L.Nk) ? 0 : t;
-    unsigned char* base = smem + P::kRing + slot * P::kStage;
-    mbar_arrive_expect_tx(&bar[slot], P::kTx);
-    // (y coordinates are padded rows: logical row y is padded row y + kPadY)
-    for_each_comp([&](auto cc) {
-      constexpr int c = decltype(cc)::value;
-      tma_load_3d(base + P::template kHiAt<c>, &maps.ld.hi[c], x0 + kPadX - P::template kXOff<c>,
-                  y0 - 1 + kPadY + P::template kRow0<c>, kk, &bar[slot]);
-      if (P::kLo)
-        tma_load_3d(base + P::template kLoAt<c>, &maps.ld.lo[c], x0 + kPadX - P::template kLXOff<c>,
-                    y0 - 1 + kPadY + P::template kRow0<c>, kk, &bar[slot]);
-    });
-  };
-
-  if (leader)
-    for (int t = k0; t <= k1 && t < k0 + NS; ++t) issue(t);
-
-  // Per-column factor (amp gx) gy of the first kFastSources listed sources
-  // (only the z factor changes from plane to plane).
-  T sxy[kFastSources];
-  unsigned smask = 0;
-#pragma unroll
-  for (int q = 0; q < kFastSources; ++q) {
-    sxy[q] = A::cur_zero();
-    if (kSrc && q < nsrc) {
-      const DevSource& d = ss.src[list[q]];
-      const int di = box_offset(xl, d.i0, d.ni, L.Ni);
-      const int dj = box_offset(yl, d.j0, d.nj, L.Nj);
-      if (active && di >= 0 && dj >= 0) {
-        sxy[q] = A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + step), A::cur_table(ss, d.gx_off + di)),
-                            A::cur_table(ss, d.gy_off + dj));
-        smask |= 1u << q;
-      }
-    }
-  }
-
-  Pair pbx{0.f, 0.f}, pby{0.f, 0.f}, pbz{0.f, 0.f};
-  Pair pex{0.f, 0.f}, pey{0.f, 0.f}, pez{0.f, 0.f};
-  if (active) {
-    const int64_t b0 = L.at(xu, yu, wrap_prev(k0, L.Nk));
-    pbx = st.load(3, b0);
-    pby = st.load(4, b0);
-  }
-
-  int slot = slot0;
-  uint32_t phase = phase0;
-  for (int t = k0; t <= k1; ++t) {
-    const int cur = t & 1;
-    const int kk = (t == L.Nk) ? 0 : t;
-    const bool timed_out = !mbar_wait_bounded(&bar[slot], phase, wc);
-    const unsigned char* stage = smem + P::kRing + slot * P::kStage;
-    const HiT* H = reinterpret_cast<const HiT*>(stage) + hi_own;
-    const LoT* Q = reinterpret_cast<const LoT*>(stage) + lo_own;
-    // component c at box offset (dr rows, dc columns) from this thread's cell
-    auto V = [&](auto cc, int dr, int dc) -> Pair {
-      constexpr int c = decltype(cc)::value;
-      const HiT h = H[P::template kHiAt<c> / P::HS + (dr - P::template kRow0<c>) * P::W + P::template kXOff<c> + dc];
-      const LoT q = P::kLo ? Q[P::template kLoAt<c> / P::LS + (dr - P::template kRow0<c>) * P::LW +
-                               P::template kLXOff<c> + dc]
-                           : LoT(0);
-      return st.decode(c, h, q);
-    };
-
-    // 1. E'(t)
-    const Pair bx = V(Comp<3>{}, 0, 0), by = V(Comp<4>{}, 0, 0), bz = V(Comp<5>{}, 0, 0);
-    Pair qx = A::curl(ecoef<S>(cs, st, 0, 0), bz, V(Comp<5>{}, -1, 0), ecoef<S>(cs, st, 0, 1), by, pby);
-    Pair qy = A::curl(ecoef<S>(cs, st, 1, 0), bx, pbx, ecoef<S>(cs, st, 1, 1), bz, V(Comp<5>{}, 0, -1));
-    Pair qz = A::curl(ecoef<S>(cs, st, 2, 0), by, V(Comp<4>{}, 0, -1), ecoef<S>(cs, st, 2, 1), bx, V(Comp<3>{}, -1, 0));
-    if (kDenseJ || kSrc) {
-      // Current, accumulated per J component in registration order; only the
-      // components that received current get the current term.
-      T jv[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
-      unsigned has = 0;
-      if (kDenseJ && active) {
-        const int64_t d = xl + (int64_t)yl * L.Ni + (int64_t)kk * L.Ni * L.Nj;
-        jv[0] = A::cur_dense(Jx[d]);
-        jv[1] = A::cur_dense(Jy[d]);
-        jv[2] = A::cur_dense(Jz[d]);
-        has = 7u;
-      }
-#pragma unroll
-      for (int q = 0; q < kFastSources; ++q) {
-        if (kSrc && q < nsrc) {
-          const DevSource& d = ss.src[list[q]];
-          const int dk = box_offset(kk, d.k0, d.nk, L.Nk);  // the same for the whole tile
-          if (dk >= 0 && (smask >> q & 1u)) {
-            add_current<A>(jv, d.comp_mask, A::cur_mul(sxy[q], A::cur_table(ss, d.gz_off + dk)));
-            has |= (unsigned)d.comp_mask;
-          }
-        }
-      }
-      for (int i = kFastSources; kSrc && i < nsrc; ++i) {
-        const DevSource& d = ss.src[list[i]];
-        const int dk = box_offset(kk, d.k0, d.nk, L.Nk);
-        if (dk < 0) continue;
-        const int di = box_offset(xl, d.i0, d.ni, L.Ni);
-        const int dj = box_offset(yl, d.j0, d.nj, L.Nj);
-        if (active && di >= 0 && dj >= 0) {
-          add_current<A>(jv, d.comp_mask,
-                         A::cur_mul(A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + step),
-                                                          A::cur_table(ss, d.gx_off + di)),
-                                               A::cur_table(ss, d.gy_off + dj)),
-                                    A::cur_table(ss, d.gz_off + dk)));
-          has |= (unsigned)d.comp_mask;
-        }
-      }
-      if (has & 1u) qx = A::add(qx, A::cur_term(jcoef<S>(cs, st, 0), jv[0]));
-      if (has & 2u) qy = A::add(qy, A::cur_term(jcoef<S>(cs, st, 1), jv[1]));
-      if (has & 4u) qz = A::add(qz, A::cur_term(jcoef<S>(cs, st, 2), jv[2]));
-    }
-    const Pair ax = A::acc(V(Comp<0>{}, 0, 0), qx), ay = A::acc(V(Comp<1>{}, 0, 0), qy), az = A::acc(V(Comp<2>{}, 0, 0), qz);
-    // E' in its stored words; the B update uses the value they hold.
-    const HiT ehx = st.enc_hi(0, ax), ehy = st.enc_hi(1, ay), ehz = st.enc_hi(2, az);
-    const LoT elx = st.enc_lo(ax), ely = st.enc_lo(ay), elz = st.enc_lo(az);
-    const Pair nex = st.decode(0, ehx, elx), ney = st.decode(1, ehy, ely), nez = st.decode(2, ehz, elz);
-
-    unsigned char* xb = smem + P::kExch + cur * P::kXBytes;
-    if (active) {
-      HiT* xh = reinterpret_cast<HiT*>(xb + P::kXHi) + xo_own;
-      xh[0] = ehx;
-      xh[P::kXComp] = ehy;
-      xh[2 * P::kXComp] = ehz;
-      if (P::kLo) {
-        LoT* xq = reinterpret_cast<LoT*>(xb + P::kXLo) + xo_own;
-        xq[0] = elx;
-        xq[P::kXComp] = ely;
-        xq[2 * P::kXComp] = elz;
-      }
-    }
-
-    // 2. B'(t-1)
-    Pair nbx{0.f, 0.f}, nby{0.f, 0.f}, nbz{0.f, 0.f};
-    unsigned char* bb = smem + P::kBst + cur * P::kBBytes;
-    if (t > k0 && interior) {
-      const unsigned char* pb = smem + P::kExch + (cur ^ 1) * P::kXBytes;
-      const HiT* ph = reinterpret_cast<const HiT*>(pb + P::kXHi);
-      const LoT* pq = reinterpret_cast<const LoT*>(pb + P::kXLo);
-      auto E = [&](int c, int off) -> Pair {
-        return st.decode(c, ph[c * P::kXComp + off], P::kLo ? pq[c * P::kXComp + off] : LoT(0));
-      };
-      Pair ux = A::curl(bcoef<S>(cs, st, 0, 0), ney, pey, bcoef<S>(cs, st, 0, 1), E(2, xo_up), pez);
-      Pair uy = A::curl(bcoef<S>(cs, st, 1, 0), E(2, xo_right), pez, bcoef<S>(cs, st, 1, 1), nex, pex);
-      Pair uz = A::curl(bcoef<S>(cs, st, 2, 0), E(0, xo_up), pex, bcoef<S>(cs, st, 2, 1), E(1, xo_right), pey);
-      if (kApps == 2) {
-        ux = A::twice(ux);
-        uy = A::twice(uy);
-        uz = A::twice(uz);
-      }
-      nbx = A::acc(pbx, ux);
-      nby = A::acc(pby, uy);
-      nbz = A::acc(pbz, uz);
-      HiT* bh = reinterpret_cast<HiT*>(bb) + bo_own;
-      bh[0] = st.enc_hi(3, nbx);
-      bh[P::kBComp] = st.enc_hi(4, nby);
-      bh[2 * P::kBComp] = st.enc_hi(5, nbz);
-      if (P::kLo) {
-        LoT* bq = reinterpret_cast<LoT*>(bb + P::kBLo) + bo_own;
-        bq[0] = st.enc_lo(nbx);
-        bq[P::kBComp] = st.enc_lo(nby);
-        bq[2 * P::kBComp] = st.enc_lo(nbz);
-      }
-    }
-    if (!tma_out && interior) {
-      const int64_t o = L.at(xl, yl, 0);
-      if (t < k1) {
-        out.store(0, o + (int64_t)t * L.pplane, nex);
-        out.store(1, o + (int64_t)t * L.pplane, ney);
-        out.store(2, o + (int64_t)t * L.pplane, nez);
-      }
-      if (t > k0) {
-        out.store(3, o + (int64_t)(t - 1) * L.pplane, nbx);
-        out.store(4, o + (int64_t)(t - 1) * L.pplane, nby);
-        out.store(5, o + (int64_t)(t - 1) * L.pplane, nbz);
-      }
-    }
-    // Ghost copies of edge cells (their tiles only).
-    if (tile_edge && edge_cell) {
-      if (t < k1) {
-        store_ghost_rows(out, L, true, true, 0, xl, yl, t, nex);
-        store_ghost_rows(out, L, true, true, 1, xl, yl, t, ney);
-        store_ghost_rows(out, L, true, true, 2, xl, yl, t, nez);
-      }
-      if (t > k0) {
-        store_ghost_rows(out, L, true, true, 3, xl, yl, t - 1, nbx);
-        store_ghost_rows(out, L, true, true, 4, xl, yl, t - 1, nby);
-        store_ghost_rows(out, L, true, true, 5, xl, yl, t - 1, nbz);
-      }
-    }
-
-    pbx = bx;
-    pby = by;
-    pbz = bz;
-    pex = nex;
-    pey = ney;
-    pez = nez;
-    fence_async_smem();
-    // The previous iteration's stores must have read their staging (written
-    // again next iteration) before anyone passes this barrier.
-    if (leader) bulk_wait_read_all();
-    if (__syncthreads_or(timed_out)) {
-      if (leader) drain_tile<NS>(bar, ring, t - k0, issued, wc);
-      return false;
-    }
-    if (w == RY && lane < ny && (x0 == 0 || x0 + nx == L.Ni)) {
-      // ghost columns the bulk copies do not write: x = Ni from column 0,
-      // x = -1 from column nx-1, row y0+lane, copied as stored words
-#pragma unroll 1
-      for (int side = 0; side < 2; ++side) {
-        const bool on = side == 0 ? (x0 == 0 && !ghost_r()) : (x0 + nx == L.Ni && !ghost_l());
-        if (!on) continue;
-        const int col = side == 0 ? 0 : nx - 1;
-        const int64_t g = L.at(side == 0 ? L.Ni : -1, y0 + lane, 0);
-        const HiT* eh = reinterpret_cast<const HiT*>(xb + P::kXHi) + lane * 32 + col;
-        const LoT* eq = reinterpret_cast<const LoT*>(xb + P::kXLo) + lane * 32 + col;
-        const HiT* bh = reinterpret_cast<const HiT*>(bb) + lane * 32 + col;
-        const LoT* bq = reinterpret_cast<const LoT*>(bb + P::kBLo) + lane * 32 + col;
-        if (t < k1)
-          for (int c = 0; c < 3; ++c)
-            out.store_words(c, g + (int64_t)t * L.pplane, eh[c * P::kXComp], P::kLo ? eq[c * P::kXComp] : LoT(0));
-        if (t > k0)
-          for (int c = 0; c < 3; ++c)
-            out.store_words(3 + c, g + (int64_t)(t - 1) * L.pplane, bh[c * P::kBComp],
-                            P::kLo ? bq[c * P::kBComp] : LoT(0));
-      }
-    }
-    if (leader) {
-      // the tile's boxes at its own columns, then the margins it fills
-#pragma unroll 1
-      for (int g = 0; g < 3 && tma_out; ++g) {
-        if ((g == 1 && !ghost_r()) || (g == 2 && !ghost_l())) continue;
-        const int xs = g == 0 ? x0 + kPadX : g == 1 ? L.Ni + kPadX : 0;
-        if (t < k1)
-          for (int c = 0; c < 3; ++c) {
-            tma_store_3d(&maps.st.hi[c], xb + P::kXHi + c * P::kXComp * P::HS, xs, y0, t);
-            if (P::kLo) tma_store_3d(&maps.st.lo[c], xb + P::kXLo + c * P::kXComp * P::LS, xs, y0, t);
-          }
-        if (t > k0)
-          for (int c = 0; c < 3; ++c) {
-            tma_store_3d(&maps.st.hi[3 + c], bb + c * P::kBComp * P::HS, xs, y0, t - 1);
-            if (P::kLo) tma_store_3d(&maps.st.lo[3 + c], bb + P::kBLo + c * P::kBComp * P::LS, xs, y0, t - 1);
-          }
-      }
-      bulk_commit();
-      if (t + NS <= k1) issue(t + NS);
-    }
-    if (++slot == NS) {
-      slot = 0;
-      phase ^= 1u;
-    }
-  }
-  ring += (uint32_t)(k1 - k0 + 1);
-  if (leader) bulk_wait_read_all();
-  return true;
-}
-
-// The B-first sweep of one tile (see the file comment): planes k1-1 down to
-// k0-1.  Same contract as fused1_planes.
+// The sweep of one tile (see the file comment): planes k1-1 down to k0-1.
 template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSrc>
 __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                                                const CoefSet& cs, int bx, int by, int bz, int kchunk, int2 zr,
                                                const float* __restrict__ Jx, const float* __restrict__ Jy,
                                                const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
                                                const WaitCtl& wc, unsigned char* smem, uint32_t& ring, int nsrc) {
-  using P = Plan1<S, RY, true>;
+  using P = Plan1<S, RY>;
   using HiT = typename S::HiT;
   using T = typename A::Cur;
   constexpr int NS = kStages1;
@@ -892,16 +534,15 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
 // kSplit: compile the plane loop twice and run the source-free copy on tiles
 // that no source reaches (fewer live registers there).  The batched kernel
 // takes either: where its tiles alternate between the two cases, two hot
-// copies of the loop ran slower than one (its autotuner picks).  kBF selects
-// the B-first sweep.  Returns false when a bounded wait gave up (uniform over
-// the CTA).
-template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSplit, bool kBF>
+// copies of the loop ran slower than one (its autotuner picks).  Returns false
+// when a bounded wait gave up (uniform over the CTA).
+template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSplit>
 __device__ __forceinline__ bool fused1_tile(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                                             const CoefSet& cs, int bx, int by, int bz, int kchunk, int2 zr,
                                             const float* __restrict__ Jx, const float* __restrict__ Jy,
                                             const float* __restrict__ Jz, const SourceSet& ss, int64_t step,
                                             const WaitCtl& wc, unsigned char* smem, uint32_t& ring) {
-  using P = Plan1<S, RY, kBF>;
+  using P = Plan1<S, RY>;
   int* list = reinterpret_cast<int*>(smem + P::kList);
   // Sources that can touch this tile's cells (with one cell of halo on each
   // side), in registration order; the exact per-cell test comes in the plane loop.
@@ -926,11 +567,9 @@ __device__ __forceinline__ bool fused1_tile(const PLayout& L, const S& st, const
   }
   __syncthreads();
   const int nsrc = list[kMaxSources];
-#define FDTD_PLANES(SRC, NSRC)                                                                                   \
-  return kBF ? fused1b_planes<S, A, RY, kApps, kDenseJ, SRC>(L, st, out, maps, cs, bx, by, bz, kchunk, zr, Jx, Jy, Jz, \
-                                                            ss, step, wc, smem, ring, NSRC)                      \
-             : fused1_planes<S, A, RY, kApps, kDenseJ, SRC>(L, st, out, maps, cs, bx, by, bz, kchunk, zr, Jx, Jy, Jz, \
-                                                           ss, step, wc, smem, ring, NSRC)
+#define FDTD_PLANES(SRC, NSRC)                                                                                     \
+  return fused1b_planes<S, A, RY, kApps, kDenseJ, SRC>(L, st, out, maps, cs, bx, by, bz, kchunk, zr, Jx, Jy, Jz, ss, \
+                                                      step, wc, smem, ring, NSRC)
   if (!kSplit || nsrc > 0) FDTD_PLANES(true, nsrc);
   FDTD_PLANES(false, 0);
 #undef FDTD_PLANES
@@ -945,15 +584,15 @@ __device__ __forceinline__ void init_ring(uint64_t* bar) {
   __syncthreads();
 }
 
-template <class S, class A, int RY, int kApps, bool kDenseJ, bool kBF>
+template <class S, class A, int RY, int kApps, bool kDenseJ>
 __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
     fused1(PLayout L, S st, S out, const __grid_constant__ StepMaps maps, CoefSet cs, int kchunk, int2 zr,
            const float* __restrict__ Jx, const float* __restrict__ Jy, const float* __restrict__ Jz,
            SourceSet ss, int64_t step, WaitCtl wc) {
   extern __shared__ __align__(128) unsigned char smem[];
-  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY, kBF>::kBar));
+  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
   uint32_t ring = 0;
-  fused1_tile<S, A, RY, kApps, kDenseJ, true, kBF>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z, kchunk, zr,
+  fused1_tile<S, A, RY, kApps, kDenseJ, true>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z, kchunk, zr,
                                                    Jx, Jy, Jz, ss, step, wc, smem, ring);
   if (threadIdx.x == 0 && threadIdx.y == RY + 1) bulk_wait_all();  // the copy-engine leader's stores
 }
@@ -971,7 +610,7 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ BatchDomain<S> dom;
   __shared__ int4 tile;
-  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY, true>::kBar));
+  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
   const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const int64_t step = *step_base + step_off;
@@ -994,10 +633,10 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
       const StepMaps& m = maps[2 * w.x + parity];
       const int q = threadIdx.x;
       const CUtensorMap* tm = q < 6 ? &m.ld.hi[q] : q < 12 ? &m.ld.lo[q - 6] : q < 18 ? &m.st.hi[q - 12] : &m.st.lo[q - 18];
-      if (Plan1<S, RY, true>::kLo || (q < 6 || (q >= 12 && q < 18))) prefetch_tensormap(tm);
+      if (Plan1<S, RY>::kLo || (q < 6 || (q >= 12 && q < 18))) prefetch_tensormap(tm);
     }
     __syncthreads();
-    const bool ok = fused1_tile<S, A, RY, kApps, false, kSplit, true>(
+    const bool ok = fused1_tile<S, A, RY, kApps, false, kSplit>(
         dom.L, dom.s[parity], dom.s[parity ^ 1], maps[2 * w.x + parity], dom.cs, w.y, w.z, w.w, kchunk,
         make_int2(0, dom.L.Nk), nullptr,
         nullptr, nullptr, dom.ss, step, wc, smem, ring);
@@ -1016,20 +655,20 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
 
 // ---------------------------------------------------------------------------
 
-template <class S, int RY, int APPS, bool DJ, bool BF>
+template <class S, int RY, int APPS, bool DJ>
 static cudaError_t launch1_one(dim3 grid, const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                                const CoefSet& cs, int kchunk, int2 zr, const float* const J[3], const SourceSet& ss,
                                int64_t step, const WaitCtl& wc, cudaStream_t stream) {
   using A = typename ArithOf1<S>::type;
-  auto kern = fused1<S, A, RY, APPS, DJ, BF>;
-  const int bytes = Plan1<S, RY, BF>::kTotal;
+  auto kern = fused1<S, A, RY, APPS, DJ>;
+  const int bytes = Plan1<S, RY>::kTotal;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
   kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(L, st, out, maps, cs, kchunk, zr, J[0], J[1], J[2], ss, step, wc);
   return cudaGetLastError();
 }
 
-template <class S, int RY, bool BF>
+template <class S, int RY>
 static cudaError_t launch1_ry(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                               const float* const J[3], bool dense_j, const CoefSet& cs, const SourceSet& ss,
                               int64_t step, int applications, int kchunk, int2 zr, const WaitCtl& wc,
@@ -1038,7 +677,7 @@ static cudaError_t launch1_ry(const PLayout& L, const S& st, const S& out, const
   if (zr.x < 0 || zr.y > L.Nk || zr.y <= zr.x) return cudaErrorInvalidValue;
   dim3 grid((L.Ni + 31) / 32, (L.Nj + RY - 1) / RY, (zr.y - zr.x + kchunk - 1) / kchunk);
 #define FDTD_F(APPS, DJ) \
-  return launch1_one<S, RY, APPS, DJ, BF>(grid, L, st, out, maps, cs, kchunk, zr, J, ss, step, wc, stream)
+  return launch1_one<S, RY, APPS, DJ>(grid, L, st, out, maps, cs, kchunk, zr, J, ss, step, wc, stream)
   if (applications == 2) {
     if (dense_j) FDTD_F(2, true);
     FDTD_F(2, false);
@@ -1051,15 +690,13 @@ static cudaError_t launch1_ry(const PLayout& L, const S& st, const S& out, const
 template <class S>
 cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const void* maps,
                               const float* const J[3], bool dense_j, const CoefSet& cs, const SourceSet& ss,
-                              int64_t step, int applications, const FusedConfig& cfg, bool b_first,
-                              const WaitCtl& wc, cudaStream_t stream, int kbeg, int kend) {
+                              int64_t step, int applications, const FusedConfig& cfg, const WaitCtl& wc,
+                              cudaStream_t stream, int kbeg, int kend) {
   const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 48;
   const StepMaps& m = *static_cast<const StepMaps*>(maps);
   const int2 zr = make_int2(kbeg, kend < 0 ? L.Nk : kend);
-#define FDTD_RY(RY)                                                                                               \
-  return b_first                                                                                                  \
-             ? launch1_ry<S, RY, true>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, zr, wc, stream) \
-             : launch1_ry<S, RY, false>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, zr, wc, stream)
+#define FDTD_RY(RY) \
+  return launch1_ry<S, RY>(L, st, out, m, J, dense_j, cs, ss, step, applications, kchunk, zr, wc, stream)
   if (cfg.tile_y == 6) FDTD_RY(6);
   if (cfg.tile_y == 30) FDTD_RY(30);
   FDTD_RY(14);
@@ -1072,7 +709,7 @@ static cudaError_t launch1_batch_one(const BatchDomain<S>* doms, const StepMaps*
                                      int* counters, const WaitCtl& wc, cudaStream_t stream) {
   using A = typename ArithOf1<S>::type;
   auto kern = fused1_batch<S, A, RY, APPS, SPLIT>;
-  const int bytes = Plan1<S, RY, true>::kTotal;
+  const int bytes = Plan1<S, RY>::kTotal;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
@@ -1112,8 +749,8 @@ cudaError_t launch_fused1_batch(const void* doms, const StepMaps* maps, const in
 }
 
 template <class S>
-void fused1_box_widths(bool b_first, int hi[6], int lo[6]) {
-  const BoxTable b = b_first ? Plan1<S, 14, true>::box() : Plan1<S, 14, false>::box();
+void fused1_box_widths(int hi[6], int lo[6]) {
+  const BoxTable b = Plan1<S, 14>::box();
   for (int c = 0; c < 6; ++c) {
     hi[c] = b.w[c];
     lo[c] = b.lw[c];
@@ -1123,12 +760,12 @@ void fused1_box_widths(bool b_first, int hi[6], int lo[6]) {
 #define FDTD_INSTANTIATE(S)                                                                              \
   template cudaError_t launch_fused1_f32<S>(const PLayout&, const S&, const S&, const void*,            \
                                             const float* const[3], bool, const CoefSet&, const SourceSet&, \
-                                            int64_t, int, const FusedConfig&, bool, const WaitCtl&, cudaStream_t,   \
+                                            int64_t, int, const FusedConfig&, const WaitCtl&, cudaStream_t,   \
                                             int, int);                                                     \
   template cudaError_t launch_fused1_batch<S>(const void*, const StepMaps*, const int4*, int, int, int,          \
                                               const FusedConfig&, const int64_t*, int, int*, const WaitCtl&,     \
                                               cudaStream_t);                                                     \
-  template void fused1_box_widths<S>(bool, int[6], int[6]);
+  template void fused1_box_widths<S>(int[6], int[6]);
 FDTD_INSTANTIATE(StoreF32)
 FDTD_INSTANTIATE(StoreF32C)
 FDTD_INSTANTIATE(StoreF16)

@@ -97,10 +97,9 @@ cudaError_t build_tma_maps(void* maps, const PLayout& L, HiType ht, void* const 
   const CUtensorMapDataType dt = ht == HiType::F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
   const size_t es = ht == HiType::F32 ? 4 : 2;
   for (int c = 0; c < 6; ++c) {
-    // E-first sweep: only Bx and Bz (components 3, 5) carry a second halo row
-    // (the row below the tile); B-first sweep: only Ex and Ez (0, 2) do (the
-    // row above it); every other box is one row shorter.
-    const bool tall = trim == BoxTrim::None || (trim == BoxTrim::EFirst ? (c == 3 || c == 5) : (c == 0 || c == 2));
+    // B-first sweeps: only Ex and Ez (0, 2) carry a second halo row (the
+    // row above the tile); every other box is one row shorter.
+    const bool tall = trim == BoxTrim::None || c == 0 || c == 2;
     const int rows = tall ? tile_y + 2 : tile_y + 1;
     if (!encode(&m->hi[c], dt, es, hi[c], L, box_w[c], rows)) return cudaErrorInvalidValue;
     if (lo && lo[c] && !encode(&m->lo[c], CU_TENSOR_MAP_DATA_TYPE_UINT16, sizeof(LoT), lo[c], L, lo_box_w[c], rows))
