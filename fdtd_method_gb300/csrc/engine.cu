@@ -185,14 +185,32 @@ struct LaunchTimer {
   }
 };
 
+bool b_first(const fdtd_handle* h);
+
 // B update with `apps` applications of the curl term (2: the last half
 // step of one update_fields and the first of the next share one sweep).
 int run_b(fdtd_handle* h, int apps) {
+  // the fused sweep's tiles, in place, where the handle has its second copy
+  // and one-cell maps (a z slab and the two-cell kernel use the column sweep)
+  const bool tiles = h->form != Form::F64 && !h->zhalo && h->alt_field[0] && b_first(h);
+  if (tiles)
+    if (int rc = ensure_alt(h)) return rc;
   LaunchTimer lt(h, apps == 2 ? FDTD_KERNEL_B_DOUBLE : FDTD_KERNEL_B_HALF);
   cudaError_t e = cudaSuccess;
   const Box box = h->sweep_box();
   const StateView v = h->sweep_view();
-  if (h->form == Form::F64) {
+  if (tiles) {
+    StepMaps sm;
+    sm.ld = h->bmaps_cur;
+    sm.st = h->smaps_cur;
+    const WaitCtl wc = h->wait_ctl();
+    switch (h->form) {
+      case Form::F32: e = launch_bhalf_f32(v.L, v.s32, v.s32, &sm, h->cs, apps, h->fused_cfg, wc, h->stream); break;
+      case Form::F32C: e = launch_bhalf_f32(v.L, v.s32c, v.s32c, &sm, h->cs, apps, h->fused_cfg, wc, h->stream); break;
+      case Form::F16: e = launch_bhalf_f32(v.L, v.s16, v.s16, &sm, h->cs, apps, h->fused_cfg, wc, h->stream); break;
+      default: e = cudaErrorInvalidValue; break;
+    }
+  } else if (h->form == Form::F64) {
     Fp64Fields F;
     for (int c = 0; c < 9; ++c) F.f[c] = (double*)h->field[c] - h->halo_elems();
     e = launch_b_fp64(v.g, box, F, &h->coef[3], apps, h->fp64_fma, h->stream);
@@ -523,11 +541,28 @@ int read_view(fdtd_handle* h, StateView* v) {
     const StateView cur = h->sweep_view(), side = h->with_halo(h->view_side());
     const Box box = h->sweep_box();
     cudaError_t e = cudaSuccess;
-    switch (h->form) {
-      case Form::F32: e = launch_b_f32_into(cur.L, cur.s32, side.s32, h->cs, box.k0, box.k1, h->stream); break;
-      case Form::F32C: e = launch_b_f32_into(cur.L, cur.s32c, side.s32c, h->cs, box.k0, box.k1, h->stream); break;
-      case Form::F16: e = launch_b_f32_into(cur.L, cur.s16, side.s16, h->cs, box.k0, box.k1, h->stream); break;
-      default: e = cudaErrorInvalidValue; break;
+    if (!h->zhalo && b_first(h)) {
+      // the fused sweep's tiles: loads from the current copy, stores into the
+      // second copy's B arrays
+      LaunchTimer lt(h, FDTD_KERNEL_B_HALF);
+      StepMaps sm;
+      sm.ld = h->bmaps_cur;
+      sm.st = h->smaps_alt;
+      const WaitCtl wc = h->wait_ctl();
+      switch (h->form) {
+        case Form::F32: e = launch_bhalf_f32(cur.L, cur.s32, side.s32, &sm, h->cs, 1, h->fused_cfg, wc, h->stream); break;
+        case Form::F32C: e = launch_bhalf_f32(cur.L, cur.s32c, side.s32c, &sm, h->cs, 1, h->fused_cfg, wc, h->stream); break;
+        case Form::F16: e = launch_bhalf_f32(cur.L, cur.s16, side.s16, &sm, h->cs, 1, h->fused_cfg, wc, h->stream); break;
+        default: e = cudaErrorInvalidValue; break;
+      }
+      lt.done();
+    } else {
+      switch (h->form) {
+        case Form::F32: e = launch_b_f32_into(cur.L, cur.s32, side.s32, h->cs, box.k0, box.k1, h->stream); break;
+        case Form::F32C: e = launch_b_f32_into(cur.L, cur.s32c, side.s32c, h->cs, box.k0, box.k1, h->stream); break;
+        case Form::F16: e = launch_b_f32_into(cur.L, cur.s16, side.s16, h->cs, box.k0, box.k1, h->stream); break;
+        default: e = cudaErrorInvalidValue; break;
+      }
     }
     if (e != cudaSuccess) return cuda_fail(e, "pending B half step");
     h->b_side = true;

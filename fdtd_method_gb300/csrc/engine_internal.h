@@ -138,6 +138,14 @@ cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const
 // maps.
 template <class S>
 void fused1_box_widths(int hi[6], int lo[6]);
+// kernels_fused1.cu: `applications` B half steps alone over planes
+// [kbeg, kend) (kend < 0: Nk), from `st` into `out` (which may be `st`), with
+// the fused sweep's tiles (32 x cfg.tile_y, cfg.kchunk planes) and its load
+// and store maps (`maps`: a StepMaps built for that tile height).
+template <class S>
+cudaError_t launch_bhalf_f32(const PLayout& L, const S& st, const S& out, const void* maps, const CoefSet& cs,
+                             int applications, const FusedConfig& cfg, const WaitCtl& wc, cudaStream_t stream,
+                             int kbeg = 0, int kend = -1);
 
 // kernels_tblock.cu: the depth-2 sweep (two B-first steps per pass; the
 // first step applies `apps1` B half steps, the second two) of one cell per

@@ -222,7 +222,9 @@ __device__ __forceinline__ void drain_tile(uint64_t* bar, uint32_t ring, int fir
 }
 
 // The sweep of one tile (see the file comment): planes k1-1 down to k0-1.
-template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSrc>
+// kE false: the B half steps alone (planes k1-1 down to k0, no E step and no
+// halo cells; E is only read, so `out` may be `st`).
+template <class S, class A, int RY, int kApps, bool kDenseJ, bool kSrc, bool kE = true>
 __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, const S& out, const StepMaps& maps,
                                                const CoefSet& cs, int bx, int by, int bz, int kchunk, int2 zr,
                                                const float* __restrict__ Jx, const float* __restrict__ Jy,
@@ -244,14 +246,15 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
   // row: they compute but never publish.
   const int r = hrow ? 0 : hcol ? min(lane, RY - 1) + 1 : w + 1;
   const int cx = hcol ? -1 : lane;
-  const bool active = hrow ? (lane < nx) : hcol ? (lane < ny) : (w < ny && lane < nx);
+  const bool active =
+      (kE || (!hrow && !hcol)) && (hrow ? (lane < nx) : hcol ? (lane < ny) : (w < ny && lane < nx));
   const bool interior = !hrow && !hcol && w < ny && lane < nx;
   // unwrapped coordinates (x = -1 and y = -1 are the ghost copies of Ni-1 and
   // Nj-1); interior cells have 0 <= x < Ni, 0 <= y < Nj
   const int xu = x0 + cx, yu = y0 + r - 1;
   const int k0 = zr.x + bz * kchunk;
   const int k1 = min(k0 + kchunk, zr.y);
-  const int n_it = k1 - k0 + 1;
+  const int n_it = kE ? k1 - k0 + 1 : k1 - k0;
   const bool leader = (w == RY + 1 && lane == 0);
   const int slot0 = (int)(ring % NS);
   const uint32_t phase0 = (ring / NS) & 1u;
@@ -373,7 +376,7 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
     // 2. E'(t+1), in the operation order of the E sweep (kernels_f32.cu e_sweep)
     Pair nex{0.f, 0.f}, ney{0.f, 0.f}, nez{0.f, 0.f};
     unsigned char* eb = smem + P::kBst + cur * P::kBBytes;
-    const bool e_step = it > 0;  // plane t+1 lies in the chunk
+    const bool e_step = kE && it > 0;  // plane t+1 lies in the chunk
     if (e_step && interior) {
       const int ke = t + 1;  // < k1 <= Nk
       const unsigned char* pb = smem + P::kExch + (cur ^ 1) * P::kXBytes;
@@ -597,6 +600,23 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
   if (threadIdx.x == 0 && threadIdx.y == RY + 1) bulk_wait_all();  // the copy-engine leader's stores
 }
 
+// The B half steps alone (`apps` of them) over planes [zr.x, zr.y), from
+// `st` into `out` (which may be `st`): the tile machinery of the fused sweep
+// without its E step.
+template <class S, class A, int RY, int kApps>
+__global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
+    fused1_bhalf(PLayout L, S st, S out, const __grid_constant__ StepMaps maps, CoefSet cs, int kchunk, int2 zr,
+                 WaitCtl wc) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
+  uint32_t ring = 0;
+  SourceSet none{};
+  fused1b_planes<S, A, RY, kApps, false, false, false>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z,
+                                                       kchunk, zr, nullptr, nullptr, nullptr, none, 0, wc, smem, ring,
+                                                       0);
+  if (threadIdx.x == 0 && threadIdx.y == RY + 1) bulk_wait_all();  // the copy-engine leader's stores
+}
+
 // Batched form: a persistent kernel of B-first sweeps; every CTA takes tiles
 // (domain, bx, by, bz) from the tile table in order, through an atomic
 // counter, until none are left.  `parity` selects which of each domain's two
@@ -703,6 +723,34 @@ cudaError_t launch_fused1_f32(const PLayout& L, const S& st, const S& out, const
 #undef FDTD_RY
 }
 
+template <class S, int RY>
+static cudaError_t launch_bhalf_ry(const PLayout& L, const S& st, const S& out, const StepMaps& m, const CoefSet& cs,
+                                   int applications, int kchunk, int2 zr, const WaitCtl& wc, cudaStream_t stream) {
+  using A = typename ArithOf1<S>::type;
+  const dim3 grid((L.Ni + 31) / 32, (L.Nj + RY - 1) / RY, (zr.y - zr.x + kchunk - 1) / kchunk);
+  auto kern = applications == 2 ? fused1_bhalf<S, A, RY, 2> : fused1_bhalf<S, A, RY, 1>;
+  const int bytes = Plan1<S, RY>::kTotal;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, dim3(32, RY + 2), bytes, stream>>>(L, st, out, m, cs, kchunk, zr, wc);
+  return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t launch_bhalf_f32(const PLayout& L, const S& st, const S& out, const void* maps, const CoefSet& cs,
+                             int applications, const FusedConfig& cfg, const WaitCtl& wc, cudaStream_t stream,
+                             int kbeg, int kend) {
+  if (kend < 0) kend = L.Nk;
+  if (kbeg < 0 || kend > L.Nk) return cudaErrorInvalidValue;
+  if (kend <= kbeg) return cudaSuccess;
+  const StepMaps& m = *static_cast<const StepMaps*>(maps);
+  const int2 zr = make_int2(kbeg, kend);
+  const int kchunk = cfg.kchunk > 0 ? cfg.kchunk : 48;
+  if (cfg.tile_y == 6) return launch_bhalf_ry<S, 6>(L, st, out, m, cs, applications, kchunk, zr, wc, stream);
+  if (cfg.tile_y == 30) return launch_bhalf_ry<S, 30>(L, st, out, m, cs, applications, kchunk, zr, wc, stream);
+  return launch_bhalf_ry<S, 14>(L, st, out, m, cs, applications, kchunk, zr, wc, stream);
+}
+
 template <class S, int RY, int APPS, bool SPLIT>
 static cudaError_t launch1_batch_one(const BatchDomain<S>* doms, const StepMaps* maps, const int4* tiles,
                                      int n_tiles, int parity, int kchunk, const int64_t* step_base, int step_off,
@@ -765,7 +813,9 @@ void fused1_box_widths(int hi[6], int lo[6]) {
   template cudaError_t launch_fused1_batch<S>(const void*, const StepMaps*, const int4*, int, int, int,          \
                                               const FusedConfig&, const int64_t*, int, int*, const WaitCtl&,     \
                                               cudaStream_t);                                                     \
-  template void fused1_box_widths<S>(int[6], int[6]);
+  template void fused1_box_widths<S>(int[6], int[6]);                                                 \
+  template cudaError_t launch_bhalf_f32<S>(const PLayout&, const S&, const S&, const void*, const CoefSet&, int, \
+                                           const FusedConfig&, const WaitCtl&, cudaStream_t, int, int);
 FDTD_INSTANTIATE(StoreF32)
 FDTD_INSTANTIATE(StoreF32C)
 FDTD_INSTANTIATE(StoreF16)

@@ -192,3 +192,26 @@ def test_wait_that_gives_up_is_reported_and_the_context_stays_usable(cpt):
     np.testing.assert_array_equal(np.concatenate(_fields(t)), np.concatenate(_fields(s)))
     s.close()
     t.close()
+
+
+@pytest.mark.parametrize("tile_y", [6, 14, 30])
+@pytest.mark.parametrize("prec", FORMS)
+def test_tile_and_column_b_half_sweeps_agree(prec, tile_y):
+    """The B half sweeps run on the fused sweep's tiles once a handle has its
+    second copy (here: after a read with a half step pending), and as column
+    sweeps before that; both give the bits of the other (split pipeline,
+    several z chunks per column, sources and a pending half on every read)."""
+    p, vals, srcs = _setup((70, 45, 53), 21)
+    runs = []
+    for read_early in (False, True):
+        s = _make(p, prec, vals, srcs, pipeline="split", cpt=1)
+        s.set_pipeline("split", tile_y, 16, 1)
+        s.step(2)
+        if read_early:
+            s.copy_to_host(4)  # allocates the second copy: tile sweeps from here on
+        s.step(5)
+        s.update_fields()
+        runs.append(_fields(s))
+        s.close()
+    for c in range(6):
+        np.testing.assert_array_equal(runs[0][c], runs[1][c], err_msg="component %d" % c)
