@@ -186,8 +186,9 @@ cudaError_t launch_fused1_batch(const void* doms, const StepMaps* maps, const in
                                 int applications, const FusedConfig& cfg, const int64_t* step_base, int step_off,
                                 int* counters, const WaitCtl& wc, cudaStream_t stream);
 
-// kernels_f32.cu: the leading B half step of every domain in place on copy
-// `parity`, as one launch of 32 x 8 blocks marching kBatchBChunk planes;
+// kernels_f32.cu: one B half step of every domain in place on copy `parity`
+// (the batch's pending half), as one launch of 32 x 8 blocks marching
+// kBatchBChunk planes;
 // block_start[d] is the first block of domain d (n_dom + 1 entries).
 constexpr int kBatchBChunk = 16;
 template <class S>

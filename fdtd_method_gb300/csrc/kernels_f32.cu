@@ -5,9 +5,11 @@
 // per cell-step.  x/y neighbours come from the ghost cells; z wraps by index.
 //
 // Same stencil as the FP64 drop-in (kokkos_functors.h:64-90 E, :128-151 B);
-// the arithmetic comes from the policies in arith.cuh.  The first B half step
-// of every run uses b_sweep; the fused pipeline (kernels_fused.cu) evaluates
-// the same arithmetic and reproduces these sweeps bit for bit.
+// the arithmetic comes from the policies in arith.cuh.  These sweeps run the
+// split pipeline of a handle without its second copy, z slabs' split
+// schedule and the batch's pending half; the fused sweeps (kernels_fused1.cu,
+// kernels_fused.cu, kernels_tblock.cu) evaluate the same arithmetic and
+// reproduce them bit for bit.
 #include "arith.cuh"
 #include "engine_internal.h"
 #include "sources.cuh"
@@ -53,8 +55,9 @@ __global__ void __launch_bounds__(256) b_sweep(PLayout L, S st, S out, CoefSet c
                                 blockIdx.y * blockDim.y + threadIdx.y, kbeg + blockIdx.z * kchunk, kchunk, kend);
 }
 
-// The leading B half step of every domain of a batch: block b belongs to the
-// domain d with block_start[d] <= b < block_start[d+1].
+// One B half step of every domain of a batch (the pending one, applied before
+// a write): block b belongs to the domain d with block_start[d] <= b <
+// block_start[d+1].
 template <class S, class A>
 __global__ void __launch_bounds__(256) b_sweep_batch(const BatchDomain<S>* __restrict__ doms,
                                                      const int64_t* __restrict__ block_start, int n_dom, int parity) {
