@@ -6,9 +6,10 @@
 //   ArithPlain  l is always 0: plain FP32 (also the FP16 storage form).
 //   ArithComp   compensated accumulation: the curl increment is one float
 //               formed from differences that keep both words of each pair,
-//               and it is added to the stored pair error-free (TwoSum, then
-//               renormalisation), so the accumulated field loses nothing but
-//               its final rounding.  Source terms are double-float products
+//               and it is added to the stored pair with Fast2Sum (exact
+//               where the field outweighs its increment) and renormalised,
+//               so the accumulated field loses nothing but its final
+//               rounding.  Source terms are double-float products
 //               (FMA splits).  This is the compensated form (a BF16 l word
 //               keeps the pair's significand at 32 bits or more, against 24
 //               for plain FP32).
@@ -82,7 +83,7 @@ struct ArithComp {
   // The curl increment c1 (a1 - b1) - c2 (a2 - b2) as one float (lo = 0),
   // with the coefficients' lo parts folded in.  Its rounding error is
   // relative to the increment, a small fraction of the field it is added
-  // to; the accumulation (acc) is the error-free part.
+  // to; the accumulation (acc) is the compensated part.
   __device__ __forceinline__ static Pair curl(Coef c1, Pair a1, Pair b1, Coef c2, Pair a2, Pair b2) {
     const float d1 = dif(a1, b1), d2 = dif(a2, b2);
     const float m = __fmaf_rn(c2.hi, d2, __fmul_rn(c2.lo, d2));
@@ -110,10 +111,13 @@ struct ArithComp {
   __device__ __forceinline__ static bool cur_nonzero(Cur a) { return a.hi != 0.f || a.lo != 0.f; }
   __device__ __forceinline__ static Pair cur_term(Coef cj, Cur j) { return df_mul(Pair{cj.hi, cj.lo}, j); }
 
-  // v + t, renormalised: |l| <= ulp(h)/2 afterwards.
+  // v + t, renormalised: |l| <= ulp(h)/2 afterwards.  The sum of the hi
+  // words is split with Fast2Sum, exact when |v.hi| >= |t.hi| (the field
+  // against its increment: every cell but those where the field crosses
+  // zero, whose error then stays within an ulp of the increment).
   __device__ __forceinline__ static Pair acc(Pair v, Pair t) {
-    float s, e;
-    two_sum(v.hi, t.hi, s, e);
+    const float s = __fadd_rn(v.hi, t.hi);
+    const float e = __fsub_rn(t.hi, __fsub_rn(s, v.hi));
     const float l = __fadd_rn(__fadd_rn(v.lo, e), t.lo);
     const float h2 = __fadd_rn(s, l);
     const float l2 = __fsub_rn(l, __fsub_rn(h2, s));

@@ -75,8 +75,8 @@ struct Arith2<ArithComp> {
     return P2{mul2(t.hi, make_float2(2.f, 2.f)), mul2(t.lo, make_float2(2.f, 2.f))};
   }
   __device__ __forceinline__ static P2 acc(P2 v, P2 t) {
-    float2 s, e;
-    two_sum2(v.hi, t.hi, s, e);
+    const float2 s = add2(v.hi, t.hi);
+    const float2 e = sub2(t.hi, sub2(s, v.hi));
     const float2 l = add2(add2(v.lo, e), t.lo);
     const float2 h2 = add2(s, l);
     return P2{h2, sub2(l, sub2(h2, s))};
