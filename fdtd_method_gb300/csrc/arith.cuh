@@ -59,6 +59,7 @@ struct ArithPlain {
   __device__ __forceinline__ static Pair add(Pair p, Pair q) { return Pair{__fadd_rn(p.hi, q.hi), 0.f}; }
   __device__ __forceinline__ static Pair twice(Pair t) { return Pair{2.f * t.hi, 0.f}; }
   __device__ __forceinline__ static Pair acc(Pair v, Pair t) { return Pair{__fadd_rn(v.hi, t.hi), 0.f}; }
+  __device__ __forceinline__ static Pair acc_curl(Pair v, Pair t) { return acc(v, t); }
 
   // Current values: FP32.
   using Cur = float;
@@ -119,6 +120,17 @@ struct ArithComp {
     const float s = __fadd_rn(v.hi, t.hi);
     const float e = __fsub_rn(t.hi, __fsub_rn(s, v.hi));
     const float l = __fadd_rn(__fadd_rn(v.lo, e), t.lo);
+    const float h2 = __fadd_rn(s, l);
+    const float l2 = __fsub_rn(l, __fsub_rn(h2, s));
+    return Pair{h2, l2};
+  }
+  // acc for an increment whose lo word is zero (a curl term without
+  // current): the same value without the addition of t.lo (it can differ
+  // from acc only in the sign of a zero lo word).
+  __device__ __forceinline__ static Pair acc_curl(Pair v, Pair t) {
+    const float s = __fadd_rn(v.hi, t.hi);
+    const float e = __fsub_rn(t.hi, __fsub_rn(s, v.hi));
+    const float l = __fadd_rn(v.lo, e);
     const float h2 = __fadd_rn(s, l);
     const float l2 = __fsub_rn(l, __fsub_rn(h2, s));
     return Pair{h2, l2};

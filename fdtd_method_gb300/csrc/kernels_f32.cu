@@ -41,9 +41,9 @@ __device__ __forceinline__ void b_column(const PLayout& L, const S& st, const S&
       ty = A::twice(ty);
       tz = A::twice(tz);
     }
-    store_with_ghosts(out, L, 3, i, j, k, A::acc(st.load(3, col + base), tx));
-    store_with_ghosts(out, L, 4, i, j, k, A::acc(st.load(4, col + base), ty));
-    store_with_ghosts(out, L, 5, i, j, k, A::acc(st.load(5, col + base), tz));
+    store_with_ghosts(out, L, 3, i, j, k, A::acc_curl(st.load(3, col + base), tx));
+    store_with_ghosts(out, L, 4, i, j, k, A::acc_curl(st.load(4, col + base), ty));
+    store_with_ghosts(out, L, 5, i, j, k, A::acc_curl(st.load(5, col + base), tz));
     ex = ex_kn;
     ey = ey_kn;
   }
@@ -115,9 +115,9 @@ __global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __r
     if (has & 1u) tx = A::add(tx, A::cur_term(jcoef<S>(cs, st, 0), jv[0]));
     if (has & 2u) ty = A::add(ty, A::cur_term(jcoef<S>(cs, st, 1), jv[1]));
     if (has & 4u) tz = A::add(tz, A::cur_term(jcoef<S>(cs, st, 2), jv[2]));
-    store_with_ghosts(st, L, 0, i, j, k, A::acc(st.load(0, col + base), tx));
-    store_with_ghosts(st, L, 1, i, j, k, A::acc(st.load(1, col + base), ty));
-    store_with_ghosts(st, L, 2, i, j, k, A::acc(st.load(2, col + base), tz));
+    store_with_ghosts(st, L, 0, i, j, k, (has & 1u) ? A::acc(st.load(0, col + base), tx) : A::acc_curl(st.load(0, col + base), tx));
+    store_with_ghosts(st, L, 1, i, j, k, (has & 2u) ? A::acc(st.load(1, col + base), ty) : A::acc_curl(st.load(1, col + base), ty));
+    store_with_ghosts(st, L, 2, i, j, k, (has & 4u) ? A::acc(st.load(2, col + base), tz) : A::acc_curl(st.load(2, col + base), tz));
     bx_kp = bx;
     by_kp = by;
   }

@@ -352,8 +352,8 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
       uy = A::twice(uy);
       uz = A::twice(uz);
     }
-    const Pair ax = A::acc(V(Comp<3>{}, 0, 0), ux), ay = A::acc(V(Comp<4>{}, 0, 0), uy),
-               az = A::acc(V(Comp<5>{}, 0, 0), uz);
+    const Pair ax = A::acc_curl(V(Comp<3>{}, 0, 0), ux), ay = A::acc_curl(V(Comp<4>{}, 0, 0), uy),
+               az = A::acc_curl(V(Comp<5>{}, 0, 0), uz);
     // B' in its stored words; the E update uses the value they hold.
     const HiT bhx = st.enc_hi(3, ax), bhy = st.enc_hi(4, ay), bhz = st.enc_hi(5, az);
     const LoT blx = st.enc_lo(ax), bly = st.enc_lo(ay), blz = st.enc_lo(az);
@@ -388,9 +388,9 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
       Pair qx = A::curl(ecoef<S>(cs, st, 0, 0), pbz, Bn(2, xo_down), ecoef<S>(cs, st, 0, 1), pby, nby);
       Pair qy = A::curl(ecoef<S>(cs, st, 1, 0), pbx, nbx, ecoef<S>(cs, st, 1, 1), pbz, Bn(2, xo_left));
       Pair qz = A::curl(ecoef<S>(cs, st, 2, 0), pby, Bn(1, xo_left), ecoef<S>(cs, st, 2, 1), pbx, Bn(0, xo_down));
+      unsigned has = 0;  // E components that received current (their increment has a lo word)
       if (kDenseJ || kSrc) {
         T jv[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};
-        unsigned has = 0;
         if (kDenseJ) {
           const int64_t d = xu + (int64_t)yu * L.Ni + (int64_t)ke * L.Ni * L.Nj;
           jv[0] = A::cur_dense(Jx[d]);
@@ -428,9 +428,9 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
         if (has & 2u) qy = A::add(qy, A::cur_term(jcoef<S>(cs, st, 1), jv[1]));
         if (has & 4u) qz = A::add(qz, A::cur_term(jcoef<S>(cs, st, 2), jv[2]));
       }
-      nex = A::acc(pex, qx);
-      ney = A::acc(pey, qy);
-      nez = A::acc(pez, qz);
+      nex = (has & 1u) ? A::acc(pex, qx) : A::acc_curl(pex, qx);
+      ney = (has & 2u) ? A::acc(pey, qy) : A::acc_curl(pey, qy);
+      nez = (has & 4u) ? A::acc(pez, qz) : A::acc_curl(pez, qz);
       HiT* eh = reinterpret_cast<HiT*>(eb) + bo_own;
       eh[0] = st.enc_hi(0, nex);
       eh[P::kBComp] = st.enc_hi(1, ney);

@@ -330,7 +330,7 @@ __device__ __forceinline__ bool tblock_tile(const PLayout& L, const S& st, const
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         if (kApps1 == 2) u[c] = A::twice(u[c]);
-        nb1[c] = q3(A::acc(V(3 + c, 0, 0), u[c]), 3 + c);
+        nb1[c] = q3(A::acc_curl(V(3 + c, 0, 0), u[c]), 3 + c);
       }
     }
     if (b1 && s >= k0 - 2)
@@ -370,7 +370,7 @@ __device__ __forceinline__ bool tblock_tile(const PLayout& L, const S& st, const
       const int i3 = cy < 0 ? (cx < 0 ? (RY + 1) * 32 : RY * 32 + cx) : (cx < 0 ? (RY + 1) * 32 + cy + 1 : cy * 32 + cx);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        nb2[c] = q3(A::acc(b1p2[c], A::twice(u[c])), 3 + c);
+        nb2[c] = q3(A::acc_curl(b1p2[c], A::twice(u[c])), 3 + c);
         xput(x3at, P::kX3, c, i3, nb2[c], 3 + c);
       }
     }
