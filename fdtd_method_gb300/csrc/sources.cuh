@@ -9,8 +9,11 @@
 
 namespace fdtd {
 
-// Sources whose per-column factor a kernel keeps in registers.
-constexpr int kFastSources = 2;
+// Sources whose per-column factor a kernel keeps in registers (the first
+// listed for a tile; further ones are evaluated per cell).  One: with two,
+// the batched compensated sweep spilled 92 bytes per thread and ran 12 %
+// slower on its workload of one pulse per domain.
+constexpr int kFastSources = 1;
 
 template <class A>
 __device__ __forceinline__ void add_current(typename A::Cur jv[3], int mask, typename A::Cur v) {
