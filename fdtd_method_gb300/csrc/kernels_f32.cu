@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256) e_sweep(PLayout L, S st, const float* __r
       jv[2] = A::cur_dense(Jz[d]);
       has = 7u;
     }
-    if (kSources) has |= source_sum<A>(ss, step, i, j, k, L, jv);
+    if (kSources) has |= source_sum<A>(ss, step, i, j, k, L, jv, has);
     if (has & 1u) tx = A::add(tx, A::cur_term(jcoef<S>(cs, st, 0), jv[0]));
     if (has & 2u) ty = A::add(ty, A::cur_term(jcoef<S>(cs, st, 1), jv[1]));
     if (has & 4u) tz = A::add(tz, A::cur_term(jcoef<S>(cs, st, 2), jv[2]));

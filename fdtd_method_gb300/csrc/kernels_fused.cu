@@ -246,11 +246,11 @@ __global__ void __launch_bounds__(32 * (RY + 2))
           }
         }
         if (kSrc == 1) {
-          if (e0) h0 |= src0.eval(ss, kk, L, j0);
-          if (e1) h1 |= src1.eval(ss, kk, L, j1);
+          if (e0) h0 |= src0.eval(ss, kk, L, j0, h0);
+          if (e1) h1 |= src1.eval(ss, kk, L, j1, h1);
         } else if (kSrc == 2) {
-          if (e0) h0 |= source_sum<A>(ss, step, xl0, yl, kk, L, j0);
-          if (e1) h1 |= source_sum<A>(ss, step, xl1, yl, kk, L, j1);
+          if (e0) h0 |= source_sum<A>(ss, step, xl0, yl, kk, L, j0, h0);
+          if (e1) h1 |= source_sum<A>(ss, step, xl1, yl, kk, L, j1, h1);
         }
         if (h0 || h1) {
           // per lane, exactly the one-cell update: add cJ J only where current flows

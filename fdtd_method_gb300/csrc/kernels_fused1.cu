@@ -404,7 +404,7 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
             const DevSource& d = ss.src[list[q]];
             const int dk = box_offset(ke, d.k0, d.nk, L.Nk);  // the same for the whole tile
             if (dk >= 0 && (smask >> q & 1u)) {
-              add_current<A>(jv, d.comp_mask, A::cur_mul(sxy[q], A::cur_table(ss, d.gz_off + dk)));
+              add_current<A>(jv, d.comp_mask, A::cur_mul(sxy[q], A::cur_table(ss, d.gz_off + dk)), has);
               has |= (unsigned)d.comp_mask;
             }
           }
@@ -420,7 +420,8 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
                            A::cur_mul(A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + step),
                                                             A::cur_table(ss, d.gx_off + di)),
                                                  A::cur_table(ss, d.gy_off + dj)),
-                                      A::cur_table(ss, d.gz_off + dk)));
+                                      A::cur_table(ss, d.gz_off + dk)),
+                           has);
             has |= (unsigned)d.comp_mask;
           }
         }

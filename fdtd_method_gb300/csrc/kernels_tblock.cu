@@ -250,7 +250,7 @@ __device__ __forceinline__ bool tblock_tile(const PLayout& L, const S& st, const
         const DevSource& d = ss.src[list[q]];
         const int dk = box_offset(ke, d.k0, d.nk, L.Nk);
         if (dk >= 0 && (smask >> q & 1u) && sh < d.n_amp) {
-          add_current<A>(jv, d.comp_mask, A::cur_mul(sxy[h][q], A::cur_table(ss, d.gz_off + dk)));
+          add_current<A>(jv, d.comp_mask, A::cur_mul(sxy[h][q], A::cur_table(ss, d.gz_off + dk)), has);
           has |= (unsigned)d.comp_mask;
         }
       }
@@ -266,7 +266,8 @@ __device__ __forceinline__ bool tblock_tile(const PLayout& L, const S& st, const
         add_current<A>(jv, d.comp_mask,
                        A::cur_mul(A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + sh), A::cur_table(ss, d.gx_off + di)),
                                              A::cur_table(ss, d.gy_off + dj)),
-                                  A::cur_table(ss, d.gz_off + dk)));
+                                  A::cur_table(ss, d.gz_off + dk)),
+                       has);
         has |= (unsigned)d.comp_mask;
       }
     }

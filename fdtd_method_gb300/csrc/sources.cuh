@@ -15,19 +15,23 @@ namespace fdtd {
 // slower on its workload of one pulse per domain.
 constexpr int kFastSources = 1;
 
+// jv[c] += v for the components in `mask`; a component not yet in `set`
+// (bit c: jv[c] already holds current) takes v itself, which is the bits of
+// 0 + v (v is a normalised value) without the addition.
 template <class A>
-__device__ __forceinline__ void add_current(typename A::Cur jv[3], int mask, typename A::Cur v) {
-  if (mask & 1) jv[0] = A::cur_add(jv[0], v);
-  if (mask & 2) jv[1] = A::cur_add(jv[1], v);
-  if (mask & 4) jv[2] = A::cur_add(jv[2], v);
+__device__ __forceinline__ void add_current(typename A::Cur jv[3], int mask, typename A::Cur v, unsigned set) {
+  if (mask & 1) jv[0] = (set & 1u) ? A::cur_add(jv[0], v) : v;
+  if (mask & 2) jv[1] = (set & 2u) ? A::cur_add(jv[1], v) : v;
+  if (mask & 4) jv[2] = (set & 4u) ? A::cur_add(jv[2], v) : v;
 }
 
-// Every source at logical cell (i, j, k), time step s.  Returns the mask of
-// the J components that received current (bit c: component c); only those
-// get the current term.
+// Every source at logical cell (i, j, k), time step s, added to jv (whose
+// components in `set` already hold current).  Returns the mask of the J
+// components that received current (bit c: component c); only those get the
+// current term.
 template <class A>
 __device__ __forceinline__ unsigned source_sum(const SourceSet& ss, int64_t s, int i, int j, int k,
-                                               const PLayout& L, typename A::Cur jv[3]) {
+                                               const PLayout& L, typename A::Cur jv[3], unsigned set) {
   unsigned any = 0;
   for (int q = 0; q < ss.count; ++q) {
     const DevSource& d = ss.src[q];
@@ -42,7 +46,7 @@ __device__ __forceinline__ unsigned source_sum(const SourceSet& ss, int64_t s, i
         A::cur_mul(A::cur_mul(A::cur_mul(A::cur_table(ss, d.amp_off + s), A::cur_table(ss, d.gx_off + di)),
                               A::cur_table(ss, d.gy_off + dj)),
                    A::cur_table(ss, d.gz_off + dk));
-    add_current<A>(jv, d.comp_mask, v);
+    add_current<A>(jv, d.comp_mask, v, set | any);
     any |= (unsigned)d.comp_mask;
   }
   return any;
@@ -74,7 +78,7 @@ struct ColumnSources {
   // Adds the contributions at plane k; returns the mask of J components that
   // received current.
   __device__ __forceinline__ unsigned eval(const SourceSet& ss, int k, const PLayout& L,
-                                           typename A::Cur jv[3]) const {
+                                           typename A::Cur jv[3], unsigned set) const {
     unsigned any = 0;
 #pragma unroll
     for (int q = 0; q < kFastSources; ++q) {
@@ -82,7 +86,7 @@ struct ColumnSources {
         const DevSource& d = ss.src[q];
         const int dk = box_offset(k, d.k0, d.nk, L.Nk);
         if (dk >= 0) {
-          add_current<A>(jv, d.comp_mask, A::cur_mul(xy[q], A::cur_table(ss, d.gz_off + dk)));
+          add_current<A>(jv, d.comp_mask, A::cur_mul(xy[q], A::cur_table(ss, d.gz_off + dk)), set | any);
           any |= (unsigned)d.comp_mask;
         }
       }
