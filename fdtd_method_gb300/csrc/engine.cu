@@ -1214,6 +1214,10 @@ int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out) 
       for (int kc : kTuneChunksDepth2) cands.emplace_back(2, 1, ry, kc);
     const int depth_before = h->fused_cfg.depth;
     int rc = FDTD_OK;
+    // An E-first (two-cell) sweep needs a B half sweep at the start of every
+    // call: with update_fields called once per step, as the reference's
+    // callers do, that is one more sweep per step, which its candidates pay.
+    double ms_lead_half = -1.0;
     for (const auto& cand : cands) {
       const int depth = std::get<0>(cand);
       h->fused_cfg.depth = 1;
@@ -1235,7 +1239,30 @@ int fdtd_autotune(fdtd_handle* h, int sweeps, int reuse, fdtd_tune_result* out) 
         break;
       }
       best.candidates += 1;
-      const double per_step = ms / sweeps / depth;
+      if (std::get<1>(cand) == 2 && ms_lead_half < 0.0) {
+        // the column B half sweep the E-first pipeline starts a call with,
+        // timed into the second copy's B arrays (the state is only read)
+        const StateView cur = h->view(), side = h->view_side();
+        e = cudaEventRecord(e0, h->stream);
+        for (int q = 0; q < sweeps && e == cudaSuccess; ++q) {
+          switch (h->form) {
+            case Form::F32: e = launch_b_f32_into(h->L, cur.s32, side.s32, h->cs, 0, h->g.Nk, h->stream); break;
+            case Form::F32C: e = launch_b_f32_into(h->L, cur.s32c, side.s32c, h->cs, 0, h->g.Nk, h->stream); break;
+            case Form::F16: e = launch_b_f32_into(h->L, cur.s16, side.s16, h->cs, 0, h->g.Nk, h->stream); break;
+            default: e = cudaErrorInvalidValue; break;
+          }
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float mh = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&mh, e0, e1);
+        if (e != cudaSuccess) {
+          rc = cuda_fail(e, "autotune B half sweep");
+          break;
+        }
+        ms_lead_half = mh / sweeps;
+      }
+      const double per_step = ms / sweeps / depth + (std::get<1>(cand) == 2 ? ms_lead_half : 0.0);
       if (per_step < best.ms_per_sweep) {
         best.ms_per_sweep = per_step;
         best.tile_y = std::get<2>(cand);

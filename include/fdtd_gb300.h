@@ -274,8 +274,10 @@ int fdtd_kernel_times(fdtd_handle* h, double ms[FDTD_KERNEL_KINDS], int64_t laun
  * launch shape of the FP32-arithmetic forms (cells_per_thread 1 with tile_y
  * 6, 14 and 30; cells_per_thread 2 with tile_y 6 and 14; each with kchunk 16,
  * 24, 32, 48, 64 and 96; and the depth-2 sweep with tile_y 6 and 14 and
- * kchunk 24, 48 and 96, compared per step) on the handle's own grid, and
- * keeps the fastest
+ * kchunk 24, 48 and 96, compared per step; a two-cell shape, whose E-first
+ * pipeline starts every call with a B half sweep, is charged that sweep per
+ * step, as update_fields once per step costs it) on the handle's own grid,
+ * and keeps the fastest
  * (fdtd_set_pipeline's shape arguments).  The timed sweeps read the current
  * state and write the handle's second copy, so the simulation state does not
  * change.  Results are cached per (precision, Ni, Nj, Nk) in the process;
