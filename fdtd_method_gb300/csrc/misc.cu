@@ -158,13 +158,33 @@ __global__ void __launch_bounds__(kDiagThreads) sums_pass2(const double* partial
 // as their bits; NaN is skipped by fmaxf).  out must hold zeros.
 __global__ void __launch_bounds__(256) f16_absmax_kernel(PLayout L, StoreF16 st, unsigned* out) {
   float m[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  // Work items: per grid row, its 16-byte groups of 8 words (rows start on
+  // 64-byte boundaries), then the words past the last whole group.
   const int64_t rows = (int64_t)L.Nj * L.Nk;
-  for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+  const int groups = L.Ni / 8, per_row = groups + (L.Ni - groups * 8);
+  const int64_t items = rows * per_row;
+  for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < items;
+       it += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = it / per_row;
+    const int q = (int)(it - row * per_row);
     const int z = (int)(row / L.Nj), y = (int)(row - (int64_t)z * L.Nj);
     const int64_t base = L.at(0, y, z);
-    for (int x = threadIdx.x; x < L.Ni; x += blockDim.x)
+    if (q < groups) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const uint4 w = *reinterpret_cast<const uint4*>(st.v[c] + base + 8 * q);
+        const unsigned u[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&u[k]));
+          m[c] = fmaxf(m[c], fmaxf(fabsf(f.x), fabsf(f.y)));
+        }
+      }
+    } else {
+      const int x = groups * 8 + (q - groups);
 #pragma unroll
       for (int c = 0; c < 6; ++c) m[c] = fmaxf(m[c], fabsf(__half2float(st.v[c][base + x])));
+    }
   }
   __shared__ float red[8][6];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
