@@ -53,7 +53,12 @@ namespace fdtd {
 template <class S> struct ArithOf1 { using type = ArithPlain; };
 template <> struct ArithOf1<StoreF32C> { using type = ArithComp; };
 
-constexpr int kStages1 = 3;
+// Ring stages per storage form.  Three for the FP32 words (the compensated
+// form's 21.6 KB stages of a 14-row tile leave room for no more at two CTAs
+// per SM; plain FP32 measured 2-10 % slower with four or six), four for the
+// FP16 words (8 KB stages; 0.8 % faster than three, and flat up to eight).
+template <class S>
+constexpr int kStages1 = sizeof(typename S::HiT) == 2 ? 4 : 3;
 constexpr int kLoOff1 = 8;  // BF16 lo boxes start 8 columns left of the tile
 
 // Box widths (elements) and the left offset of the boxes that hold the
@@ -171,10 +176,11 @@ struct Plan1 {
   static constexpr int kBLo = round128(3 * kBComp * HS);
   static constexpr int kBBytes = kBLo + (kLo ? round128(3 * kBComp * LS) : 0);
   static constexpr int kRing = 0;
-  static constexpr int kExch = kStages1 * kStage;
+  static constexpr int kNS = kStages1<S>;
+  static constexpr int kExch = kNS * kStage;
   static constexpr int kBst = kExch + 2 * kXBytes;
   static constexpr int kBar = kBst + 2 * kBBytes;
-  static constexpr int kList = kBar + kStages1 * 8;
+  static constexpr int kList = kBar + kNS * 8;
   static constexpr int kTotal = kList + 4 * (kMaxSources + 1);
   // The box the B-first sweep's halo column reads starts one column left of
   // the tile, inside every box's left offset.
@@ -235,7 +241,7 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
   using P = Plan1<S, RY>;
   using HiT = typename S::HiT;
   using T = typename A::Cur;
-  constexpr int NS = kStages1;
+  constexpr int NS = P::kNS;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + P::kBar);
   int* list = reinterpret_cast<int*>(smem + P::kList);
 
@@ -606,7 +612,7 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
            const float* __restrict__ Jx, const float* __restrict__ Jy, const float* __restrict__ Jz,
            SourceSet ss, int64_t step, WaitCtl wc) {
   extern __shared__ __align__(128) unsigned char smem[];
-  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
+  init_ring<Plan1<S, RY>::kNS>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
   uint32_t ring = 0;
   fused1_tile<S, A, RY, kApps, kDenseJ, true>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z, kchunk, zr,
                                                    Jx, Jy, Jz, ss, step, wc, smem, ring);
@@ -621,7 +627,7 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
     fused1_bhalf(PLayout L, S st, S out, const __grid_constant__ StepMaps maps, CoefSet cs, int kchunk, int2 zr,
                  WaitCtl wc) {
   extern __shared__ __align__(128) unsigned char smem[];
-  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
+  init_ring<Plan1<S, RY>::kNS>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
   uint32_t ring = 0;
   SourceSet none{};
   fused1b_planes<S, A, RY, kApps, false, false, false>(L, st, out, maps, cs, blockIdx.x, blockIdx.y, blockIdx.z,
@@ -643,7 +649,7 @@ __global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ BatchDomain<S> dom;
   __shared__ int4 tile;
-  init_ring<kStages1>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
+  init_ring<Plan1<S, RY>::kNS>(reinterpret_cast<uint64_t*>(smem + Plan1<S, RY>::kBar));
   const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const int64_t step = *step_base + step_off;
