@@ -86,10 +86,13 @@ __device__ __forceinline__ void for_each_comp(F&& f) {
   f(Comp<5>{});
 }
 
-// CTAs per SM the register budget is sized for (30-row tiles: one
-// 1024-thread CTA; otherwise two).
-template <int RY>
-constexpr int kMinCtas1 = RY == 30 ? 1 : 2;
+// CTAs per SM the register budget is sized for: one 1024-thread CTA for
+// 30-row tiles, otherwise two; three for the step sweep of FP16 words in
+// 14-row tiles (40 registers and about 100 bytes of spill, but 48 warps per
+// SM to cover the issue-bound loop: 0.826 against 0.926 ms at 512^3; four
+// CTAs, or three for FP32 words, ran 10-27 % slower).
+template <int RY, class S = void>
+constexpr int kMinCtas1 = RY == 30 ? 1 : (std::is_same<S, StoreF16>::value && RY == 14 ? 3 : 2);
 
 // Ring-stage layout of the per-component tile boxes (see Plan1): byte offset
 // of each hi and lo box, box rows, first box row and x shift per component.
@@ -607,7 +610,7 @@ __device__ __forceinline__ void init_ring(uint64_t* bar) {
 }
 
 template <class S, class A, int RY, int kApps, bool kDenseJ>
-__global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY>)
+__global__ void __launch_bounds__(32 * (RY + 2), kMinCtas1<RY, S>)
     fused1(PLayout L, S st, S out, const __grid_constant__ StepMaps maps, CoefSet cs, int kchunk, int2 zr,
            const float* __restrict__ Jx, const float* __restrict__ Jy, const float* __restrict__ Jz,
            SourceSet ss, int64_t step, WaitCtl wc) {
