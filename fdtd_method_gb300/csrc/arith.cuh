@@ -49,12 +49,34 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 
+// Differences with one FP16 operand, rounded once to FP32 (the sm_100
+// family's mixed-precision sub/fma): the same value as converting the half
+// first and subtracting in FP32, without the conversion instruction.
+// h - c:
+__device__ __forceinline__ float sub_h_f(__half h, float c) {
+  float d;
+  asm("sub.rn.f32.f16 %0, %1, %2;" : "=f"(d) : "h"(__half_as_ushort(h)), "f"(c));
+  return d;
+}
+// c - h, as h * (-1) + c (one rounding; a zero result is +0 exactly when
+// c - h gives +0):
+__device__ __forceinline__ float sub_f_h(float c, __half h) {
+  float d;
+  const unsigned short minus_one = 0xBC00u;
+  asm("fma.rn.f32.f16 %0, %1, %2, %3;" : "=f"(d) : "h"(__half_as_ushort(h)), "h"(minus_one), "f"(c));
+  return d;
+}
+
 struct ArithPlain {
   static constexpr bool kPairs = false;  // neighbours need only h
   // c1 (a1 - b1) - c2 (a2 - b2) with one FMA, written out so that every
   // kernel evaluates it identically.
   __device__ __forceinline__ static Pair curl(Coef c1, Pair a1, Pair b1, Coef c2, Pair a2, Pair b2) {
     return Pair{__fmaf_rn(c1.hi, __fsub_rn(a1.hi, b1.hi), -__fmul_rn(c2.hi, __fsub_rn(a2.hi, b2.hi))), 0.f};
+  }
+  // curl from its two differences d1 = a1 - b1, d2 = a2 - b2 (as curl forms them)
+  __device__ __forceinline__ static Pair curl_d(Coef c1, float d1, Coef c2, float d2) {
+    return Pair{__fmaf_rn(c1.hi, d1, -__fmul_rn(c2.hi, d2)), 0.f};
   }
   __device__ __forceinline__ static Pair add(Pair p, Pair q) { return Pair{__fadd_rn(p.hi, q.hi), 0.f}; }
   __device__ __forceinline__ static Pair twice(Pair t) { return Pair{2.f * t.hi, 0.f}; }

@@ -245,6 +245,7 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
   using HiT = typename S::HiT;
   using T = typename A::Cur;
   constexpr int NS = P::kNS;
+  constexpr bool kHalfWords = std::is_same<S, StoreF16>::value;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + P::kBar);
   int* list = reinterpret_cast<int*>(smem + P::kList);
 
@@ -355,9 +356,26 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
 
     // 1. B'(t), in the operation order of the B sweep (kernels_f32.cu b_column)
     const Pair ex = V(Comp<0>{}, 0, 0), ey = V(Comp<1>{}, 0, 0), ez = V(Comp<2>{}, 0, 0);
-    Pair ux = A::curl(bcoef<S>(cs, st, 0, 0), pey, ey, bcoef<S>(cs, st, 0, 1), V(Comp<2>{}, 1, 0), ez);
-    Pair uy = A::curl(bcoef<S>(cs, st, 1, 0), V(Comp<2>{}, 0, 1), ez, bcoef<S>(cs, st, 1, 1), pex, ex);
-    Pair uz = A::curl(bcoef<S>(cs, st, 2, 0), V(Comp<0>{}, 1, 0), ex, bcoef<S>(cs, st, 2, 1), V(Comp<1>{}, 0, 1), ey);
+    Pair ux, uy, uz;
+    if constexpr (kHalfWords) {
+      // FP16 words: a neighbour that enters one difference only enters it
+      // unconverted (sub_h_f: the same FP32 difference)
+      auto VH = [&](auto cc, int dr, int dc) -> HiT {
+        constexpr int c = decltype(cc)::value;
+        return H[P::template kHiAt<c> / P::HS + (r + dr - P::template kRow0<c>) * P::template kW<c> +
+                 P::template kXOff<c> + cx + dc];
+      };
+      ux = A::curl_d(bcoef<S>(cs, st, 0, 0), __fsub_rn(pey.hi, ey.hi), bcoef<S>(cs, st, 0, 1),
+                     sub_h_f(VH(Comp<2>{}, 1, 0), ez.hi));
+      uy = A::curl_d(bcoef<S>(cs, st, 1, 0), sub_h_f(VH(Comp<2>{}, 0, 1), ez.hi), bcoef<S>(cs, st, 1, 1),
+                     __fsub_rn(pex.hi, ex.hi));
+      uz = A::curl_d(bcoef<S>(cs, st, 2, 0), sub_h_f(VH(Comp<0>{}, 1, 0), ex.hi), bcoef<S>(cs, st, 2, 1),
+                     sub_h_f(VH(Comp<1>{}, 0, 1), ey.hi));
+    } else {
+      ux = A::curl(bcoef<S>(cs, st, 0, 0), pey, ey, bcoef<S>(cs, st, 0, 1), V(Comp<2>{}, 1, 0), ez);
+      uy = A::curl(bcoef<S>(cs, st, 1, 0), V(Comp<2>{}, 0, 1), ez, bcoef<S>(cs, st, 1, 1), pex, ex);
+      uz = A::curl(bcoef<S>(cs, st, 2, 0), V(Comp<0>{}, 1, 0), ex, bcoef<S>(cs, st, 2, 1), V(Comp<1>{}, 0, 1), ey);
+    }
     if (kApps == 2) {
       ux = A::twice(ux);
       uy = A::twice(uy);
@@ -396,9 +414,20 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
       auto Bn = [&](int c, int off) -> Pair {  // B'(t+1), component 3 + c
         return st.decode(3 + c, ph[c * P::kXComp + off], P::kLo ? pq[c * P::kXComp + off] : LoT(0));
       };
-      Pair qx = A::curl(ecoef<S>(cs, st, 0, 0), pbz, Bn(2, xo_down), ecoef<S>(cs, st, 0, 1), pby, nby);
-      Pair qy = A::curl(ecoef<S>(cs, st, 1, 0), pbx, nbx, ecoef<S>(cs, st, 1, 1), pbz, Bn(2, xo_left));
-      Pair qz = A::curl(ecoef<S>(cs, st, 2, 0), pby, Bn(1, xo_left), ecoef<S>(cs, st, 2, 1), pbx, Bn(0, xo_down));
+      Pair qx, qy, qz;
+      if constexpr (kHalfWords) {
+        auto BH = [&](int c, int off) -> HiT { return ph[c * P::kXComp + off]; };  // B'(t+1) word
+        qx = A::curl_d(ecoef<S>(cs, st, 0, 0), sub_f_h(pbz.hi, BH(2, xo_down)), ecoef<S>(cs, st, 0, 1),
+                       __fsub_rn(pby.hi, nby.hi));
+        qy = A::curl_d(ecoef<S>(cs, st, 1, 0), __fsub_rn(pbx.hi, nbx.hi), ecoef<S>(cs, st, 1, 1),
+                       sub_f_h(pbz.hi, BH(2, xo_left)));
+        qz = A::curl_d(ecoef<S>(cs, st, 2, 0), sub_f_h(pby.hi, BH(1, xo_left)), ecoef<S>(cs, st, 2, 1),
+                       sub_f_h(pbx.hi, BH(0, xo_down)));
+      } else {
+        qx = A::curl(ecoef<S>(cs, st, 0, 0), pbz, Bn(2, xo_down), ecoef<S>(cs, st, 0, 1), pby, nby);
+        qy = A::curl(ecoef<S>(cs, st, 1, 0), pbx, nbx, ecoef<S>(cs, st, 1, 1), pbz, Bn(2, xo_left));
+        qz = A::curl(ecoef<S>(cs, st, 2, 0), pby, Bn(1, xo_left), ecoef<S>(cs, st, 2, 1), pbx, Bn(0, xo_down));
+      }
       unsigned has = 0;  // E components that received current (their increment has a lo word)
       if (kDenseJ || kSrc) {
         T jv[3] = {A::cur_zero(), A::cur_zero(), A::cur_zero()};

@@ -153,6 +153,34 @@ def test_fused_step_equals_split_sweeps(prec, shape, tile_y, kchunk, cpt):
         np.testing.assert_array_equal(a[q], b[q], err_msg="component %d" % q)
 
 
+@pytest.mark.parametrize("prec", [Precision.FP32, Precision.FP32_COMP, Precision.FP16_SCALED])
+def test_fused_equals_split_with_signed_zeros(prec):
+    """Mostly-zero fields with negative zeros, and values too small for FP16
+    (stored as signed zeros): the fused and split pipelines give the same
+    bits, the signs of zero results included (a difference formed as
+    -(b - a) instead of a - b would flip them)."""
+    p = normalised_parameters(45, 23, 17)
+    rng = np.random.default_rng(12)
+    vals = []
+    for _ in range(6):
+        v = rng.standard_normal(p.cells) * 0.5
+        r = rng.random(p.cells)
+        v[r < 0.45] = 0.0
+        v[(r >= 0.45) & (r < 0.9)] = -0.0
+        v[(r >= 0.9) & (r < 0.95)] *= 1e-12
+        vals.append(v)
+    srcs = [sources.gaussian_pulse(p, (20, 11, 8), 1.0, 1.0, 20.0, 3.0, 4.0, 20, comp="z")]
+    for steps in (1, 3):
+        a = _run(p, prec, vals, srcs, steps, "split")
+        b = _run(p, prec, vals, srcs, steps, "fused", 14, 8, cpt=1)
+        if steps == 1:
+            assert any((x == 0).any() for x in a)  # zero results to compare
+        for q in range(6):
+            np.testing.assert_array_equal(np.ascontiguousarray(a[q]).view(np.uint64),
+                                          np.ascontiguousarray(b[q]).view(np.uint64),
+                                          err_msg="component %d after %d steps" % (q, steps))
+
+
 @pytest.mark.parametrize("cpt", [1, 2])
 @pytest.mark.parametrize("prec", [Precision.FP32, Precision.FP32_COMP])
 def test_fused_many_sources_and_dense_current(prec, cpt):
