@@ -67,6 +67,20 @@ __device__ __forceinline__ float sub_f_h(float c, __half h) {
   return d;
 }
 
+// The same with a BF16 operand (the compensated form's lo words): h - c and
+// c - h.
+__device__ __forceinline__ float sub_bf_f(uint16_t h, float c) {
+  float d;
+  asm("sub.rn.f32.bf16 %0, %1, %2;" : "=f"(d) : "h"(h), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float sub_f_bf(float c, uint16_t h) {
+  float d;
+  const unsigned short minus_one = 0xBF80u;
+  asm("fma.rn.f32.bf16 %0, %1, %2, %3;" : "=f"(d) : "h"(h), "h"(minus_one), "f"(c));
+  return d;
+}
+
 struct ArithPlain {
   static constexpr bool kPairs = false;  // neighbours need only h
   // c1 (a1 - b1) - c2 (a2 - b2) with one FMA, written out so that every
@@ -108,7 +122,10 @@ struct ArithComp {
   // relative to the increment, a small fraction of the field it is added
   // to; the accumulation (acc) is the compensated part.
   __device__ __forceinline__ static Pair curl(Coef c1, Pair a1, Pair b1, Coef c2, Pair a2, Pair b2) {
-    const float d1 = dif(a1, b1), d2 = dif(a2, b2);
+    return curl_d(c1, dif(a1, b1), c2, dif(a2, b2));
+  }
+  // curl from its two differences d1 = dif(a1, b1), d2 = dif(a2, b2)
+  __device__ __forceinline__ static Pair curl_d(Coef c1, float d1, Coef c2, float d2) {
     const float m = __fmaf_rn(c2.hi, d2, __fmul_rn(c2.lo, d2));
     return Pair{__fmaf_rn(c1.hi, d1, __fmaf_rn(c1.lo, d1, -m)), 0.f};
   }

@@ -371,6 +371,18 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
                      __fsub_rn(pex.hi, ex.hi));
       uz = A::curl_d(bcoef<S>(cs, st, 2, 0), sub_h_f(VH(Comp<0>{}, 1, 0), ex.hi), bcoef<S>(cs, st, 2, 1),
                      sub_h_f(VH(Comp<1>{}, 0, 1), ey.hi));
+    } else if constexpr (S::kComp) {
+      // compensated words: the same for a neighbour's BF16 lo word (sub_bf_f)
+      auto VN = [&](auto cc, int dr, int dc, const Pair& own) -> float {
+        constexpr int c = decltype(cc)::value;
+        const int row = r + dr - P::template kRow0<c>;
+        const float h = H[P::template kHiAt<c> / P::HS + row * P::template kW<c> + P::template kXOff<c> + cx + dc];
+        const LoT q = Q[P::template kLoAt<c> / P::LS + row * P::template kLW<c> + P::template kLXOff<c> + cx + dc];
+        return __fadd_rn(__fsub_rn(h, own.hi), sub_bf_f(q, own.lo));
+      };
+      ux = A::curl_d(bcoef<S>(cs, st, 0, 0), A::dif(pey, ey), bcoef<S>(cs, st, 0, 1), VN(Comp<2>{}, 1, 0, ez));
+      uy = A::curl_d(bcoef<S>(cs, st, 1, 0), VN(Comp<2>{}, 0, 1, ez), bcoef<S>(cs, st, 1, 1), A::dif(pex, ex));
+      uz = A::curl_d(bcoef<S>(cs, st, 2, 0), VN(Comp<0>{}, 1, 0, ex), bcoef<S>(cs, st, 2, 1), VN(Comp<1>{}, 0, 1, ey));
     } else {
       ux = A::curl(bcoef<S>(cs, st, 0, 0), pey, ey, bcoef<S>(cs, st, 0, 1), V(Comp<2>{}, 1, 0), ez);
       uy = A::curl(bcoef<S>(cs, st, 1, 0), V(Comp<2>{}, 0, 1), ez, bcoef<S>(cs, st, 1, 1), pex, ex);
@@ -423,6 +435,14 @@ __device__ __forceinline__ bool fused1b_planes(const PLayout& L, const S& st, co
                        sub_f_h(pbz.hi, BH(2, xo_left)));
         qz = A::curl_d(ecoef<S>(cs, st, 2, 0), sub_f_h(pby.hi, BH(1, xo_left)), ecoef<S>(cs, st, 2, 1),
                        sub_f_h(pbx.hi, BH(0, xo_down)));
+      } else if constexpr (S::kComp) {
+        // own pair minus a neighbour's B'(t+1) words (sub_f_bf on the lo word)
+        auto DN = [&](const Pair& own, int c, int off) -> float {
+          return __fadd_rn(__fsub_rn(own.hi, ph[c * P::kXComp + off]), sub_f_bf(own.lo, pq[c * P::kXComp + off]));
+        };
+        qx = A::curl_d(ecoef<S>(cs, st, 0, 0), DN(pbz, 2, xo_down), ecoef<S>(cs, st, 0, 1), A::dif(pby, nby));
+        qy = A::curl_d(ecoef<S>(cs, st, 1, 0), A::dif(pbx, nbx), ecoef<S>(cs, st, 1, 1), DN(pbz, 2, xo_left));
+        qz = A::curl_d(ecoef<S>(cs, st, 2, 0), DN(pby, 1, xo_left), ecoef<S>(cs, st, 2, 1), DN(pbx, 0, xo_down));
       } else {
         qx = A::curl(ecoef<S>(cs, st, 0, 0), pbz, Bn(2, xo_down), ecoef<S>(cs, st, 0, 1), pby, nby);
         qy = A::curl(ecoef<S>(cs, st, 1, 0), pbx, nbx, ecoef<S>(cs, st, 1, 1), pbz, Bn(2, xo_left));
