@@ -55,7 +55,7 @@ template <> struct ArithOf1<StoreF32C> { using type = ArithComp; };
 
 // Ring stages per storage form.  Three for the FP32 words (the compensated
 // form's 21.6 KB stages of a 14-row tile leave room for no more at two CTAs
-// per SM; plain FP32 measured 2-10 % slower with four or six), four for the
+// per SM; plain FP32 measured 1-14 % slower with four or six), four for the
 // FP16 words (8 KB stages; 0.8 % faster than three, and flat up to eight).
 template <class S>
 constexpr int kStages1 = sizeof(typename S::HiT) == 2 ? 4 : 3;
