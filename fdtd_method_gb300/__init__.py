@@ -9,10 +9,10 @@ Amazingkivas/FDTD_Method, behind the reference solver class's API.
 """
 from .fdtd import (FDTD, FDTD_PML, FDTDBatch, Axis, Component, Const, CurrentParameters, Field, FDTDError,  # noqa: F401
                    InvalidArgument, LogicError, OutOfMemory, Parameters, Precision,
-                   SelectedFields, SeparableSource)
+                   SelectedFields, SeparableSource, fp16_choose_exponents)
 from . import sources  # noqa: F401
 from .slabs import FDTDSlabs, Slab  # noqa: F401
 
 __all__ = ["FDTD", "FDTD_PML", "FDTDBatch", "Axis", "Component", "Const", "CurrentParameters", "Field", "FDTDError",
            "InvalidArgument", "LogicError", "OutOfMemory", "Parameters", "Precision",
-           "SelectedFields", "SeparableSource", "sources", "FDTDSlabs", "Slab"]
+           "SelectedFields", "SeparableSource", "fp16_choose_exponents", "sources", "FDTDSlabs", "Slab"]

@@ -96,6 +96,8 @@ SIGNATURES = {
     "fdtd_set_fp64_arith": [_H, ctypes.c_int],
     "fdtd_get_fp16_exponents": [_H, ctypes.POINTER(ctypes.c_int)],
     "fdtd_fp16_autoscale": [_H, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
+    "fdtd_fp16_choose_exponents": [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
     "fdtd_set_fp16_autoscale": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "fdtd_set_wait_limit": [_H, ctypes.c_int64, ctypes.c_int],
     "fdtd_set_temporal_depth": [_H, ctypes.c_int],

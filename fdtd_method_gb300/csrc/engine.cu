@@ -882,35 +882,48 @@ int step_sweeps(fdtd_handle* h, int64_t n) {
 // k_all) (a component with no field gets the bound).  `force` sets every
 // exponent to e*; otherwise a component is re-encoded when its exponent is
 // above the bound or 3 or more from e*.  Synchronous (reads six maxima).
+// The rule itself (host only): from the stored peaks m_c (FP32 values of
+// the stored halves' magnitudes) and the current exponents, the exponents
+// to re-encode to (equal to `cur` where nothing changes).
+void fp16_choose(const float peak[6], const int cur[6], int target, int headroom, bool force, int out[6]) {
+  int k[6];
+  bool has[6];
+  int k_all = INT_MIN;
+  for (int c = 0; c < 6; ++c) {
+    const float m = peak[c];
+    has[c] = m > 0.f && std::isfinite(m);
+    k[c] = has[c] ? (int)std::ceil(std::log2((double)m)) - cur[c] : 0;
+    if (has[c]) k_all = std::max(k_all, k[c]);
+  }
+  for (int c = 0; c < 6; ++c) {
+    out[c] = cur[c];
+    if (k_all == INT_MIN) continue;  // no field anywhere: nothing to go by
+    const int bound = target + headroom - k_all;
+    const int want = std::max(-60, std::min(60, has[c] ? std::min(target - k[c], bound) : bound));
+    if (!force && cur[c] <= bound && std::abs(want - cur[c]) < 3) continue;
+    out[c] = want;
+  }
+}
+
 int fp16_rescan(fdtd_handle* h, int target, int headroom, bool force, int out[6]) {
   unsigned* d_max = reinterpret_cast<unsigned*>(h->d_diag_out);
   FDTD_CUDA(launch_f16_absmax(h->L, h->view().s16, d_max, h->stream), "FP16 peak scan");
   unsigned bits[6];
   FDTD_CUDA(cudaMemcpyAsync(bits, d_max, sizeof(bits), cudaMemcpyDeviceToHost, h->stream), "FP16 peak scan");
   FDTD_CUDA(cudaStreamSynchronize(h->stream), "FP16 peak scan");
-  int k[6];
-  bool has[6];
-  int k_all = INT_MIN;
+  float peak[6];
+  std::memcpy(peak, bits, sizeof(peak));
+  int want[6];
+  fp16_choose(peak, h->fp16_exp, target, headroom, force, want);
   for (int c = 0; c < 6; ++c) {
-    float m;
-    std::memcpy(&m, &bits[c], sizeof(m));
-    has[c] = m > 0.f && std::isfinite(m);
-    k[c] = has[c] ? (int)std::ceil(std::log2((double)m)) - h->fp16_exp[c] : 0;
-    if (has[c]) k_all = std::max(k_all, k[c]);
-  }
-  for (int c = 0; c < 6; ++c) {
-    if (out) out[c] = h->fp16_exp[c];
-    if (k_all == INT_MIN) continue;  // no field anywhere: nothing to go by
-    const int bound = target + headroom - k_all;
-    const int want = std::max(-60, std::min(60, has[c] ? std::min(target - k[c], bound) : bound));
     const int cur = h->fp16_exp[c];
-    if (!force && cur <= bound && std::abs(want - cur) < 3) continue;
-    if (want == cur) continue;
-    FDTD_CUDA(launch_f16_rescale(static_cast<__half*>(h->field[c]), h->L.elems(), want - cur, h->stream),
-              "FP16 rescale");
-    h->fp16_exp[c] = want;
-    h->b_side = false;
-    if (out) out[c] = want;
+    if (want[c] != cur) {
+      FDTD_CUDA(launch_f16_rescale(static_cast<__half*>(h->field[c]), h->L.elems(), want[c] - cur, h->stream),
+                "FP16 rescale");
+      h->fp16_exp[c] = want[c];
+      h->b_side = false;
+    }
+    if (out) out[c] = h->fp16_exp[c];
   }
   return FDTD_OK;
 }
@@ -1346,6 +1359,17 @@ int fdtd_fp16_autoscale(fdtd_handle* h, int target_log2, int headroom_log2, int 
   DeviceGuard dg(h->device);
   if (int rc = fp16_rescan(h, target_log2, headroom_log2, true, exponents)) return rc;
   FDTD_CUDA(cudaStreamSynchronize(h->stream), "FP16 rescale");
+  return FDTD_OK;
+}
+
+int fdtd_fp16_choose_exponents(const float peaks[6], const int current[6], int target_log2, int headroom_log2,
+                               int force, int exponents[6]) {
+  if (!peaks || !current || !exponents) return fail(FDTD_ERR_INVALID_ARGUMENT, "null pointer");
+  if (target_log2 < 0 || target_log2 > 15) return fail(FDTD_ERR_INVALID_ARGUMENT, "target_log2 must be in [0, 15]");
+  if (headroom_log2 < 0 || headroom_log2 > 60) return fail(FDTD_ERR_INVALID_ARGUMENT, "headroom_log2 must be in [0, 60]");
+  for (int c = 0; c < 6; ++c)
+    if (current[c] < -60 || current[c] > 60) return fail(FDTD_ERR_INVALID_ARGUMENT, "exponents must be in [-60, 60]");
+  fp16_choose(peaks, current, target_log2, headroom_log2, force != 0, exponents);
   return FDTD_OK;
 }
 

@@ -64,6 +64,19 @@ class Precision(enum.IntEnum):
     FP16_SCALED = 3   # FP16 storage, power-of-two scale per component
 
 
+def fp16_choose_exponents(peaks, current, target_log2=10, headroom_log2=5, force=False):
+    """The FP16 form's exponent rule on the host (fdtd_fp16_choose_exponents):
+    from the six stored peaks (largest |stored value| per component; 0, Inf
+    or NaN count as no field) and the current exponents, the exponents a scan
+    re-encodes to."""
+    lib = _lib.load()
+    pk = (ctypes.c_float * 6)(*[float(v) for v in peaks])
+    cur = (ctypes.c_int * 6)(*[int(e) for e in current])
+    out = (ctypes.c_int * 6)()
+    _lib.check(lib.fdtd_fp16_choose_exponents(pk, cur, int(target_log2), int(headroom_log2), 1 if force else 0, out))
+    return list(out)
+
+
 @dataclass
 class Parameters:
     Ni: int

@@ -241,6 +241,13 @@ int fdtd_get_fp16_exponents(fdtd_handle* h, int exponents[6]);
  * synchronises the handle's stream. */
 int fdtd_fp16_autoscale(fdtd_handle* h, int target_log2, int headroom_log2, int exponents[6]);
 int fdtd_set_fp16_autoscale(fdtd_handle* h, int every_steps, int target_log2, int headroom_log2);
+/* The rule alone, on the host (no handle, no GPU): from the six stored peaks
+ * (the largest |stored value| per component; 0, Inf or NaN counts as no
+ * field) and the current exponents, the exponents a scan re-encodes to; a
+ * component keeps its exponent unless `force`, its exponent is above the
+ * bound, or the wanted one is 3 or more away.  No field anywhere: unchanged. */
+int fdtd_fp16_choose_exponents(const float peaks[6], const int current[6], int target_log2, int headroom_log2,
+                               int force, int exponents[6]);
 
 /* Kernel timing (new; for roofline accounting).  While enabled, every kernel
  * launch of the step pipeline is bracketed by CUDA events on the handle's
